@@ -1,0 +1,427 @@
+// extern "C" entry points: workspace planning and the launch sequences of the forward
+// pass, the forward-Laplacian local energy and the Metropolis-Hastings chain.
+#include "net.cuh"
+#include "mcmc.cuh"
+#include "gemm_tc.cuh"
+#include <string.h>
+#include <algorithm>
+
+namespace dw {
+
+// ------------------------------------------------------------------ prepared weights
+// Per iteration l: Wmain_l [kw_l, D] = rows of h_el_l.w for (h_one, conv_ee, conv_ei) and
+// Wmean_l [mw_l, D] = rows for (mean_up, mean_dn) (the spin means are identical for all
+// electrons of a walker, so their product is formed once per walker and channel).
+// Mixed precision additionally keeps BF16 K-major copies ([N, K]) for the tensor-core GEMMs.
+struct Prepared {
+    float* main[4]; float* mean[4];
+    __nv_bfloat16* main_bf[4]; __nv_bfloat16* mean_bf[4]; __nv_bfloat16* map_bf[4];
+    __nv_bfloat16* bf_up; __nv_bfloat16* bf_dn; __nv_bfloat16* jas0; __nv_bfloat16* jas1;
+    size_t bytes;
+};
+static inline int mean_width(const Dims& d, int l) { return round_up(2 * d.hw[l], 64); }
+
+static Prepared carve_prepared(const DwArch* a, int precision, void* base) {
+    Dims d = make_dims(a, false);
+    Carver c(base, (size_t)-1);
+    Prepared p;
+    memset(&p, 0, sizeof(p));
+    for (int l = 0; l < 4; ++l) {
+        p.main[l] = c.take<float>((size_t)d.kw[l] * d.D);
+        p.mean[l] = c.take<float>((size_t)mean_width(d, l) * d.D);
+    }
+    if (precision == DW_PRECISION_MIXED) {
+        for (int l = 0; l < 4; ++l) {
+            p.main_bf[l] = c.take<__nv_bfloat16>((size_t)d.kw[l] * d.D);
+            p.mean_bf[l] = c.take<__nv_bfloat16>((size_t)mean_width(d, l) * d.D);
+            p.map_bf[l] = c.take<__nv_bfloat16>((size_t)round_up(d.hw[l], 64) * d.E);
+        }
+        p.bf_up = c.take<__nv_bfloat16>((size_t)d.D * round_up(d.KN, 16));
+        p.bf_dn = c.take<__nv_bfloat16>((size_t)d.D * round_up(d.KN, 16));
+        p.jas0 = c.take<__nv_bfloat16>((size_t)d.D * d.J0);
+        p.jas1 = c.take<__nv_bfloat16>((size_t)d.J0 * d.J1);
+    }
+    p.bytes = c.used;
+    return p;
+}
+
+// Row gather for the prepared FP32 layer weights: mode 0 builds Wmain (rows h, conv_ee,
+// conv_ei of h_el_l.w), mode 1 builds Wmean (rows mean_up, mean_dn); other rows are zero.
+__global__ void k_gather_rows(const float* __restrict__ src, int cols, int rows, int hw, int nconv, int mode,
+                              float* __restrict__ dst) {
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)rows * cols) return;
+    int r = idx / cols, c = idx % cols;
+    int sr;
+    if (mode == 0) sr = r < hw ? r : (r < hw + nconv ? 2 * hw + r : -1);
+    else sr = r < 2 * hw ? hw + r : -1;
+    dst[idx] = sr >= 0 ? src[(int64_t)sr * cols + c] : 0.f;
+}
+// dstT[c][r] = bf16(src[r][c]) for r < rows_src, 0 for rows_src <= r < rows_pad; cols padded to cols_pad.
+__global__ void k_transpose_bf16(const float* __restrict__ src, int rows_src, int rows_pad, int cols, int cols_pad,
+                                 __nv_bfloat16* __restrict__ dst) {
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)rows_pad * cols_pad) return;
+    int c = idx / rows_pad, r = idx % rows_pad;
+    float v = (r < rows_src && c < cols) ? src[(int64_t)r * cols + c] : 0.f;
+    dst[idx] = __float2bfloat16_rn(v);
+}
+
+static int prepare(const DwArch* a, int precision, const float* P, void* prep, size_t bytes, cudaStream_t s) {
+    Dims d = make_dims(a, false);
+    ParamLayout L;
+    make_layout(a, &L);
+    Prepared p = carve_prepared(a, precision, prep);
+    if (p.bytes > bytes) return DW_ERR_WORKSPACE;
+    for (int l = 0; l < 4; ++l) {
+        for (int which = 0; which < 2; ++which) {
+            int rows = which == 0 ? d.kw[l] : mean_width(d, l);
+            float* dst = which == 0 ? p.main[l] : p.mean[l];
+            int64_t n = (int64_t)rows * d.D;
+            k_gather_rows<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P + L.h_el_w[l], d.D, rows, d.hw[l],
+                                                                     d.E + d.eiw[l], which, dst);
+            count_launch();
+        }
+    }
+    if (precision == DW_PRECISION_MIXED) {
+        auto tr = [&](const float* src, int rows_src, int rows_pad, int cols, int cols_pad, __nv_bfloat16* dst) {
+            int64_t n = (int64_t)rows_pad * cols_pad;
+            k_transpose_bf16<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, rows_src, rows_pad, cols, cols_pad, dst);
+            count_launch();
+        };
+        for (int l = 0; l < 4; ++l) {
+            tr(p.main[l], d.kw[l], d.kw[l], d.D, d.D, p.main_bf[l]);
+            tr(p.mean[l], mean_width(d, l), mean_width(d, l), d.D, d.D, p.mean_bf[l]);
+            tr(P + L.h_map_w[l], d.hw[l], round_up(d.hw[l], 64), d.E, d.E, p.map_bf[l]);
+        }
+        tr(P + L.bf_up, d.D, d.D, d.KN, round_up(d.KN, 16), p.bf_up);
+        tr(P + L.bf_dn, d.D, d.D, d.KN, round_up(d.KN, 16), p.bf_dn);
+        tr(P + L.jas_w[0], d.D, d.D, d.J0, d.J0, p.jas0);
+        tr(P + L.jas_w[1], d.J0, d.J0, d.J1, d.J1, p.jas1);
+    }
+    DW_CHECK_CUDA(cudaGetLastError());
+    return DW_OK;
+}
+
+// ------------------------------------------------------------------ forward plan
+template <class Act>
+struct Plan {
+    Dims d;
+    int Bc;             // walkers per chunk
+    int rows;           // Bc * n * Tp
+    float* him;
+    Act* X0; Act* XA; Act* XB;
+    Act* Mcat; float* WB; float* HM; float* Zb;
+    float* WP; float* HE;
+    float* BF; float* MO;
+    double* logdet; double* sign; float* Ainv; double* g; double* lapdet;
+    Act* J1; Act* J2; double* jas;
+    size_t bytes;
+};
+
+static const int kXW = 320;   // row width of the layer-1..3 inputs: 256 (h) + 32 (conv_ee) + 32 (conv_ei)
+
+template <class Act>
+static Plan<Act> carve_plan(const Dims& d, int Bc, void* ws) {
+    Carver c(ws, (size_t)-1);
+    Plan<Act> p;
+    p.d = d; p.Bc = Bc;
+    int64_t rows = (int64_t)Bc * d.n * d.Tp;
+    p.rows = (int)rows;
+    int mw = 0;
+    for (int l = 0; l < 4; ++l) mw = std::max(mw, mean_width(d, l));
+    int zw = std::max(std::max(d.D, d.J0), d.KN);
+    p.him = c.take<float>(4 * d.N * 32);
+    p.X0 = c.take<Act>(rows * d.kw[0]);
+    p.XA = c.take<Act>(rows * kXW);
+    p.XB = c.take<Act>(rows * kXW);
+    p.Mcat = c.take<Act>((int64_t)Bc * d.Tp * mw);
+    p.WB = c.take<float>((int64_t)Bc * d.Tp * d.D);
+    p.HM = c.take<float>(rows * d.E);
+    p.Zb = c.take<float>(rows * std::max(d.D, d.J0));
+    int pc = d.Tp > 1 ? 3 : 1, ec = d.Tp > 1 ? 5 : 1;
+    p.WP = c.take<float>((int64_t)4 * Bc * d.n * d.n * pc * 32);
+    p.HE = c.take<float>((int64_t)4 * Bc * d.n * d.N * ec * 32);
+    p.BF = c.take<float>(rows * d.KN);
+    p.MO = c.take<float>((int64_t)Bc * d.K * d.T * d.n * d.n);
+    p.logdet = c.take<double>((int64_t)Bc * d.K);
+    p.sign = c.take<double>((int64_t)Bc * d.K);
+    if (d.Tp > 1) {
+        p.Ainv = c.take<float>((int64_t)Bc * d.K * d.n * d.n);
+        p.g = c.take<double>((int64_t)Bc * d.K * 3 * d.n);
+        p.lapdet = c.take<double>((int64_t)Bc * d.K);
+    } else {
+        p.Ainv = nullptr; p.g = nullptr; p.lapdet = nullptr;
+    }
+    p.J1 = c.take<Act>(rows * d.J0);
+    p.J2 = c.take<Act>(rows * d.J1);
+    p.jas = c.take<double>((int64_t)Bc * d.Tp);
+    (void)zw;
+    p.bytes = c.used;
+    return p;
+}
+
+static const size_t kChunkBudget = (size_t)6 << 30;   // bytes of activations per walker chunk
+
+template <class Act>
+static int choose_chunk(const Dims& d, int B) {
+    size_t per = carve_plan<Act>(d, 1, nullptr).bytes;
+    int bc = (int)std::max<size_t>(1, kChunkBudget / std::max<size_t>(per, 1));
+    return std::min(bc, B);
+}
+
+// The forward (value or tangent) of one chunk of walkers.
+template <class Act>
+static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, const ParamLayout& L,
+                     const Prepared& pre, const float* r, const float* R, const int32_t* Z,
+                     float* lp, float* phase, float* E_loc, float* grad, cudaStream_t s) {
+    const Dims& d = p.d;
+    const int rows = Bc * d.n * d.Tp;
+    const bool tang = d.Tp > 1;
+    const bool tc = precision == DW_PRECISION_MIXED && tc_available();
+    launch_features<Act>(r, R, d, Bc, p.X0, s);
+    launch_streams(r, R, P, L, d, Bc, p.WP, p.HE, s);
+    Act* xin = p.X0;
+    int ldin = d.kw[0];
+    int pc = tang ? 3 : 1, ec = tang ? 5 : 1;
+    for (int l = 0; l < 4; ++l) {
+        Act* xout = (l % 2 == 0) ? p.XA : p.XB;
+        int hw = d.hw[l], mw = mean_width(d, l);
+        // (a) spin means and their per-walker contribution
+        launch_spin_means<Act>(xin, ldin, hw, d, Bc, p.Mcat, mw, s);
+        GemmEpi e1; e1.bias = P + L.h_el_b[l]; e1.Tp = d.Tp; e1.rows_per_walker = d.Tp;
+        if (tc) DW_CHECK(gemm_bf16_tc((const __nv_bfloat16*)p.Mcat, mw, pre.mean_bf[l], p.WB, d.D, Bc * d.Tp, d.D, mw, e1, s));
+        else gemm_f32((const float*)p.Mcat, mw, pre.mean[l], d.D, p.WB, d.D, Bc * d.Tp, d.D, mw, e1, 1, 0, 0, s);
+        // (b) h_map = tanh(h_one W + b)
+        GemmEpi e2; e2.bias = P + L.h_map_b[l]; e2.Tp = d.Tp; e2.rows_per_walker = d.n * d.Tp; e2.act = tang ? 0 : 1;
+        float* hm_pre = tang ? p.Zb : p.HM;
+        if (tc) DW_CHECK(gemm_bf16_tc((const __nv_bfloat16*)xin, ldin, pre.map_bf[l], hm_pre, d.E, rows, d.E, hw, e2, s));
+        else gemm_f32((const float*)xin, ldin, P + L.h_map_w[l], d.E, hm_pre, d.E, rows, d.E, hw, e2, 1, 0, 0, s);
+        if (tang) launch_tanh_fl<float>(p.Zb, d.E, d.E, Bc * d.n, d, p.HM, d.E, s);
+        // (c) SchNet convolutions into the input columns [hw, hw + E + eiw)
+        int64_t wp_plane = (int64_t)Bc * d.n * d.n * pc * 32, he_plane = (int64_t)Bc * d.n * d.N * ec * 32;
+        launch_conv<Act>(r, p.WP + l * wp_plane, p.HM, p.HE + l * he_plane, p.him + l * d.N * 32, d, l, Bc, xin, ldin, s);
+        // (d) h_el = tanh([h | conv_ee | conv_ei] W_main + per-walker mean term)
+        GemmEpi e3; e3.rowbias = p.WB; e3.ldrb = d.D; e3.Tp = d.Tp; e3.rows_per_walker = d.n * d.Tp; e3.act = tang ? 0 : 1;
+        float* zout = tang ? p.Zb : nullptr;
+        if (tang) {
+            if (tc) DW_CHECK(gemm_bf16_tc((const __nv_bfloat16*)xin, ldin, pre.main_bf[l], zout, d.D, rows, d.D, d.kw[l], e3, s));
+            else gemm_f32((const float*)xin, ldin, pre.main[l], d.D, zout, d.D, rows, d.D, d.kw[l], e3, 1, 0, 0, s);
+            launch_tanh_fl<Act>(p.Zb, d.D, d.D, Bc * d.n, d, xout, kXW, s);
+        } else {
+            if (tc) DW_CHECK(gemm_bf16_tc_act((const __nv_bfloat16*)xin, ldin, pre.main_bf[l], (__nv_bfloat16*)xout, kXW,
+                                              rows, d.D, d.kw[l], e3, s));
+            else gemm_f32((const float*)xin, ldin, pre.main[l], d.D, (float*)xout, kXW, rows, d.D, d.kw[l], e3, 1, 0, 0, s);
+        }
+        xin = xout;
+        ldin = kXW;
+    }
+    const Act* H = xin;   // final embedding, row width kXW
+    // backflow (envelope_orbitals.py:46-75): up-electron rows x W_up, down-electron rows x W_dn
+    GemmEpi e0; e0.Tp = d.Tp; e0.rows_per_walker = d.n * d.Tp;
+    int64_t sA = (int64_t)d.n * d.Tp * kXW, sC = (int64_t)d.n * d.Tp * d.KN;
+    if (tc) {
+        DW_CHECK(gemm_bf16_tc_batched((const __nv_bfloat16*)H, kXW, pre.bf_up, p.BF, d.KN, d.nu * d.Tp, d.KN, d.D, Bc, sA, sC, s));
+        DW_CHECK(gemm_bf16_tc_batched((const __nv_bfloat16*)H + (int64_t)d.nu * d.Tp * kXW, kXW, pre.bf_dn,
+                                      p.BF + (int64_t)d.nu * d.Tp * d.KN, d.KN, d.nd * d.Tp, d.KN, d.D, Bc, sA, sC, s));
+    } else {
+        gemm_f32((const float*)H, kXW, P + L.bf_up, d.KN, p.BF, d.KN, d.nu * d.Tp, d.KN, d.D, e0, Bc, sA, sC, s);
+        gemm_f32((const float*)H + (int64_t)d.nu * d.Tp * kXW, kXW, P + L.bf_dn, d.KN, p.BF + (int64_t)d.nu * d.Tp * d.KN,
+                 d.KN, d.nd * d.Tp, d.KN, d.D, e0, Bc, sA, sC, s);
+    }
+    launch_envelope(r, R, P, L, d, Bc, p.BF, d.KN, p.MO, s);
+    if (precision == DW_PRECISION_MIXED) launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s);
+    else launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s);
+    if (tang) launch_det_tangents(p.MO, p.Ainv, p.sign, d, Bc, p.g, p.lapdet, s);
+    // Jastrow MLP([64, 64, 1]) on the final embedding
+    GemmEpi j0; j0.bias = P + L.jas_b[0]; j0.Tp = d.Tp; j0.rows_per_walker = d.n * d.Tp; j0.act = tang ? 0 : 1;
+    GemmEpi j1 = j0; j1.bias = P + L.jas_b[1];
+    if (tang) {
+        if (tc) DW_CHECK(gemm_bf16_tc((const __nv_bfloat16*)H, kXW, pre.jas0, p.Zb, d.J0, rows, d.J0, d.D, j0, s));
+        else gemm_f32((const float*)H, kXW, P + L.jas_w[0], d.J0, p.Zb, d.J0, rows, d.J0, d.D, j0, 1, 0, 0, s);
+        launch_tanh_fl<Act>(p.Zb, d.J0, d.J0, Bc * d.n, d, p.J1, d.J0, s);
+        if (tc) DW_CHECK(gemm_bf16_tc((const __nv_bfloat16*)p.J1, d.J0, pre.jas1, p.Zb, d.J1, rows, d.J1, d.J0, j1, s));
+        else gemm_f32((const float*)p.J1, d.J0, P + L.jas_w[1], d.J1, p.Zb, d.J1, rows, d.J1, d.J0, j1, 1, 0, 0, s);
+        launch_tanh_fl<Act>(p.Zb, d.J1, d.J1, Bc * d.n, d, p.J2, d.J1, s);
+    } else {
+        if (tc) {
+            DW_CHECK(gemm_bf16_tc_act((const __nv_bfloat16*)H, kXW, pre.jas0, (__nv_bfloat16*)p.J1, d.J0, rows, d.J0, d.D, j0, s));
+            DW_CHECK(gemm_bf16_tc_act((const __nv_bfloat16*)p.J1, d.J0, pre.jas1, (__nv_bfloat16*)p.J2, d.J1, rows, d.J1, d.J0, j1, s));
+        } else {
+            gemm_f32((const float*)H, kXW, P + L.jas_w[0], d.J0, (float*)p.J1, d.J0, rows, d.J0, d.D, j0, 1, 0, 0, s);
+            gemm_f32((const float*)p.J1, d.J0, P + L.jas_w[1], d.J1, (float*)p.J2, d.J1, rows, d.J1, d.J0, j1, 1, 0, 0, s);
+        }
+    }
+    launch_jastrow_out<Act>(p.J2, d.J1, P + L.jas_w[2], d, Bc, p.jas, s);
+    launch_combine(p.logdet, p.sign, p.g, p.lapdet, p.jas, r, R, Z, d, Bc, lp, phase, E_loc, grad, s);
+    DW_CHECK_CUDA(cudaGetLastError());
+    return DW_OK;
+}
+
+static bool uses_bf16_acts(int precision) { return precision == DW_PRECISION_MIXED && tc_available(); }
+
+template <class Act>
+static size_t ws_bytes_t(const DwArch* a, int n_walkers, int mode) {
+    Dims d = make_dims(a, mode == 1);
+    int bc = choose_chunk<Act>(d, std::max(n_walkers, 1));
+    size_t b = carve_plan<Act>(d, bc, nullptr).bytes + 4096;
+    if (mode == 2) {
+        Dims dv = make_dims(a, false);
+        int bcv = choose_chunk<Act>(dv, std::max(n_walkers, 1));
+        b = carve_plan<Act>(dv, bcv, nullptr).bytes + 4096;
+        b += (size_t)n_walkers * a->n_el * 3 * sizeof(float) + 256;      // proposals
+        b += (size_t)n_walkers * sizeof(float) + 256;                    // proposal log psi^2
+        b += (size_t)mh_partials_needed(n_walkers) * sizeof(int) + 256;
+    }
+    return b;
+}
+
+template <class Act>
+static int forward_all(const DwArch* a, int precision, const float* P, const void* prepared, const float* r, int B,
+                       const float* R, const int32_t* Z, float* lp, float* phase, float* E, float* grad, bool tang,
+                       void* ws, size_t ws_bytes, cudaStream_t s) {
+    Dims d = make_dims(a, tang);
+    ParamLayout L;
+    make_layout(a, &L);
+    Prepared pre = carve_prepared(a, precision, const_cast<void*>(prepared));
+    int bc = choose_chunk<Act>(d, B);
+    Plan<Act> p = carve_plan<Act>(d, bc, ws);
+    if (p.bytes > ws_bytes) return DW_ERR_WORKSPACE;
+    launch_ion_maps(P, L, d, Z, p.him, s);
+    for (int b0 = 0; b0 < B; b0 += bc) {
+        int nb = std::min(bc, B - b0);
+        DW_CHECK(run_chunk<Act>(p, nb, precision, P, L, pre, r + (int64_t)b0 * d.n * 3, R, Z, lp + b0,
+                                phase ? phase + b0 : nullptr, E ? E + b0 : nullptr,
+                                grad ? grad + (int64_t)b0 * 3 * d.n : nullptr, s));
+    }
+    return DW_OK;
+}
+
+}  // namespace dw
+
+using namespace dw;
+
+extern "C" {
+
+size_t dw_prepared_bytes(const DwArch* a, int precision) {
+    if (check_arch(a) != DW_OK) return 0;
+    return carve_prepared(a, precision, nullptr).bytes + 256;
+}
+
+int dw_prepare_params(const DwArch* a, int precision, const float* params, void* prepared, size_t bytes, void* stream) {
+    reset_launch_count();
+    DW_CHECK(check_arch(a));
+    if (!params || !prepared) return DW_ERR_ARG;
+    if (precision != DW_PRECISION_FP32 && precision != DW_PRECISION_MIXED) return DW_ERR_ARG;
+    return prepare(a, precision, params, prepared, bytes, (cudaStream_t)stream);
+}
+
+size_t dw_workspace_bytes(const DwArch* a, int precision, int n_walkers, int mode) {
+    if (check_arch(a) != DW_OK || n_walkers <= 0) return 0;
+    if (uses_bf16_acts(precision)) return ws_bytes_t<__nv_bfloat16>(a, n_walkers, mode);
+    return ws_bytes_t<float>(a, n_walkers, mode);
+}
+
+int dw_log_psi_sqr(const DwArch* a, int precision, const float* params, const void* prepared, const float* r,
+                   int B, const float* R, const int32_t* Z, float* lp, float* phase, void* ws, size_t wsb, void* stream) {
+    reset_launch_count();
+    DW_CHECK(check_arch(a));
+    if (!params || !prepared || !r || !R || !Z || !lp || B <= 0) return DW_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (uses_bf16_acts(precision))
+        return forward_all<__nv_bfloat16>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s);
+    return forward_all<float>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s);
+}
+
+int dw_local_energy(const DwArch* a, int precision, const float* params, const void* prepared, const float* r, int B,
+                    const float* R, const int32_t* Z, float* E, float* lp, float* grad, void* ws, size_t wsb, void* stream) {
+    reset_launch_count();
+    DW_CHECK(check_arch(a));
+    if (!params || !prepared || !r || !R || !Z || !E || B <= 0) return DW_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    // log psi^2 output is optional; route it to the workspace tail when absent
+    Carver c(ws, wsb);
+    size_t plan_bytes = uses_bf16_acts(precision) ? carve_plan<__nv_bfloat16>(make_dims(a, true), choose_chunk<__nv_bfloat16>(make_dims(a, true), B), nullptr).bytes
+                                                   : carve_plan<float>(make_dims(a, true), choose_chunk<float>(make_dims(a, true), B), nullptr).bytes;
+    if (!lp) {
+        if (plan_bytes + (size_t)B * sizeof(float) + 512 > wsb) return DW_ERR_WORKSPACE;
+        lp = reinterpret_cast<float*>(static_cast<char*>(ws) + (plan_bytes + 255) / 256 * 256);
+        wsb = plan_bytes;
+    }
+    if (uses_bf16_acts(precision))
+        return forward_all<__nv_bfloat16>(a, precision, params, prepared, r, B, R, Z, lp, nullptr, E, grad, true, ws, wsb, s);
+    return forward_all<float>(a, precision, params, prepared, r, B, R, Z, lp, nullptr, E, grad, true, ws, wsb, s);
+}
+
+int dw_potential_energy(const float* r, int B, int n, const float* R, const int32_t* Z, int N, float* E, void* stream) {
+    reset_launch_count();
+    if (!r || !R || !Z || !E || B <= 0 || n <= 0 || N <= 0) return DW_ERR_ARG;
+    launch_coulomb(r, B, n, R, Z, N, E, (cudaStream_t)stream);
+    DW_CHECK_CUDA(cudaGetLastError());
+    return DW_OK;
+}
+
+int dw_mcmc_steps(const DwArch* a, int precision, const float* params, const void* prepared, float* r, int B,
+                  const float* R, const int32_t* Z, float* lp, int32_t* age, DwMcmcScalars* scalars,
+                  const DwMcmcConfig* cfg, void* ws, size_t wsb, void* stream) {
+    reset_launch_count();
+    DW_CHECK(check_arch(a));
+    if (!params || !prepared || !r || !R || !Z || !lp || !age || !scalars || !cfg || B <= 0) return DW_ERR_ARG;
+    if (cfg->n_steps < 0) return DW_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    bool bf = uses_bf16_acts(precision);
+    Dims dv = make_dims(a, false);
+    size_t fwd = bf ? carve_plan<__nv_bfloat16>(dv, choose_chunk<__nv_bfloat16>(dv, B), nullptr).bytes
+                    : carve_plan<float>(dv, choose_chunk<float>(dv, B), nullptr).bytes;
+    fwd = (fwd + 4096 + 255) / 256 * 256;
+    if (wsb < dw_workspace_bytes(a, precision, B, 2)) return DW_ERR_WORKSPACE;
+    char* tail = static_cast<char*>(ws) + fwd;
+    Carver c(tail, wsb - fwd);
+    float* r_prop = c.take<float>((size_t)B * a->n_el * 3);
+    float* lp_prop = c.take<float>((size_t)B);
+    int* partials = c.take<int>((size_t)mh_partials_needed(B));
+    if (!c.ok()) return DW_ERR_WORKSPACE;
+    auto fwd_call = [&](const float* rr, float* out) {
+        if (bf) return forward_all<__nv_bfloat16>(a, precision, params, prepared, rr, B, R, Z, out, nullptr, nullptr, nullptr, false, ws, fwd, s);
+        return forward_all<float>(a, precision, params, prepared, rr, B, R, Z, out, nullptr, nullptr, nullptr, false, ws, fwd, s);
+    };
+    int64_t launches = 0;
+    if (cfg->reevaluate) { DW_CHECK(fwd_call(r, lp)); launches += launch_count(); }   // mcmc.py:396
+    if (cfg->n_steps == 0) return DW_OK;
+    MhArgs m;
+    m.r = r; m.r_prop = r_prop; m.lp = lp; m.lp_prop = lp_prop; m.age = age; m.scalars = scalars; m.partials = partials;
+    m.B = B; m.n = a->n_el; m.max_age = cfg->max_age; m.interval = cfg->stepsize_update_interval;
+    m.target = cfg->target_acceptance_rate; m.min_step = cfg->min_stepsize; m.max_step = cfg->max_stepsize; m.seed = cfg->seed;
+    reset_launch_count();
+    launch_mh(m, 0, s);
+    launches += launch_count();
+    for (int k = 0; k < cfg->n_steps; ++k) {
+        reset_launch_count();
+        DW_CHECK(fwd_call(r_prop, lp_prop));
+        launch_mh(m, k + 1 < cfg->n_steps ? 1 : 2, s);
+        launches += launch_count();
+    }
+    reset_launch_count();
+    count_launch((int)launches);
+    DW_CHECK_CUDA(cudaGetLastError());
+    return DW_OK;
+}
+
+int dw_energy_stats(const float* E, int n, double* out, void* stream) {
+    reset_launch_count();
+    if (!E || !out || n <= 0) return DW_ERR_ARG;
+    launch_stats(E, n, 0, 0.0, 1.0, 1.0, nullptr, out, (cudaStream_t)stream);
+    DW_CHECK_CUDA(cudaGetLastError());
+    return DW_OK;
+}
+
+int dw_clip_energies(const float* E, int n, double center, double width, double clip_by, float* E_clip, double* out,
+                     void* stream) {
+    reset_launch_count();
+    if (!E || !out || !E_clip || n <= 0 || !(width > 0)) return DW_ERR_ARG;
+    launch_stats(E, n, 1, center, width, clip_by, E_clip, out, (cudaStream_t)stream);
+    DW_CHECK_CUDA(cudaGetLastError());
+    return DW_OK;
+}
+
+}  // extern "C"

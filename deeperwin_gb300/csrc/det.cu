@@ -1,0 +1,256 @@
+// Determinants, their forward-mode derivatives, the multi-determinant combine, the
+// Jastrow add, the kinetic energy and the Coulomb potential.
+#include "net.cuh"
+
+namespace dw {
+
+// ------------------------------------------------------------------ slogdet (+ inverse)
+// One warp per (walker, determinant). Gauss-Jordan elimination with partial pivoting
+// (first maximal |pivot| wins, as LAPACK getrf) on [A | I] in scalar type S; in value-only
+// mode an LU elimination on A alone. Mirrors jnp.linalg.slogdet in
+// evaluate_sum_of_determinants (model/wavefunction.py:63-73).
+template <class S>
+__global__ void k_slogdet(const float* __restrict__ MO, int n, int T, int nmat, int want_inv,
+                          double* __restrict__ logdet, double* __restrict__ sign, float* __restrict__ Ainv) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    const int mat = blockIdx.x * wpb + wid;
+    if (mat >= nmat) return;
+    const int nc = want_inv ? 2 * n : n;
+    S* M = reinterpret_cast<S*>(smem_raw) + (size_t)wid * n * nc;
+    const float* A = MO + (int64_t)mat * T * n * n;      // channel 0 of this (walker, det)
+    for (int e = lane; e < n * nc; e += 32) {
+        int r = e / nc, c = e % nc;
+        M[e] = c < n ? (S)A[r * n + c] : (S)((c - n) == r ? 1 : 0);
+    }
+    __syncwarp();
+    double ld = 0.0, sg = 1.0;
+    bool singular = false;
+    for (int c = 0; c < n; ++c) {
+        // pivot search over rows c..n-1
+        S best = (S)-1; int bi = n;
+        for (int r = c + lane; r < n; r += 32) {
+            S v = M[r * nc + c]; v = v < 0 ? -v : v;
+            if (v > best) { best = v; bi = r; }
+        }
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            S ob = __shfl_xor_sync(0xffffffffu, best, o);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (!(best > (S)0)) { singular = true; break; }
+        if (bi != c) {
+            for (int j = lane; j < nc; j += 32) {
+                S t = M[c * nc + j]; M[c * nc + j] = M[bi * nc + j]; M[bi * nc + j] = t;
+            }
+            sg = -sg;
+            __syncwarp();
+        }
+        S piv = M[c * nc + c];
+        ld += log(fabs((double)piv));
+        if (piv < (S)0) sg = -sg;
+        S inv = (S)1 / piv;
+        for (int j = c + 1 + lane; j < nc; j += 32) M[c * nc + j] *= inv;
+        __syncwarp();
+        int r0 = want_inv ? 0 : c + 1;
+        for (int r = r0; r < n; ++r) {
+            if (r == c) continue;
+            S f = M[r * nc + c];
+            if (f != (S)0)
+                for (int j = c + 1 + lane; j < nc; j += 32) M[r * nc + j] -= f * M[c * nc + j];
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        logdet[mat] = singular ? -INFINITY : ld;
+        sign[mat] = singular ? 0.0 : sg;
+    }
+    if (want_inv) {
+        float* out = Ainv + (int64_t)mat * n * n;
+        for (int e = lane; e < n * n; e += 32) {
+            int r = e / n, c = e % n;
+            out[e] = singular ? 0.f : (float)M[r * nc + n + c];
+        }
+    }
+}
+
+template <class S>
+void launch_slogdet(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, cudaStream_t s) {
+    int n = d.n, want_inv = d.Tp > 1 ? 1 : 0;
+    int nc = want_inv ? 2 * n : n;
+    size_t per = (size_t)n * nc * sizeof(S);
+    int wpb = (int)(96 * 1024 / per);
+    wpb = wpb < 1 ? 1 : (wpb > 8 ? 8 : wpb);
+    int nmat = B * d.K;
+    size_t sm = per * wpb;
+    if (sm > 48 * 1024) cudaFuncSetAttribute(k_slogdet<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_slogdet<S><<<(nmat + wpb - 1) / wpb, wpb * 32, sm, s>>>(MO, n, d.T, nmat, want_inv, logdet, sign, Ainv);
+    count_launch();
+}
+template void launch_slogdet<float>(const float*, const Dims&, int, double*, double*, float*, cudaStream_t);
+template void launch_slogdet<double>(const float*, const Dims&, int, double*, double*, float*, cudaStream_t);
+
+// ------------------------------------------------------------------ determinant tangents
+// g_t = tr(A^-1 dA_t), lap = tr(A^-1 Lap A) - sum_t tr((A^-1 dA_t)^2), traces accumulated in FP64.
+__global__ void k_det_tangents(const float* __restrict__ MO, const float* __restrict__ Ainv,
+                               const double* __restrict__ sign, int n, int T, int nmat,
+                               double* __restrict__ g, double* __restrict__ lapdet) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* Ai = reinterpret_cast<float*>(smem_raw);
+    float* dA = Ai + n * n;
+    float* C = dA + n * n;
+    __shared__ double red[2][32];
+    const int mat = blockIdx.x;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (sign[mat] == 0.0) {
+        for (int t = tid; t < 3 * n; t += nt) g[(int64_t)mat * 3 * n + t] = 0.0;
+        if (tid == 0) lapdet[mat] = 0.0;
+        return;
+    }
+    for (int e = tid; e < n * n; e += nt) Ai[e] = Ainv[(int64_t)mat * n * n + e];
+    double lap_acc = 0.0;
+    for (int t = 1; t < T; ++t) {
+        const float* src = MO + ((int64_t)mat * T + t) * n * n;
+        __syncthreads();
+        for (int e = tid; e < n * n; e += nt) dA[e] = src[e];
+        __syncthreads();
+        double tr = 0.0, tr2 = 0.0;
+        for (int e = tid; e < n * n; e += nt) {
+            int a = e / n, c = e % n;
+            float acc = 0.f;
+            for (int m = 0; m < n; ++m) acc = fmaf(Ai[a * n + m], dA[m * n + c], acc);
+            C[e] = acc;
+            if (a == c) tr += acc;
+        }
+        __syncthreads();
+        if (t != T - 1) {
+            for (int e = tid; e < n * n; e += nt) {
+                int a = e / n, c = e % n;
+                tr2 += (double)C[a * n + c] * (double)C[c * n + a];
+            }
+        }
+        tr = warp_sum(tr); tr2 = warp_sum(tr2);
+        if ((tid & 31) == 0) { red[0][tid >> 5] = tr; red[1][tid >> 5] = tr2; }
+        __syncthreads();
+        if (tid == 0) {
+            double s0 = 0, s1 = 0;
+            for (int w = 0; w < (nt + 31) / 32; ++w) { s0 += red[0][w]; s1 += red[1][w]; }
+            if (t == T - 1) lap_acc += s0;
+            else { g[(int64_t)mat * 3 * n + (t - 1)] = s0; lap_acc -= s1; }
+        }
+    }
+    if (tid == 0) lapdet[mat] = lap_acc;
+}
+
+void launch_det_tangents(const float* MO, const float* Ainv, const double* sign, const Dims& d, int B,
+                         double* g, double* lapdet, cudaStream_t s) {
+    int nmat = B * d.K;
+    size_t sm = 3 * (size_t)d.n * d.n * sizeof(float);
+    if (sm > 48 * 1024) cudaFuncSetAttribute(k_det_tangents, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_det_tangents<<<nmat, 128, sm, s>>>(MO, Ainv, sign, d.n, d.T, nmat, g, lapdet);
+    count_launch();
+}
+
+// ------------------------------------------------------------------ Coulomb (hamiltonian.py:17-39)
+__device__ double coulomb_walker(const float* rb, int n, const float* R, const int32_t* Z, int N, int lane) {
+    double e = 0.0;
+    for (int p = lane; p < n * n; p += 32) {
+        int i = p / n, j = p % n;
+        if (j <= i) continue;
+        double dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
+        e += 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    for (int p = lane; p < n * N; p += 32) {
+        int i = p / N, I = p % N;
+        double dx = rb[i * 3] - R[I * 3], dy = rb[i * 3 + 1] - R[I * 3 + 1], dz = rb[i * 3 + 2] - R[I * 3 + 2];
+        e -= (double)Z[I] / sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    for (int p = lane; p < N * N; p += 32) {
+        int I = p / N, J = p % N;
+        if (J <= I) continue;
+        double dx = R[J * 3] - R[I * 3], dy = R[J * 3 + 1] - R[I * 3 + 1], dz = R[J * 3 + 2] - R[I * 3 + 2];
+        e += (double)Z[I] * Z[J] / sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    return warp_sum(e);
+}
+
+__global__ void k_coulomb(const float* __restrict__ r, int B, int n, const float* __restrict__ R,
+                          const int32_t* __restrict__ Z, int N, float* __restrict__ E) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= B) return;
+    double e = coulomb_walker(r + (int64_t)warp * n * 3, n, R, Z, N, lane);
+    if (lane == 0) E[warp] = (float)e;
+}
+
+void launch_coulomb(const float* r, int B, int n, const float* R, const int32_t* Z, int N, float* E, cudaStream_t s) {
+    k_coulomb<<<(B * 32 + 255) / 256, 256, 0, s>>>(r, B, n, R, Z, N, E);
+    count_launch();
+}
+
+// ------------------------------------------------------------------ combine
+// log psi^2 = 2 (log(|sum_k s_k e^{l_k - l_max}| + 1e-8) + l_max) + J   (wavefunction.py:77-81, :127-128)
+// With tangents: grad/Laplacian of f = log(|psi~| + eps) + l_{k*} (k* = argmax), all in FP64;
+// E_kin = -1/2 (1/2 Lap log psi^2 + 1/4 |grad log psi^2|^2) (hamiltonian.py:216).
+__global__ void k_combine(const double* __restrict__ logdet, const double* __restrict__ sign,
+                          const double* __restrict__ g, const double* __restrict__ lapdet,
+                          const double* __restrict__ jas, const float* __restrict__ r, const float* __restrict__ R,
+                          const int32_t* __restrict__ Z, Dims d, int B, float* __restrict__ log_psi_sqr,
+                          float* __restrict__ phase, float* __restrict__ E_loc, float* __restrict__ grad_out) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= B) return;
+    const int b = warp, K = d.K, n3 = 3 * d.n;
+    const double* ld = logdet + (int64_t)b * K;
+    const double* sg = sign + (int64_t)b * K;
+    double lmax = -INFINITY; int ks = 0;
+    for (int k = 0; k < K; ++k) if (ld[k] > lmax) { lmax = ld[k]; ks = k; }
+    double psi = 0.0;
+    for (int k = 0; k < K; ++k) psi += sg[k] * exp(ld[k] - lmax);
+    const double eps = 1e-8;
+    double u = fabs(psi), sgn = psi < 0 ? -1.0 : 1.0;
+    double f = log(u + eps) + lmax;
+    const double* jb = jas + (int64_t)b * d.Tp;
+    if (lane == 0) {
+        log_psi_sqr[b] = (float)(2.0 * f + jb[0]);
+        if (phase) phase[b] = psi < 0 ? 3.14159265358979323846f : 0.f;
+    }
+    if (d.Tp == 1) return;
+    // tangents
+    const double* gb = g + (int64_t)b * K * n3;
+    const double* gs = gb + (int64_t)ks * n3;
+    double grad_sq = 0.0, gpsi_sq = 0.0;
+    // lane-parallel over coordinates
+    for (int t = lane; t < n3; t += 32) {
+        double gp = 0.0;
+        for (int k = 0; k < K; ++k) gp += sg[k] * exp(ld[k] - lmax) * (gb[(int64_t)k * n3 + t] - gs[t]);
+        double gf = sgn * gp / (u + eps) + gs[t];
+        double gl = 2.0 * gf + jb[1 + t];
+        grad_sq += gl * gl;
+        gpsi_sq += gp * gp;
+        if (grad_out) grad_out[(int64_t)b * n3 + t] = (float)gl;
+    }
+    // Laplacian of psi~
+    double lp = 0.0;
+    for (int k = lane; k < K; k += 32) {
+        double a = sg[k] * exp(ld[k] - lmax);
+        double dg2 = 0.0;
+        for (int t = 0; t < n3; ++t) { double dd = gb[(int64_t)k * n3 + t] - gs[t]; dg2 += dd * dd; }
+        lp += a * ((lapdet[(int64_t)b * K + k] - lapdet[(int64_t)b * K + ks]) + dg2);
+    }
+    grad_sq = warp_sum(grad_sq); gpsi_sq = warp_sum(gpsi_sq); lp = warp_sum(lp);
+    double lapf = sgn * lp / (u + eps) - gpsi_sq / ((u + eps) * (u + eps)) + lapdet[(int64_t)b * K + ks];
+    double lap = 2.0 * lapf + jb[d.lap];
+    double ekin = -0.5 * (0.5 * lap + 0.25 * grad_sq);
+    double epot = coulomb_walker(r + (int64_t)b * d.n * 3, d.n, R, Z, d.N, lane);
+    if (lane == 0) E_loc[b] = (float)(ekin + epot);
+}
+
+void launch_combine(const double* logdet, const double* sign, const double* g, const double* lapdet, const double* jas,
+                    const float* r, const float* R, const int32_t* Z, const Dims& d, int B,
+                    float* log_psi_sqr, float* phase, float* E_loc, float* grad_out, cudaStream_t s) {
+    k_combine<<<(B * 32 + 255) / 256, 256, 0, s>>>(logdet, sign, g, lapdet, jas, r, R, Z, d, B, log_psi_sqr, phase,
+                                                   E_loc, grad_out);
+    count_launch();
+}
+
+}  // namespace dw

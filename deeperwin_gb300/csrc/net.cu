@@ -1,0 +1,407 @@
+// Per-walker network kernels of the dpe4 wavefunction with forward-mode Laplacian.
+//
+// Channel convention for every per-electron tensor X[(b, i, t), col] (rows ordered walker,
+// electron, channel; Tp rows per electron):
+//   t = 0            value
+//   t = 1 + 3m + c   d/d r_{m,c}   (m = electron, c = x,y,z)
+//   t = 3n + 1       Laplacian over all 3n coordinates
+//   t > 3n + 1       zero padding up to Tp (a power of two)
+// In value-only mode Tp = 1.
+//
+// The 2-el streams depend on r only through d_ij = |r_j - r_i|, so they are carried in
+// 1-D Taylor form (f, df/dd, d2f/dd2) and expanded to the 3n channels where they are
+// contracted (SchNet convolution). The el-ion streams depend on r_i - R_I only and carry
+// (value, 3 gradients w.r.t. r_i, Laplacian w.r.t. r_i).
+#include "common.cuh"
+#include "net.cuh"
+
+namespace dw {
+
+// ------------------------------------------------------------------ ion maps (constant per geometry)
+// him[l][I][f] = tanh(Embed(Z_I - z_min) @ W_ion_map_l + b)   (ferminet_embedding.py:172-174,
+// input_features.py:184-191)
+__global__ void k_ion_maps(const float* __restrict__ P, ParamLayout L, Dims d, const int32_t* __restrict__ Z,
+                           float* __restrict__ him) {
+    for (int idx = threadIdx.x; idx < 4 * d.N * 32; idx += blockDim.x) {
+        int l = idx / (d.N * 32), rem = idx % (d.N * 32), I = rem / 32, f = rem % 32;
+        float v = 0.f;
+        if (f < d.eiw[l]) {
+            int z = Z[I] - d.zmin;
+            z = z < 0 ? 0 : (z > d.zmax - d.zmin ? d.zmax - d.zmin : z);
+            const float* emb = P + L.ion_embed + (int64_t)z * d.EI;
+            const float* W = P + L.h_ion_map_w[l];
+            float acc = P[L.h_ion_map_b[l] + f];
+            for (int k = 0; k < d.EI; ++k) acc += emb[k] * W[k * d.eiw[l] + f];
+            v = tanhf(acc);
+        }
+        him[idx] = v;
+    }
+}
+
+// ------------------------------------------------------------------ input features
+// X0[(b,i,t), 4I + q] = [d_iI, (r_i - R_I)_{x,y,z}] with tangents (input_features.py:51-68, :237-239).
+// Also zero-fills the padding columns of the layer-0 input.
+template <class Act>
+__global__ void k_features(const float* __restrict__ r, const float* __restrict__ R, Dims d, int B,
+                           Act* __restrict__ X0) {
+    int bi = blockIdx.x;          // b * n + i
+    int i = bi % d.n;
+    const float* ri = r + (int64_t)bi * 3;
+    int width = d.kw[0];
+    int nf = 4 * d.N;
+    int64_t row0 = (int64_t)bi * d.Tp;
+    for (int idx = threadIdx.x; idx < d.Tp * width; idx += blockDim.x) {
+        int t = idx / width, col = idx % width;
+        if (col >= nf && col < nf + d.E + 4) continue;   // conv columns written by k_conv
+        float v = 0.f;
+        if (col < nf) {
+            int I = col >> 2, q = col & 3;
+            float sx = ri[0] - R[I * 3 + 0], sy = ri[1] - R[I * 3 + 1], sz = ri[2] - R[I * 3 + 2];
+            float dd = sqrtf(sx * sx + sy * sy + sz * sz);
+            float s[3] = {sx, sy, sz};
+            if (t == 0) {
+                v = q == 0 ? dd : s[q - 1];
+            } else if (t == d.lap) {
+                v = q == 0 ? 2.f / dd : 0.f;
+            } else if (t >= 1 && t <= 3 * d.n) {
+                int m = (t - 1) / 3, c = (t - 1) % 3;
+                if (m == i) v = q == 0 ? s[c] / dd : (q - 1 == c ? 1.f : 0.f);
+            }
+        }
+        X0[(row0 + t) * width + col] = from_f<Act>(v);
+    }
+}
+
+// ------------------------------------------------------------------ 2-el and el-ion streams
+// One warp per unordered electron pair (pair streams) or per (electron, ion) (el-ion stream);
+// lane f owns output feature f. Pair streams: ferminet_embedding.py:137-150 (w maps) and
+// :247-253 (h_same / h_diff MLPs, residual (x+y)/sqrt2 on equal widths, mlp.py:13-17).
+// El-ion stream: ferminet_embedding.py:259-262.
+//
+// WP[l][b][i*n+j][ch][32], ch = (f, f', f'') in tangent mode, (f) in value mode.
+// HE[l][b][i*N+I][ch][32], ch = (f, dx, dy, dz, lap) or (f).
+template <int CH>
+__device__ __forceinline__ void dense32(const float (&x)[CH], int in_w, const float* __restrict__ W,
+                                        const float* __restrict__ bias, float (&z)[CH], int lane) {
+    #pragma unroll
+    for (int c = 0; c < CH; ++c) z[c] = 0.f;
+    z[0] = __ldg(bias + lane);
+    for (int k = 0; k < in_w; ++k) {
+        float w = __ldg(W + k * 32 + lane);
+        #pragma unroll
+        for (int c = 0; c < CH; ++c) z[c] += __shfl_sync(0xffffffffu, x[c], k) * w;
+    }
+}
+
+__global__ void k_pair_streams(const float* __restrict__ r, const float* __restrict__ P, ParamLayout L, Dims d,
+                               int B, int tangent, float* __restrict__ WP) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    int npair = d.n * (d.n + 1) / 2;
+    if (warp >= B * npair) return;
+    int b = warp / npair, p = warp % npair;
+    // unordered pair (i <= j) from linear index
+    int i = 0, rem = p;
+    while (rem >= d.n - i) { rem -= d.n - i; ++i; }
+    int j = i + rem;
+    bool same = (i < d.nu) == (j < d.nu);
+    const float* rb = r + (int64_t)b * d.n * 3;
+    float dd = 0.f;
+    if (i != j) {
+        float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
+        dd = sqrtf(dx * dx + dy * dy + dz * dz);
+    }
+    const int CH = 3;
+    float h[CH], z[CH], w[CH];
+    // input feature [dist]: value d, d' = 1, d'' = 0 (diagonal: constant 0, utils.py:297-300)
+    h[0] = lane == 0 ? dd : 0.f;
+    h[1] = (lane == 0 && i != j) ? 1.f : 0.f;
+    h[2] = 0.f;
+    int64_t plane = (int64_t)B * d.n * d.n;      // elements per l (in units of pair records)
+    int chs = tangent ? 3 : 1;
+    for (int l = 0; l < 4; ++l) {
+        int in_w = d.eew[l];
+        const float* Wm = P + (same ? L.w_same_w[l] : L.w_diff_w[l]);
+        const float* bm = P + (same ? L.w_same_b[l] : L.w_diff_b[l]);
+        dense32<CH>(h, in_w, Wm, bm, z, lane);
+        float y = tanhf(z[0]), d1 = 1.f - y * y;
+        w[0] = y; w[1] = d1 * z[1]; w[2] = d1 * z[2] - 2.f * y * d1 * z[1] * z[1];
+        float* o1 = WP + ((int64_t)l * plane + (int64_t)b * d.n * d.n + i * d.n + j) * chs * 32;
+        float* o2 = WP + ((int64_t)l * plane + (int64_t)b * d.n * d.n + j * d.n + i) * chs * 32;
+        for (int c = 0; c < chs; ++c) { o1[c * 32 + lane] = w[c]; o2[c * 32 + lane] = w[c]; }
+        if (l < 3) {
+            const float* Ws = P + (same ? L.h_same_w[l] : L.h_diff_w[l]);
+            const float* bs = P + (same ? L.h_same_b[l] : L.h_diff_b[l]);
+            dense32<CH>(h, in_w, Ws, bs, z, lane);
+            float yy = tanhf(z[0]), e1 = 1.f - yy * yy;
+            float hn[CH] = {yy, e1 * z[1], e1 * z[2] - 2.f * yy * e1 * z[1] * z[1]};
+            const float rs = 0.70710678118654752f;
+            #pragma unroll
+            for (int c = 0; c < CH; ++c) h[c] = (l == 0) ? hn[c] : (h[c] + hn[c]) * rs;
+        }
+    }
+}
+
+__global__ void k_ei_streams(const float* __restrict__ r, const float* __restrict__ R, const float* __restrict__ P,
+                             ParamLayout L, Dims d, int B, int tangent, float* __restrict__ HE) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    int nei = d.n * d.N;
+    if (warp >= B * nei) return;
+    int b = warp / nei, p = warp % nei;
+    int i = p / d.N, I = p % d.N;
+    const float* ri = r + ((int64_t)b * d.n + i) * 3;
+    float s[3] = {ri[0] - R[I * 3], ri[1] - R[I * 3 + 1], ri[2] - R[I * 3 + 2]};
+    float dd = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    const int CH = 5;
+    float h[CH];
+    // [d, sx, sy, sz] (input_features.py:56-66)
+    h[0] = lane == 0 ? dd : (lane < 4 ? s[lane - 1] : 0.f);
+    for (int c = 0; c < 3; ++c) h[1 + c] = lane == 0 ? s[c] / dd : (lane == c + 1 ? 1.f : 0.f);
+    h[4] = lane == 0 ? 2.f / dd : 0.f;
+    int chs = tangent ? 5 : 1;
+    int64_t plane = (int64_t)B * nei;
+    for (int l = 0; l < 4; ++l) {
+        float* o = HE + ((int64_t)l * plane + (int64_t)b * nei + p) * chs * 32;
+        for (int c = 0; c < chs; ++c) o[c * 32 + lane] = h[c];
+        if (l == 3) break;
+        float z[CH];
+        dense32<CH>(h, d.eiw[l], P + L.h_ei_w[l], P + L.h_ei_b[l], z, lane);
+        float y = tanhf(z[0]), d1 = 1.f - y * y;
+        float sq = z[1] * z[1] + z[2] * z[2] + z[3] * z[3];
+        float hn[CH] = {y, d1 * z[1], d1 * z[2], d1 * z[3], d1 * z[4] - 2.f * y * d1 * sq};
+        const float rs = 0.70710678118654752f;
+        #pragma unroll
+        for (int c = 0; c < CH; ++c) h[c] = (l == 0) ? hn[c] : (h[c] + hn[c]) * rs;
+    }
+}
+
+// ------------------------------------------------------------------ spin means of h_one
+// M[(b*Tp + t), 0:hw] = mean over up electrons, [hw:2hw] = mean over down electrons
+// (SymmetricFeatures, ferminet_embedding.py:60-72). Row width mw (>= 2hw, zero padded).
+template <class Act>
+__global__ void k_spin_means(const Act* __restrict__ X, int ldx, int hw, Dims d, Act* __restrict__ M, int mw) {
+    int b = blockIdx.x;
+    for (int idx = threadIdx.x; idx < d.Tp * mw; idx += blockDim.x) {
+        int t = idx / mw, col = idx % mw;
+        float v = 0.f;
+        if (col < 2 * hw) {
+            int f = col % hw;
+            int i0 = col < hw ? 0 : d.nu, i1 = col < hw ? d.nu : d.n;
+            for (int i = i0; i < i1; ++i) v += to_f(X[((int64_t)(b * d.n + i) * d.Tp + t) * ldx + f]);
+            v /= (float)(i1 - i0);
+        }
+        M[((int64_t)b * d.Tp + t) * mw + col] = from_f<Act>(v);
+    }
+}
+
+// ------------------------------------------------------------------ tanh with forward Laplacian
+// y = tanh(z): y_t = (1 - y^2) z_t, y_lap = (1 - y^2) z_lap - 2 y (1 - y^2) sum_t z_t^2.
+template <class Act>
+__global__ void k_tanh_fl(const float* __restrict__ Zb, int ldz, int ncols, int nrow_groups, Dims d,
+                          Act* __restrict__ Y, int ldy) {
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)nrow_groups * ncols) return;
+    int64_t g = idx / ncols;
+    int f = idx % ncols;
+    const float* z = Zb + g * d.Tp * ldz + f;
+    Act* y = Y + g * d.Tp * ldy + f;
+    float z0 = z[0];
+    float y0 = tanhf(z0), d1 = 1.f - y0 * y0;
+    y[0] = from_f<Act>(y0);
+    if (d.Tp == 1) return;
+    float s = 0.f;
+    for (int t = 1; t <= 3 * d.n; ++t) {
+        float zt = z[(int64_t)t * ldz];
+        s += zt * zt;
+        y[(int64_t)t * ldy] = from_f<Act>(d1 * zt);
+    }
+    y[(int64_t)d.lap * ldy] = from_f<Act>(d1 * z[(int64_t)d.lap * ldz] - 2.f * y0 * d1 * s);
+    for (int t = d.lap + 1; t < d.Tp; ++t) y[(int64_t)t * ldy] = from_f<Act>(0.f);
+}
+
+// ------------------------------------------------------------------ SchNet convolutions
+// conv_ee[i] = sum_j w_ij * hm_j (same/diff spin blocks incl. the self pair,
+// ferminet_embedding.py:152-169) and conv_ei[i] = sum_I h_ei[i,I] * him[I] (:171-175),
+// with product-rule tangents and Laplacian. Written into columns [hw, hw+E+eiw) of X_l.
+template <class Act>
+__global__ void k_conv(const float* __restrict__ r, const float* __restrict__ WPl, const float* __restrict__ HM,
+                       const float* __restrict__ HEl, const float* __restrict__ himl, Dims d, int l, int B,
+                       Act* __restrict__ X, int ldx) {
+    int bi = blockIdx.x;
+    int b = bi / d.n, i = bi % d.n;
+    int hw = d.hw[l], E = d.E, eiw = d.eiw[l];
+    int ncol = E + eiw;
+    int pch = d.Tp > 1 ? 3 : 1, ech = d.Tp > 1 ? 5 : 1;
+    const float* rb = r + (int64_t)b * d.n * 3;
+    const float* wrow = WPl + ((int64_t)b * d.n * d.n + (int64_t)i * d.n) * pch * 32;   // w_i,: records
+    const float* hmb = HM + (int64_t)b * d.n * d.Tp * 32;
+    for (int idx = threadIdx.x; idx < d.Tp * ncol; idx += blockDim.x) {
+        int t = idx / ncol, col = idx % ncol;
+        float v = 0.f;
+        if (t < d.T) {
+            if (col < E) {
+                int f = col;
+                for (int j = 0; j < d.n; ++j) v += wrow[j * pch * 32 + f] * hmb[((int64_t)j * d.Tp + t) * 32 + f];
+                if (t >= 1 && t <= 3 * d.n) {
+                    int m = (t - 1) / 3, c = (t - 1) % 3;
+                    if (m == i) {
+                        for (int j = 0; j < d.n; ++j) {
+                            if (j == i) continue;
+                            float u = rb[j * 3 + c] - rb[i * 3 + c];
+                            float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
+                            float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+                            v -= wrow[j * pch * 32 + 32 + f] * (u / dist) * hmb[(int64_t)j * d.Tp * 32 + f];
+                        }
+                    } else {
+                        float u = rb[m * 3 + c] - rb[i * 3 + c];
+                        float dx = rb[m * 3] - rb[i * 3], dy = rb[m * 3 + 1] - rb[i * 3 + 1], dz = rb[m * 3 + 2] - rb[i * 3 + 2];
+                        float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+                        v += wrow[m * pch * 32 + 32 + f] * (u / dist) * hmb[(int64_t)m * d.Tp * 32 + f];
+                    }
+                } else if (t == d.lap) {
+                    for (int j = 0; j < d.n; ++j) {
+                        if (j == i) continue;
+                        float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
+                        float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+                        float inv = 1.f / dist;
+                        float w1 = wrow[j * pch * 32 + 32 + f], w2 = wrow[j * pch * 32 + 64 + f];
+                        const float* hj = hmb + (int64_t)j * d.Tp * 32 + f;
+                        float cross = 0.f;
+                        float uu[3] = {dx * inv, dy * inv, dz * inv};
+                        #pragma unroll
+                        for (int c = 0; c < 3; ++c)
+                            cross += uu[c] * (hj[(1 + 3 * j + c) * 32] - hj[(1 + 3 * i + c) * 32]);
+                        v += 2.f * (w2 + 2.f * w1 * inv) * hj[0] + 2.f * w1 * cross;
+                    }
+                }
+            } else {
+                int f = col - E;
+                int ch = -1;
+                if (t == 0) ch = 0;
+                else if (t == d.lap) ch = 4;
+                else if (t >= 1 + 3 * i && t < 4 + 3 * i) ch = t - 3 * i;
+                if (ch >= 0) {
+                    const float* he = HEl + ((int64_t)b * d.n * d.N + (int64_t)i * d.N) * ech * 32;
+                    for (int I = 0; I < d.N; ++I) v += he[(I * ech + ch) * 32 + f] * himl[I * 32 + f];
+                }
+            }
+        }
+        X[((int64_t)bi * d.Tp + t) * ldx + hw + col] = from_f<Act>(v);
+    }
+}
+
+// ------------------------------------------------------------------ envelope x backflow -> Slater tangents
+// mo[b][k][t][i][o] = env[i,(k,o)] * bf[i,(k,o)] with tangents (envelope_orbitals.py:91-127).
+// env = sum_I w_I exp(-softplus(alpha_I) d_iI); grad/Laplacian w.r.t. r_i only.
+__global__ void k_envelope(const float* __restrict__ r, const float* __restrict__ R, const float* __restrict__ P,
+                           ParamLayout L, Dims d, int B, const float* __restrict__ BF, int ldbf,
+                           float* __restrict__ MO) {
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)B * d.n * d.KN) return;
+    int col = idx % d.KN;
+    int64_t bi = idx / d.KN;
+    int i = bi % d.n, b = bi / d.n;
+    int k = col / d.n, o = col % d.n;
+    bool up = i < d.nu;
+    const float* alpha = P + (up ? L.alpha_up : L.alpha_dn);
+    const float* wts = P + (up ? L.weights_up : L.weights_dn);
+    const float* ri = r + bi * 3;
+    float env = 0.f, g[3] = {0.f, 0.f, 0.f}, lapv = 0.f;
+    for (int I = 0; I < d.N; ++I) {
+        float s0 = ri[0] - R[I * 3], s1 = ri[1] - R[I * 3 + 1], s2 = ri[2] - R[I * 3 + 2];
+        float dd = sqrtf(s0 * s0 + s1 * s1 + s2 * s2);
+        float a = softplus_f(alpha[I * d.KN + col]);
+        float e = wts[I * d.KN + col] * expf(-a * dd);
+        env += e;
+        if (d.Tp > 1) {
+            float gs = -a * e / dd;
+            g[0] += gs * s0; g[1] += gs * s1; g[2] += gs * s2;
+            lapv += e * (a * a - 2.f * a / dd);
+        }
+    }
+    const float* bf = BF + bi * d.Tp * ldbf + col;
+    int64_t mstride = (int64_t)d.n * d.n;                    // per channel
+    float* mo = MO + (((int64_t)b * d.K + k) * d.T) * mstride + i * d.n + o;
+    float bf0 = bf[0];
+    mo[0] = env * bf0;
+    if (d.Tp == 1) return;
+    for (int t = 1; t <= 3 * d.n; ++t) {
+        float v = env * bf[(int64_t)t * ldbf];
+        int m = (t - 1) / 3, c = (t - 1) % 3;
+        if (m == i) v += g[c] * bf0;
+        mo[t * mstride] = v;
+    }
+    float vl = env * bf[(int64_t)d.lap * ldbf] + lapv * bf0;
+    for (int c = 0; c < 3; ++c) vl += 2.f * g[c] * bf[(int64_t)(1 + 3 * i + c) * ldbf];
+    mo[d.lap * mstride] = vl;
+}
+
+// ------------------------------------------------------------------ Jastrow output layer + electron sum
+// jas[b][t] = sum_i sum_f J2[(b,i,t), f] * w2[f]  (wavefunction.py:58-59, linear output, no bias)
+template <class Act>
+__global__ void k_jastrow_out(const Act* __restrict__ J2, int ldj, const float* __restrict__ w2, Dims d, int B,
+                              double* __restrict__ jas) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= B * d.Tp) return;
+    int b = warp / d.Tp, t = warp % d.Tp;
+    float acc = 0.f;
+    for (int i = 0; i < d.n; ++i) {
+        const Act* row = J2 + ((int64_t)(b * d.n + i) * d.Tp + t) * ldj;
+        for (int f = lane; f < d.J1; f += 32) acc += to_f(row[f]) * w2[f];
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) jas[(int64_t)b * d.Tp + t] = acc;
+}
+
+// ------------------------------------------------------------------ launch wrappers
+void launch_ion_maps(const float* P, const ParamLayout& L, const Dims& d, const int32_t* Z, float* him, cudaStream_t s) {
+    k_ion_maps<<<1, 256, 0, s>>>(P, L, d, Z, him); count_launch();
+}
+template <class Act>
+void launch_features(const float* r, const float* R, const Dims& d, int B, Act* X0, cudaStream_t s) {
+    k_features<Act><<<B * d.n, 256, 0, s>>>(r, R, d, B, X0); count_launch();
+}
+void launch_streams(const float* r, const float* R, const float* P, const ParamLayout& L, const Dims& d, int B,
+                    float* WP, float* HE, cudaStream_t s) {
+    int tang = d.Tp > 1;
+    int npair = d.n * (d.n + 1) / 2;
+    int64_t warps = (int64_t)B * npair;
+    k_pair_streams<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(r, P, L, d, B, tang, WP); count_launch();
+    warps = (int64_t)B * d.n * d.N;
+    k_ei_streams<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(r, R, P, L, d, B, tang, HE); count_launch();
+}
+template <class Act>
+void launch_spin_means(const Act* X, int ldx, int hw, const Dims& d, int B, Act* M, int mw, cudaStream_t s) {
+    k_spin_means<Act><<<B, 256, 0, s>>>(X, ldx, hw, d, M, mw); count_launch();
+}
+template <class Act>
+void launch_tanh_fl(const float* Zb, int ldz, int ncols, int groups, const Dims& d, Act* Y, int ldy, cudaStream_t s) {
+    int64_t n = (int64_t)groups * ncols;
+    k_tanh_fl<Act><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(Zb, ldz, ncols, groups, d, Y, ldy); count_launch();
+}
+template <class Act>
+void launch_conv(const float* r, const float* WPl, const float* HM, const float* HEl, const float* himl, const Dims& d,
+                 int l, int B, Act* X, int ldx, cudaStream_t s) {
+    k_conv<Act><<<B * d.n, 256, 0, s>>>(r, WPl, HM, HEl, himl, d, l, B, X, ldx); count_launch();
+}
+void launch_envelope(const float* r, const float* R, const float* P, const ParamLayout& L, const Dims& d, int B,
+                     const float* BF, int ldbf, float* MO, cudaStream_t s) {
+    int64_t n = (int64_t)B * d.n * d.KN;
+    k_envelope<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, R, P, L, d, B, BF, ldbf, MO); count_launch();
+}
+template <class Act>
+void launch_jastrow_out(const Act* J2, int ldj, const float* w2, const Dims& d, int B, double* jas, cudaStream_t s) {
+    int64_t warps = (int64_t)B * d.Tp;
+    k_jastrow_out<Act><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(J2, ldj, w2, d, B, jas); count_launch();
+}
+
+#define DW_INST(Act)                                                                                          \
+    template void launch_features<Act>(const float*, const float*, const Dims&, int, Act*, cudaStream_t);     \
+    template void launch_spin_means<Act>(const Act*, int, int, const Dims&, int, Act*, int, cudaStream_t);    \
+    template void launch_tanh_fl<Act>(const float*, int, int, int, const Dims&, Act*, int, cudaStream_t);     \
+    template void launch_conv<Act>(const float*, const float*, const float*, const float*, const float*,      \
+                                   const Dims&, int, int, Act*, int, cudaStream_t);                           \
+    template void launch_jastrow_out<Act>(const Act*, int, const float*, const Dims&, int, double*, cudaStream_t);
+DW_INST(float)
+DW_INST(__nv_bfloat16)
+
+}  // namespace dw

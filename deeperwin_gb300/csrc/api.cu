@@ -5,6 +5,7 @@
 #include "gemm_tc.cuh"
 #include <string.h>
 #include <algorithm>
+#include <type_traits>
 
 namespace dw {
 
@@ -13,12 +14,21 @@ namespace dw {
 // Wmean_l [mw_l, D] = rows for (mean_up, mean_dn) (the spin means are identical for all
 // electrons of a walker, so their product is formed once per walker and channel).
 // Mixed precision additionally keeps BF16 K-major copies ([N, K]) for the tensor-core GEMMs.
+// Tensor-core paths keep BF16 K-major copies ([N, K]) of every GEMM weight: hi = bf16(w) and,
+// for the split (mixed) form, lo = bf16(w - hi).
+struct WRef {
+    const float* f32 = nullptr; int ldw = 0;                // [K, N] row-major FP32
+    const __nv_bfloat16* hi = nullptr; const __nv_bfloat16* lo = nullptr;
+};
 struct Prepared {
     float* main[4]; float* mean[4];
-    __nv_bfloat16* main_bf[4]; __nv_bfloat16* mean_bf[4]; __nv_bfloat16* map_bf[4];
-    __nv_bfloat16* bf_up; __nv_bfloat16* bf_dn; __nv_bfloat16* jas0; __nv_bfloat16* jas1;
+    __nv_bfloat16* main_bf[2][4]; __nv_bfloat16* mean_bf[2][4]; __nv_bfloat16* map_bf[2][4];
+    __nv_bfloat16* bf_up[2]; __nv_bfloat16* bf_dn[2]; __nv_bfloat16* jas0[2]; __nv_bfloat16* jas1[2];
     size_t bytes;
 };
+static inline int tc_parts(int precision) {
+    return precision == DW_PRECISION_MIXED ? 2 : (precision == DW_PRECISION_BF16 ? 1 : 0);
+}
 static inline int mean_width(const Dims& d, int l) { return round_up(2 * d.hw[l], 64); }
 
 static Prepared carve_prepared(const DwArch* a, int precision, void* base) {
@@ -30,16 +40,16 @@ static Prepared carve_prepared(const DwArch* a, int precision, void* base) {
         p.main[l] = c.take<float>((size_t)d.kw[l] * d.D);
         p.mean[l] = c.take<float>((size_t)mean_width(d, l) * d.D);
     }
-    if (precision == DW_PRECISION_MIXED) {
+    for (int part = 0; part < tc_parts(precision); ++part) {
         for (int l = 0; l < 4; ++l) {
-            p.main_bf[l] = c.take<__nv_bfloat16>((size_t)d.kw[l] * d.D);
-            p.mean_bf[l] = c.take<__nv_bfloat16>((size_t)mean_width(d, l) * d.D);
-            p.map_bf[l] = c.take<__nv_bfloat16>((size_t)round_up(d.hw[l], 64) * d.E);
+            p.main_bf[part][l] = c.take<__nv_bfloat16>((size_t)d.kw[l] * d.D);
+            p.mean_bf[part][l] = c.take<__nv_bfloat16>((size_t)mean_width(d, l) * d.D);
+            p.map_bf[part][l] = c.take<__nv_bfloat16>((size_t)round_up(d.hw[l], 64) * d.E);
         }
-        p.bf_up = c.take<__nv_bfloat16>((size_t)d.D * round_up(d.KN, 16));
-        p.bf_dn = c.take<__nv_bfloat16>((size_t)d.D * round_up(d.KN, 16));
-        p.jas0 = c.take<__nv_bfloat16>((size_t)d.D * d.J0);
-        p.jas1 = c.take<__nv_bfloat16>((size_t)d.J0 * d.J1);
+        p.bf_up[part] = c.take<__nv_bfloat16>((size_t)d.D * round_up(d.KN, 16));
+        p.bf_dn[part] = c.take<__nv_bfloat16>((size_t)d.D * round_up(d.KN, 16));
+        p.jas0[part] = c.take<__nv_bfloat16>((size_t)d.D * d.J0);
+        p.jas1[part] = c.take<__nv_bfloat16>((size_t)d.J0 * d.J1);
     }
     p.bytes = c.used;
     return p;
@@ -57,14 +67,16 @@ __global__ void k_gather_rows(const float* __restrict__ src, int cols, int rows,
     else sr = r < 2 * hw ? hw + r : -1;
     dst[idx] = sr >= 0 ? src[(int64_t)sr * cols + c] : 0.f;
 }
-// dstT[c][r] = bf16(src[r][c]) for r < rows_src, 0 for rows_src <= r < rows_pad; cols padded to cols_pad.
+// dstT[c][r] = bf16 part of src[r][c] (part 0: hi = bf16(x), part 1: lo = bf16(x - hi)) for
+// r < rows_src; zero for rows_src <= r < rows_pad and c >= cols (padding).
 __global__ void k_transpose_bf16(const float* __restrict__ src, int rows_src, int rows_pad, int cols, int cols_pad,
-                                 __nv_bfloat16* __restrict__ dst) {
+                                 int part, __nv_bfloat16* __restrict__ dst) {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)rows_pad * cols_pad) return;
     int c = idx / rows_pad, r = idx % rows_pad;
     float v = (r < rows_src && c < cols) ? src[(int64_t)r * cols + c] : 0.f;
-    dst[idx] = __float2bfloat16_rn(v);
+    __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    dst[idx] = part == 0 ? hi : __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
 static int prepare(const DwArch* a, int precision, const float* P, void* prep, size_t bytes, cudaStream_t s) {
@@ -83,21 +95,21 @@ static int prepare(const DwArch* a, int precision, const float* P, void* prep, s
             count_launch();
         }
     }
-    if (precision == DW_PRECISION_MIXED) {
+    for (int part = 0; part < tc_parts(precision); ++part) {
         auto tr = [&](const float* src, int rows_src, int rows_pad, int cols, int cols_pad, __nv_bfloat16* dst) {
             int64_t n = (int64_t)rows_pad * cols_pad;
-            k_transpose_bf16<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, rows_src, rows_pad, cols, cols_pad, dst);
+            k_transpose_bf16<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, rows_src, rows_pad, cols, cols_pad, part, dst);
             count_launch();
         };
         for (int l = 0; l < 4; ++l) {
-            tr(p.main[l], d.kw[l], d.kw[l], d.D, d.D, p.main_bf[l]);
-            tr(p.mean[l], mean_width(d, l), mean_width(d, l), d.D, d.D, p.mean_bf[l]);
-            tr(P + L.h_map_w[l], d.hw[l], round_up(d.hw[l], 64), d.E, d.E, p.map_bf[l]);
+            tr(p.main[l], d.kw[l], d.kw[l], d.D, d.D, p.main_bf[part][l]);
+            tr(p.mean[l], mean_width(d, l), mean_width(d, l), d.D, d.D, p.mean_bf[part][l]);
+            tr(P + L.h_map_w[l], d.hw[l], round_up(d.hw[l], 64), d.E, d.E, p.map_bf[part][l]);
         }
-        tr(P + L.bf_up, d.D, d.D, d.KN, round_up(d.KN, 16), p.bf_up);
-        tr(P + L.bf_dn, d.D, d.D, d.KN, round_up(d.KN, 16), p.bf_dn);
-        tr(P + L.jas_w[0], d.D, d.D, d.J0, d.J0, p.jas0);
-        tr(P + L.jas_w[1], d.J0, d.J0, d.J1, d.J1, p.jas1);
+        tr(P + L.bf_up, d.D, d.D, d.KN, round_up(d.KN, 16), p.bf_up[part]);
+        tr(P + L.bf_dn, d.D, d.D, d.KN, round_up(d.KN, 16), p.bf_dn[part]);
+        tr(P + L.jas_w[0], d.D, d.D, d.J0, d.J0, p.jas0[part]);
+        tr(P + L.jas_w[1], d.J0, d.J0, d.J1, d.J1, p.jas1[part]);
     }
     DW_CHECK_CUDA(cudaGetLastError());
     return DW_OK;
@@ -124,6 +136,7 @@ static const int kXW = 320;   // row width of the layer-1..3 inputs: 256 (h) + 3
 template <class Act>
 static Plan<Act> carve_plan(const Dims& d, int Bc, void* ws) {
     Carver c(ws, (size_t)-1);
+    const int64_t np = ActIO<Act>::kParts;
     Plan<Act> p;
     p.d = d; p.Bc = Bc;
     int64_t rows = (int64_t)Bc * d.n * d.Tp;
@@ -132,10 +145,10 @@ static Plan<Act> carve_plan(const Dims& d, int Bc, void* ws) {
     for (int l = 0; l < 4; ++l) mw = std::max(mw, mean_width(d, l));
     int zw = std::max(std::max(d.D, d.J0), d.KN);
     p.him = c.take<float>(4 * d.N * 32);
-    p.X0 = c.take<Act>(rows * d.kw[0]);
-    p.XA = c.take<Act>(rows * kXW);
-    p.XB = c.take<Act>(rows * kXW);
-    p.Mcat = c.take<Act>((int64_t)Bc * d.Tp * mw);
+    p.X0 = c.take<Act>(np * rows * d.kw[0]);
+    p.XA = c.take<Act>(np * rows * kXW);
+    p.XB = c.take<Act>(np * rows * kXW);
+    p.Mcat = c.take<Act>(np * Bc * d.Tp * mw);
     p.WB = c.take<float>((int64_t)Bc * d.Tp * d.D);
     p.HM = c.take<float>(rows * d.E);
     p.Zb = c.take<float>(rows * std::max(d.D, d.J0));
@@ -153,8 +166,8 @@ static Plan<Act> carve_plan(const Dims& d, int Bc, void* ws) {
     } else {
         p.Ainv = nullptr; p.g = nullptr; p.lapdet = nullptr;
     }
-    p.J1 = c.take<Act>(rows * d.J0);
-    p.J2 = c.take<Act>(rows * d.J1);
+    p.J1 = c.take<Act>(np * rows * d.J0);
+    p.J2 = c.take<Act>(np * rows * d.J1);
     p.jas = c.take<double>((int64_t)Bc * d.Tp);
     (void)zw;
     p.bytes = c.used;
@@ -170,6 +183,61 @@ static int choose_chunk(const Dims& d, int B) {
     return std::min(bc, B);
 }
 
+// ------------------------------------------------------------------ GEMM dispatch by activation type
+// mm:      C (fp32) = A W + epilogue
+// mm_act:  C (Act)  = act(A W + epilogue)            (value-only layers)
+// mm_bat:  batched over walkers, no epilogue
+template <class Act> struct MM;
+template <> struct MM<float> {
+    static int mm(const float* A, int lda, const WRef& W, float* C, int ldc, int M, int N, int K, const GemmEpi& e,
+                  cudaStream_t s) {
+        gemm_f32(A, lda, W.f32, W.ldw, C, ldc, M, N, K, e, 1, 0, 0, s);
+        return DW_OK;
+    }
+    static int mm_act(const float* A, int lda, const WRef& W, float* C, int ldc, int M, int N, int K, const GemmEpi& e,
+                      cudaStream_t s) {
+        gemm_f32(A, lda, W.f32, W.ldw, C, ldc, M, N, K, e, 1, 0, 0, s);
+        return DW_OK;
+    }
+    static int mm_bat(const float* A, int lda, int64_t rows_per_batch, const WRef& W, float* C, int ldc, int M, int N,
+                      int K, int batch, int64_t sC, cudaStream_t s) {
+        GemmEpi e;
+        gemm_f32(A, lda, W.f32, W.ldw, C, ldc, M, N, K, e, batch, rows_per_batch * lda, sC, s);
+        return DW_OK;
+    }
+};
+template <> struct MM<__nv_bfloat16> {
+    static int mm(const __nv_bfloat16* A, int lda, const WRef& W, float* C, int ldc, int M, int N, int K,
+                  const GemmEpi& e, cudaStream_t s) {
+        return gemm_bf16_tc(A, lda, W.hi, C, ldc, M, N, K, e, s);
+    }
+    static int mm_act(const __nv_bfloat16* A, int lda, const WRef& W, __nv_bfloat16* C, int ldc, int M, int N, int K,
+                      const GemmEpi& e, cudaStream_t s) {
+        return gemm_bf16_tc_act(A, lda, W.hi, C, ldc, M, N, K, e, s);
+    }
+    static int mm_bat(const __nv_bfloat16* A, int lda, int64_t rows_per_batch, const WRef& W, float* C, int ldc, int M,
+                      int N, int K, int batch, int64_t sC, cudaStream_t s) {
+        return gemm_bf16_tc_batched(A, lda, W.hi, C, ldc, M, N, K, batch, rows_per_batch * lda, sC, s);
+    }
+};
+template <> struct MM<Split> {
+    static int mm(const Split* A, int lda, const WRef& W, float* C, int ldc, int M, int N, int K, const GemmEpi& e,
+                  cudaStream_t s) {
+        return gemm_split_tc(A, lda, W.hi, W.lo, C, ldc, M, N, K, e, s);
+    }
+    static int mm_act(const Split* A, int lda, const WRef& W, Split* C, int ldc, int M, int N, int K, const GemmEpi& e,
+                      cudaStream_t s) {
+        return gemm_split_tc_act(A, lda, W.hi, W.lo, C, ldc, M, N, K, e, s);
+    }
+    static int mm_bat(const Split* A, int lda, int64_t rows_per_batch, const WRef& W, float* C, int ldc, int M, int N,
+                      int K, int batch, int64_t sC, cudaStream_t s) {
+        return gemm_split_tc_batched(A, lda, W.hi, W.lo, C, ldc, M, N, K, batch, rows_per_batch, sC, s);
+    }
+};
+
+// Element offset of row `row` in a logical-width-ld activation buffer of type Act.
+template <class Act> static inline int64_t act_off(int64_t row, int ld) { return row * ld * ActIO<Act>::kParts; }
+
 // The forward (value or tangent) of one chunk of walkers.
 template <class Act>
 static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, const ParamLayout& L,
@@ -178,7 +246,19 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
     const Dims& d = p.d;
     const int rows = Bc * d.n * d.Tp;
     const bool tang = d.Tp > 1;
-    const bool tc = precision == DW_PRECISION_MIXED && tc_available();
+    const int pt = tc_parts(precision);
+    auto wref = [&](const float* f32, int ldw, __nv_bfloat16* const* bf, int l) {
+        WRef w; w.f32 = f32; w.ldw = ldw;
+        if (pt >= 1) w.hi = bf[0 * 4 + l];
+        if (pt >= 2) w.lo = bf[1 * 4 + l];
+        return w;
+    };
+    auto wref1 = [&](const float* f32, int ldw, __nv_bfloat16* const* bf) {
+        WRef w; w.f32 = f32; w.ldw = ldw;
+        if (pt >= 1) w.hi = bf[0];
+        if (pt >= 2) w.lo = bf[1];
+        return w;
+    };
     launch_features<Act>(r, R, d, Bc, p.X0, s);
     launch_streams(r, R, P, L, d, Bc, p.WP, p.HE, s);
     Act* xin = p.X0;
@@ -187,70 +267,62 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
     for (int l = 0; l < 4; ++l) {
         Act* xout = (l % 2 == 0) ? p.XA : p.XB;
         int hw = d.hw[l], mw = mean_width(d, l);
-        // (a) spin means and their per-walker contribution
+        // (a) spin means and their per-walker contribution (+ the layer bias on the value channel)
         launch_spin_means<Act>(xin, ldin, hw, d, Bc, p.Mcat, mw, s);
         GemmEpi e1; e1.bias = P + L.h_el_b[l]; e1.Tp = d.Tp; e1.rows_per_walker = d.Tp;
-        if (tc) DW_CHECK(gemm_bf16_tc((const __nv_bfloat16*)p.Mcat, mw, pre.mean_bf[l], p.WB, d.D, Bc * d.Tp, d.D, mw, e1, s));
-        else gemm_f32((const float*)p.Mcat, mw, pre.mean[l], d.D, p.WB, d.D, Bc * d.Tp, d.D, mw, e1, 1, 0, 0, s);
+        DW_CHECK(MM<Act>::mm(p.Mcat, mw, wref(pre.mean[l], d.D, &pre.mean_bf[0][0], l), p.WB, d.D, Bc * d.Tp, d.D, mw,
+                             e1, s));
         // (b) h_map = tanh(h_one W + b)
         GemmEpi e2; e2.bias = P + L.h_map_b[l]; e2.Tp = d.Tp; e2.rows_per_walker = d.n * d.Tp; e2.act = tang ? 0 : 1;
         float* hm_pre = tang ? p.Zb : p.HM;
-        if (tc) DW_CHECK(gemm_bf16_tc((const __nv_bfloat16*)xin, ldin, pre.map_bf[l], hm_pre, d.E, rows, d.E, hw, e2, s));
-        else gemm_f32((const float*)xin, ldin, P + L.h_map_w[l], d.E, hm_pre, d.E, rows, d.E, hw, e2, 1, 0, 0, s);
+        DW_CHECK(MM<Act>::mm(xin, ldin, wref(P + L.h_map_w[l], d.E, &pre.map_bf[0][0], l), hm_pre, d.E, rows, d.E, hw,
+                             e2, s));
         if (tang) launch_tanh_fl<float>(p.Zb, d.E, d.E, Bc * d.n, d, p.HM, d.E, s);
         // (c) SchNet convolutions into the input columns [hw, hw + E + eiw)
         int64_t wp_plane = (int64_t)Bc * d.n * d.n * pc * 32, he_plane = (int64_t)Bc * d.n * d.N * ec * 32;
         launch_conv<Act>(r, p.WP + l * wp_plane, p.HM, p.HE + l * he_plane, p.him + l * d.N * 32, d, l, Bc, xin, ldin, s);
         // (d) h_el = tanh([h | conv_ee | conv_ei] W_main + per-walker mean term)
         GemmEpi e3; e3.rowbias = p.WB; e3.ldrb = d.D; e3.Tp = d.Tp; e3.rows_per_walker = d.n * d.Tp; e3.act = tang ? 0 : 1;
-        float* zout = tang ? p.Zb : nullptr;
+        WRef wm = wref(pre.main[l], d.D, &pre.main_bf[0][0], l);
         if (tang) {
-            if (tc) DW_CHECK(gemm_bf16_tc((const __nv_bfloat16*)xin, ldin, pre.main_bf[l], zout, d.D, rows, d.D, d.kw[l], e3, s));
-            else gemm_f32((const float*)xin, ldin, pre.main[l], d.D, zout, d.D, rows, d.D, d.kw[l], e3, 1, 0, 0, s);
+            // algorithmic work of this launch: 2 M N K with the unpadded K, A and C streamed once
+            const double kreal = hw + d.E + d.eiw[l];
+            const double flops = 2.0 * rows * d.D * kreal;
+            const double bytes = (double)rows * (kreal * sizeof(Act) * ActIO<Act>::kParts + d.D * 4.0) +
+                                 kreal * d.D * sizeof(Act) * ActIO<Act>::kParts;
+            timer_begin("layer_gemm", s);
+            DW_CHECK(MM<Act>::mm(xin, ldin, wm, p.Zb, d.D, rows, d.D, d.kw[l], e3, s));
+            timer_end("layer_gemm", s, flops, bytes);
             launch_tanh_fl<Act>(p.Zb, d.D, d.D, Bc * d.n, d, xout, kXW, s);
         } else {
-            if (tc) DW_CHECK(gemm_bf16_tc_act((const __nv_bfloat16*)xin, ldin, pre.main_bf[l], (__nv_bfloat16*)xout, kXW,
-                                              rows, d.D, d.kw[l], e3, s));
-            else gemm_f32((const float*)xin, ldin, pre.main[l], d.D, (float*)xout, kXW, rows, d.D, d.kw[l], e3, 1, 0, 0, s);
+            DW_CHECK(MM<Act>::mm_act(xin, ldin, wm, xout, kXW, rows, d.D, d.kw[l], e3, s));
         }
         xin = xout;
         ldin = kXW;
     }
-    const Act* H = xin;   // final embedding, row width kXW
+    const Act* H = xin;   // final embedding, logical row width kXW
     // backflow (envelope_orbitals.py:46-75): up-electron rows x W_up, down-electron rows x W_dn
-    GemmEpi e0; e0.Tp = d.Tp; e0.rows_per_walker = d.n * d.Tp;
-    int64_t sA = (int64_t)d.n * d.Tp * kXW, sC = (int64_t)d.n * d.Tp * d.KN;
-    if (tc) {
-        DW_CHECK(gemm_bf16_tc_batched((const __nv_bfloat16*)H, kXW, pre.bf_up, p.BF, d.KN, d.nu * d.Tp, d.KN, d.D, Bc, sA, sC, s));
-        DW_CHECK(gemm_bf16_tc_batched((const __nv_bfloat16*)H + (int64_t)d.nu * d.Tp * kXW, kXW, pre.bf_dn,
-                                      p.BF + (int64_t)d.nu * d.Tp * d.KN, d.KN, d.nd * d.Tp, d.KN, d.D, Bc, sA, sC, s));
-    } else {
-        gemm_f32((const float*)H, kXW, P + L.bf_up, d.KN, p.BF, d.KN, d.nu * d.Tp, d.KN, d.D, e0, Bc, sA, sC, s);
-        gemm_f32((const float*)H + (int64_t)d.nu * d.Tp * kXW, kXW, P + L.bf_dn, d.KN, p.BF + (int64_t)d.nu * d.Tp * d.KN,
-                 d.KN, d.nd * d.Tp, d.KN, d.D, e0, Bc, sA, sC, s);
-    }
+    const int64_t rpw = (int64_t)d.n * d.Tp, sC = (int64_t)d.n * d.Tp * d.KN;
+    DW_CHECK(MM<Act>::mm_bat(H, kXW, rpw, wref1(P + L.bf_up, d.KN, pre.bf_up), p.BF, d.KN, d.nu * d.Tp, d.KN, d.D, Bc,
+                             sC, s));
+    DW_CHECK(MM<Act>::mm_bat(H + act_off<Act>((int64_t)d.nu * d.Tp, kXW), kXW, rpw, wref1(P + L.bf_dn, d.KN, pre.bf_dn),
+                             p.BF + (int64_t)d.nu * d.Tp * d.KN, d.KN, d.nd * d.Tp, d.KN, d.D, Bc, sC, s));
     launch_envelope(r, R, P, L, d, Bc, p.BF, d.KN, p.MO, s);
-    if (precision == DW_PRECISION_MIXED) launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s);
-    else launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s);
+    if (precision == DW_PRECISION_FP32) launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s);
+    else launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s);
     if (tang) launch_det_tangents(p.MO, p.Ainv, p.sign, d, Bc, p.g, p.lapdet, s);
     // Jastrow MLP([64, 64, 1]) on the final embedding
     GemmEpi j0; j0.bias = P + L.jas_b[0]; j0.Tp = d.Tp; j0.rows_per_walker = d.n * d.Tp; j0.act = tang ? 0 : 1;
     GemmEpi j1 = j0; j1.bias = P + L.jas_b[1];
+    WRef wj0 = wref1(P + L.jas_w[0], d.J0, pre.jas0), wj1 = wref1(P + L.jas_w[1], d.J1, pre.jas1);
     if (tang) {
-        if (tc) DW_CHECK(gemm_bf16_tc((const __nv_bfloat16*)H, kXW, pre.jas0, p.Zb, d.J0, rows, d.J0, d.D, j0, s));
-        else gemm_f32((const float*)H, kXW, P + L.jas_w[0], d.J0, p.Zb, d.J0, rows, d.J0, d.D, j0, 1, 0, 0, s);
+        DW_CHECK(MM<Act>::mm(H, kXW, wj0, p.Zb, d.J0, rows, d.J0, d.D, j0, s));
         launch_tanh_fl<Act>(p.Zb, d.J0, d.J0, Bc * d.n, d, p.J1, d.J0, s);
-        if (tc) DW_CHECK(gemm_bf16_tc((const __nv_bfloat16*)p.J1, d.J0, pre.jas1, p.Zb, d.J1, rows, d.J1, d.J0, j1, s));
-        else gemm_f32((const float*)p.J1, d.J0, P + L.jas_w[1], d.J1, p.Zb, d.J1, rows, d.J1, d.J0, j1, 1, 0, 0, s);
+        DW_CHECK(MM<Act>::mm(p.J1, d.J0, wj1, p.Zb, d.J1, rows, d.J1, d.J0, j1, s));
         launch_tanh_fl<Act>(p.Zb, d.J1, d.J1, Bc * d.n, d, p.J2, d.J1, s);
     } else {
-        if (tc) {
-            DW_CHECK(gemm_bf16_tc_act((const __nv_bfloat16*)H, kXW, pre.jas0, (__nv_bfloat16*)p.J1, d.J0, rows, d.J0, d.D, j0, s));
-            DW_CHECK(gemm_bf16_tc_act((const __nv_bfloat16*)p.J1, d.J0, pre.jas1, (__nv_bfloat16*)p.J2, d.J1, rows, d.J1, d.J0, j1, s));
-        } else {
-            gemm_f32((const float*)H, kXW, P + L.jas_w[0], d.J0, (float*)p.J1, d.J0, rows, d.J0, d.D, j0, 1, 0, 0, s);
-            gemm_f32((const float*)p.J1, d.J0, P + L.jas_w[1], d.J1, (float*)p.J2, d.J1, rows, d.J1, d.J0, j1, 1, 0, 0, s);
-        }
+        DW_CHECK(MM<Act>::mm_act(H, kXW, wj0, p.J1, d.J0, rows, d.J0, d.D, j0, s));
+        DW_CHECK(MM<Act>::mm_act(p.J1, d.J0, wj1, p.J2, d.J1, rows, d.J1, d.J0, j1, s));
     }
     launch_jastrow_out<Act>(p.J2, d.J1, P + L.jas_w[2], d, Bc, p.jas, s);
     launch_combine(p.logdet, p.sign, p.g, p.lapdet, p.jas, r, R, Z, d, Bc, lp, phase, E_loc, grad, s);
@@ -258,21 +330,39 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
     return DW_OK;
 }
 
-static bool uses_bf16_acts(int precision) { return precision == DW_PRECISION_MIXED && tc_available(); }
+// Calls f(tag) with a null pointer of the activation type of the precision form.
+template <class F>
+static int with_act(int precision, bool need_device, F&& f) {
+    switch (precision) {
+        case DW_PRECISION_FP32: return f((float*)nullptr);
+        case DW_PRECISION_MIXED:
+            if (need_device && !tc_available()) return DW_ERR_UNSUPPORTED;
+            return f((Split*)nullptr);
+        case DW_PRECISION_BF16:
+            if (need_device && !tc_available()) return DW_ERR_UNSUPPORTED;
+            return f((__nv_bfloat16*)nullptr);
+        default: return DW_ERR_ARG;
+    }
+}
+template <class T> using act_of = typename std::remove_pointer<T>::type;
+
+template <class Act>
+static size_t plan_bytes(const DwArch* a, int B, bool tang) {
+    Dims d = make_dims(a, tang);
+    return (carve_plan<Act>(d, choose_chunk<Act>(d, std::max(B, 1)), nullptr).bytes + 4096 + 255) / 256 * 256;
+}
 
 template <class Act>
 static size_t ws_bytes_t(const DwArch* a, int n_walkers, int mode) {
-    Dims d = make_dims(a, mode == 1);
-    int bc = choose_chunk<Act>(d, std::max(n_walkers, 1));
-    size_t b = carve_plan<Act>(d, bc, nullptr).bytes + 4096;
     if (mode == 2) {
-        Dims dv = make_dims(a, false);
-        int bcv = choose_chunk<Act>(dv, std::max(n_walkers, 1));
-        b = carve_plan<Act>(dv, bcv, nullptr).bytes + 4096;
+        size_t b = plan_bytes<Act>(a, n_walkers, false);
         b += (size_t)n_walkers * a->n_el * 3 * sizeof(float) + 256;      // proposals
         b += (size_t)n_walkers * sizeof(float) + 256;                    // proposal log psi^2
         b += (size_t)mh_partials_needed(n_walkers) * sizeof(int) + 256;
+        return b;
     }
+    size_t b = plan_bytes<Act>(a, n_walkers, mode == 1);
+    if (mode == 1) b += (size_t)n_walkers * sizeof(float) + 256;         // log psi^2 when not requested
     return b;
 }
 
@@ -312,14 +402,15 @@ int dw_prepare_params(const DwArch* a, int precision, const float* params, void*
     reset_launch_count();
     DW_CHECK(check_arch(a));
     if (!params || !prepared) return DW_ERR_ARG;
-    if (precision != DW_PRECISION_FP32 && precision != DW_PRECISION_MIXED) return DW_ERR_ARG;
+    if (precision < DW_PRECISION_FP32 || precision > DW_PRECISION_BF16) return DW_ERR_ARG;
     return prepare(a, precision, params, prepared, bytes, (cudaStream_t)stream);
 }
 
 size_t dw_workspace_bytes(const DwArch* a, int precision, int n_walkers, int mode) {
     if (check_arch(a) != DW_OK || n_walkers <= 0) return 0;
-    if (uses_bf16_acts(precision)) return ws_bytes_t<__nv_bfloat16>(a, n_walkers, mode);
-    return ws_bytes_t<float>(a, n_walkers, mode);
+    size_t out = 0;
+    with_act(precision, false, [&](auto tag) { out = ws_bytes_t<act_of<decltype(tag)>>(a, n_walkers, mode); return 0; });
+    return out;
 }
 
 int dw_log_psi_sqr(const DwArch* a, int precision, const float* params, const void* prepared, const float* r,
@@ -328,9 +419,10 @@ int dw_log_psi_sqr(const DwArch* a, int precision, const float* params, const vo
     DW_CHECK(check_arch(a));
     if (!params || !prepared || !r || !R || !Z || !lp || B <= 0) return DW_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    if (uses_bf16_acts(precision))
-        return forward_all<__nv_bfloat16>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s);
-    return forward_all<float>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s);
+    return with_act(precision, true, [&](auto tag) {
+        using Act = act_of<decltype(tag)>;
+        return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s);
+    });
 }
 
 int dw_local_energy(const DwArch* a, int precision, const float* params, const void* prepared, const float* r, int B,
@@ -339,18 +431,18 @@ int dw_local_energy(const DwArch* a, int precision, const float* params, const v
     DW_CHECK(check_arch(a));
     if (!params || !prepared || !r || !R || !Z || !E || B <= 0) return DW_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    // log psi^2 output is optional; route it to the workspace tail when absent
-    Carver c(ws, wsb);
-    size_t plan_bytes = uses_bf16_acts(precision) ? carve_plan<__nv_bfloat16>(make_dims(a, true), choose_chunk<__nv_bfloat16>(make_dims(a, true), B), nullptr).bytes
-                                                   : carve_plan<float>(make_dims(a, true), choose_chunk<float>(make_dims(a, true), B), nullptr).bytes;
-    if (!lp) {
-        if (plan_bytes + (size_t)B * sizeof(float) + 512 > wsb) return DW_ERR_WORKSPACE;
-        lp = reinterpret_cast<float*>(static_cast<char*>(ws) + (plan_bytes + 255) / 256 * 256);
-        wsb = plan_bytes;
-    }
-    if (uses_bf16_acts(precision))
-        return forward_all<__nv_bfloat16>(a, precision, params, prepared, r, B, R, Z, lp, nullptr, E, grad, true, ws, wsb, s);
-    return forward_all<float>(a, precision, params, prepared, r, B, R, Z, lp, nullptr, E, grad, true, ws, wsb, s);
+    return with_act(precision, true, [&](auto tag) {
+        using Act = act_of<decltype(tag)>;
+        size_t pb = plan_bytes<Act>(a, B, true);
+        float* lpo = lp;
+        size_t fwd_bytes = wsb;
+        if (!lpo) {   // log psi^2 output is optional; it then lives in the workspace tail
+            if (pb + (size_t)B * sizeof(float) > wsb) return (int)DW_ERR_WORKSPACE;
+            lpo = reinterpret_cast<float*>(static_cast<char*>(ws) + pb);
+            fwd_bytes = pb;
+        }
+        return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, fwd_bytes, s);
+    });
 }
 
 int dw_potential_energy(const float* r, int B, int n, const float* R, const int32_t* Z, int N, float* E, void* stream) {
@@ -369,42 +461,41 @@ int dw_mcmc_steps(const DwArch* a, int precision, const float* params, const voi
     if (!params || !prepared || !r || !R || !Z || !lp || !age || !scalars || !cfg || B <= 0) return DW_ERR_ARG;
     if (cfg->n_steps < 0) return DW_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    bool bf = uses_bf16_acts(precision);
-    Dims dv = make_dims(a, false);
-    size_t fwd = bf ? carve_plan<__nv_bfloat16>(dv, choose_chunk<__nv_bfloat16>(dv, B), nullptr).bytes
-                    : carve_plan<float>(dv, choose_chunk<float>(dv, B), nullptr).bytes;
-    fwd = (fwd + 4096 + 255) / 256 * 256;
-    if (wsb < dw_workspace_bytes(a, precision, B, 2)) return DW_ERR_WORKSPACE;
-    char* tail = static_cast<char*>(ws) + fwd;
-    Carver c(tail, wsb - fwd);
-    float* r_prop = c.take<float>((size_t)B * a->n_el * 3);
-    float* lp_prop = c.take<float>((size_t)B);
-    int* partials = c.take<int>((size_t)mh_partials_needed(B));
-    if (!c.ok()) return DW_ERR_WORKSPACE;
-    auto fwd_call = [&](const float* rr, float* out) {
-        if (bf) return forward_all<__nv_bfloat16>(a, precision, params, prepared, rr, B, R, Z, out, nullptr, nullptr, nullptr, false, ws, fwd, s);
-        return forward_all<float>(a, precision, params, prepared, rr, B, R, Z, out, nullptr, nullptr, nullptr, false, ws, fwd, s);
-    };
-    int64_t launches = 0;
-    if (cfg->reevaluate) { DW_CHECK(fwd_call(r, lp)); launches += launch_count(); }   // mcmc.py:396
-    if (cfg->n_steps == 0) return DW_OK;
-    MhArgs m;
-    m.r = r; m.r_prop = r_prop; m.lp = lp; m.lp_prop = lp_prop; m.age = age; m.scalars = scalars; m.partials = partials;
-    m.B = B; m.n = a->n_el; m.max_age = cfg->max_age; m.interval = cfg->stepsize_update_interval;
-    m.target = cfg->target_acceptance_rate; m.min_step = cfg->min_stepsize; m.max_step = cfg->max_stepsize; m.seed = cfg->seed;
-    reset_launch_count();
-    launch_mh(m, 0, s);
-    launches += launch_count();
-    for (int k = 0; k < cfg->n_steps; ++k) {
+    return with_act(precision, true, [&](auto tag) {
+        using Act = act_of<decltype(tag)>;
+        if (wsb < ws_bytes_t<Act>(a, B, 2)) return (int)DW_ERR_WORKSPACE;
+        size_t fwd = plan_bytes<Act>(a, B, false);
+        Carver c(static_cast<char*>(ws) + fwd, wsb - fwd);
+        float* r_prop = c.take<float>((size_t)B * a->n_el * 3);
+        float* lp_prop = c.take<float>((size_t)B);
+        int* partials = c.take<int>((size_t)mh_partials_needed(B));
+        if (!c.ok()) return (int)DW_ERR_WORKSPACE;
+        auto fwd_call = [&](const float* rr, float* out) {
+            return forward_all<Act>(a, precision, params, prepared, rr, B, R, Z, out, nullptr, nullptr, nullptr, false,
+                                    ws, fwd, s);
+        };
+        int64_t launches = 0;
+        if (cfg->reevaluate) { DW_CHECK(fwd_call(r, lp)); launches += launch_count(); }   // mcmc.py:396
+        if (cfg->n_steps == 0) return (int)DW_OK;
+        MhArgs m;
+        m.r = r; m.r_prop = r_prop; m.lp = lp; m.lp_prop = lp_prop; m.age = age; m.scalars = scalars;
+        m.partials = partials; m.B = B; m.n = a->n_el; m.max_age = cfg->max_age;
+        m.interval = cfg->stepsize_update_interval; m.target = cfg->target_acceptance_rate;
+        m.min_step = cfg->min_stepsize; m.max_step = cfg->max_stepsize; m.seed = cfg->seed;
         reset_launch_count();
-        DW_CHECK(fwd_call(r_prop, lp_prop));
-        launch_mh(m, k + 1 < cfg->n_steps ? 1 : 2, s);
+        launch_mh(m, 0, s);
         launches += launch_count();
-    }
-    reset_launch_count();
-    count_launch((int)launches);
-    DW_CHECK_CUDA(cudaGetLastError());
-    return DW_OK;
+        for (int k = 0; k < cfg->n_steps; ++k) {
+            reset_launch_count();
+            DW_CHECK(fwd_call(r_prop, lp_prop));
+            launch_mh(m, k + 1 < cfg->n_steps ? 1 : 2, s);
+            launches += launch_count();
+        }
+        reset_launch_count();
+        count_launch((int)launches);
+        DW_CHECK_CUDA(cudaGetLastError());
+        return (int)DW_OK;
+    });
 }
 
 int dw_energy_stats(const float* E, int n, double* out, void* stream) {

@@ -11,7 +11,7 @@
 #define DW_CHECK_CUDA(x)                                   \
     do {                                                   \
         cudaError_t _e = (x);                              \
-        if (_e != cudaSuccess) { dw::set_last_cuda_error(_e); return DW_ERR_CUDA; } \
+        if (_e != cudaSuccess) { dw::set_last_cuda_error(_e); return (int)DW_ERR_CUDA; } \
     } while (0)
 
 #define DW_CHECK(x)                                        \
@@ -23,6 +23,12 @@ void set_last_cuda_error(cudaError_t e);
 void count_launch(int n = 1);
 int64_t launch_count();
 void reset_launch_count();
+
+// Optional per-tag kernel timing with CUDA events recorded on the launching stream
+// (enabled by dw_timer_enable; used to measure a kernel's live duration inside a run).
+bool timer_on();
+void timer_begin(const char* tag, cudaStream_t s);
+void timer_end(const char* tag, cudaStream_t s, double flops, double bytes);
 
 constexpr int kAlignFloats = 64;      // packed-parameter alignment (floats)
 constexpr int kMaxEl = 64;

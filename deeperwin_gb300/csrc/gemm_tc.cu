@@ -87,16 +87,23 @@ struct TcArgs {
     uint32_t tmem_cols;
 };
 
-template <bool OUT_BF16>
+// NP = 1: plain BF16 operands, one MMA per 16-wide K step.
+// NP = 2: split-BF16 operands A = A_hi + A_lo, W = W_hi + W_lo; three MMAs per K step
+//         (A_hi W_hi + A_hi W_lo + A_lo W_hi) into the same FP32 TMEM accumulator.
+// OUT = 0: fp32 C; 1: bf16 C; 2: split-BF16 C ([hi | lo] rows of logical width ldc).
+template <int NP, int OUT>
 __global__ void __launch_bounds__(128, 1)
-k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
+k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
+          const __grid_constant__ CUtensorMap tmB0, const __grid_constant__ CUtensorMap tmB1, TcArgs a) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int S = a.stages, BN = a.BN;
     const uint32_t a_bytes = BM * BK * 2, b_bytes = (uint32_t)BN * BK * 2;
-    uint8_t* sA = smem;
-    uint8_t* sB = smem + (size_t)S * a_bytes;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sB + (size_t)S * b_bytes);
+    const uint32_t stage_bytes = NP * (a_bytes + b_bytes);
+    // stage s: [A_0 | A_1 | B_0 | B_1]
+    auto sA = [&](int s, int part) { return smem + (size_t)s * stage_bytes + (size_t)part * a_bytes; };
+    auto sB = [&](int s, int part) { return smem + (size_t)s * stage_bytes + (size_t)NP * a_bytes + (size_t)part * b_bytes; };
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)S * stage_bytes);
     uint64_t* empty = full + S;
     uint64_t* done = empty + S;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
@@ -129,23 +136,32 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
         for (int kt = 0; kt < nk; ++kt) {
             int s = kt % S;
             if (kt >= S && !mbar_wait(&empty[s], ((kt / S) - 1) & 1)) { atomicExch(&s_err, 1); break; }
-            mbar_expect_tx(&full[s], a_bytes + b_bytes);
-            tma_load_2d(sA + (size_t)s * a_bytes, &tmA, &full[s], kt * BK, row_a);
-            tma_load_2d(sB + (size_t)s * b_bytes, &tmB, &full[s], kt * BK, n0);
+            mbar_expect_tx(&full[s], stage_bytes);
+            tma_load_2d(sA(s, 0), &tmA0, &full[s], kt * BK, row_a);
+            tma_load_2d(sB(s, 0), &tmB0, &full[s], kt * BK, n0);
+            if (NP == 2) {
+                tma_load_2d(sA(s, 1), &tmA1, &full[s], kt * BK, row_a);
+                tma_load_2d(sB(s, 1), &tmB1, &full[s], kt * BK, n0);
+            }
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         const uint32_t idesc = idesc_bf16(BN);
-        int kt = 0;
-        for (; kt < nk; ++kt) {
+        for (int kt = 0; kt < nk; ++kt) {
             int s = kt % S;
             if (!mbar_wait(&full[s], (kt / S) & 1)) { atomicExch(&s_err, 1); break; }
             tc_fence_after();
-            uint64_t ad = smem_desc_sw128(sA + (size_t)s * a_bytes);
-            uint64_t bd = smem_desc_sw128(sB + (size_t)s * b_bytes);
+            uint64_t a0 = smem_desc_sw128(sA(s, 0)), b0 = smem_desc_sw128(sB(s, 0));
+            uint64_t a1 = smem_desc_sw128(sA(s, NP - 1)), b1 = smem_desc_sw128(sB(s, NP - 1));
             #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk)
-                umma_bf16(tmem, ad + (uint64_t)(kk * 2), bd + (uint64_t)(kk * 2), idesc, (kt | kk) ? 1u : 0u);
+            for (int kk = 0; kk < BK / 16; ++kk) {
+                const uint64_t o = (uint64_t)(kk * 2);
+                umma_bf16(tmem, a0 + o, b0 + o, idesc, (kt | kk) ? 1u : 0u);
+                if (NP == 2) {
+                    umma_bf16(tmem, a0 + o, b1 + o, idesc, 1u);
+                    umma_bf16(tmem, a1 + o, b0 + o, idesc, 1u);
+                }
+            }
             umma_commit(&empty[s]);
         }
         umma_commit(done);
@@ -172,10 +188,13 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
                     if (e.bias && t == 0) x += e.bias[n];
                     if (rb) x += rb[n];
                     if (e.act == 1) x = tanhf(x);
-                    if (OUT_BF16)
-                        reinterpret_cast<__nv_bfloat16*>(a.C)[z * a.sC + (int64_t)m * a.ldc + n] = __float2bfloat16_rn(x);
-                    else
+                    if (OUT == 0) {
                         reinterpret_cast<float*>(a.C)[z * a.sC + (int64_t)m * a.ldc + n] = x;
+                    } else if (OUT == 1) {
+                        reinterpret_cast<__nv_bfloat16*>(a.C)[z * a.sC + (int64_t)m * a.ldc + n] = __float2bfloat16_rn(x);
+                    } else {
+                        ActIO<Split>::store(reinterpret_cast<Split*>(a.C) + z * a.sC, m, a.ldc, n, x);
+                    }
                 }
             }
         }
@@ -229,28 +248,39 @@ int make_map(CUtensorMap* map, const void* base, int64_t rows, int cols, int ld,
     return r == CUDA_SUCCESS ? DW_OK : DW_ERR_ARG;
 }
 
-template <bool OUT_BF16>
-int launch_tc(const __nv_bfloat16* A, int lda, int64_t a_rows_total, const __nv_bfloat16* Wt, void* C, int ldc, int M,
-              int N, int K, const GemmEpi& epi, int batch, int64_t a_rows_per_batch, int64_t sC, cudaStream_t s) {
+// A: np parts of a logical [rows, lda] activation (np = 2: [hi | lo] rows of width 2 lda).
+// W0/W1: [N, round_up(K, 64)] K-major weight parts.
+template <int NP, int OUT>
+int launch_tc(const __nv_bfloat16* A, int lda, int64_t a_rows_total, const __nv_bfloat16* W0, const __nv_bfloat16* W1,
+              void* C, int ldc, int M, int N, int K, const GemmEpi& epi, int batch, int64_t a_rows_per_batch, int64_t sC,
+              cudaStream_t s) {
     if (M <= 0 || N <= 0 || K <= 0) return DW_OK;
-    int ntiles = (N + 255) / 256;
+    const int bn_max = NP == 2 ? 128 : 256;
+    int ntiles = (N + bn_max - 1) / bn_max;
     int BN = round_up((N + ntiles - 1) / ntiles, 16);
     int Kp = round_up(K, 64);
-    CUtensorMap ma, mb;
-    DW_CHECK(make_map(&ma, A, a_rows_total, K, lda, BM));
-    DW_CHECK(make_map(&mb, Wt, N, K, Kp, BN));
+    CUtensorMap ma0, ma1, mb0, mb1;
+    const int phys_ld = NP * lda;
+    DW_CHECK(make_map(&ma0, A, a_rows_total, K, phys_ld, BM));
+    DW_CHECK(make_map(&mb0, W0, N, K, Kp, BN));
+    if (NP == 2) {
+        DW_CHECK(make_map(&ma1, A + lda, a_rows_total, K, phys_ld, BM));
+        DW_CHECK(make_map(&mb1, W1, N, K, Kp, BN));
+    } else {
+        ma1 = ma0; mb1 = mb0;
+    }
     TcArgs a;
     a.C = C; a.ldc = ldc; a.M = M; a.N = N; a.K = K; a.BN = BN;
     a.a_rows_per_batch = a_rows_per_batch; a.sC = sC; a.epi = epi;
-    int stage_bytes = BM * BK * 2 + BN * BK * 2;
+    int stage_bytes = NP * (BM * BK * 2 + BN * BK * 2);
     a.stages = std::min(4, (200 * 1024) / stage_bytes);
     a.tmem_cols = 32;
     while ((int)a.tmem_cols < BN) a.tmem_cols <<= 1;
     size_t smem = 1024 + (size_t)a.stages * stage_bytes + (2 * a.stages + 1) * 8 + 16;
-    auto kern = k_gemm_tc<OUT_BF16>;
+    auto kern = k_gemm_tc<NP, OUT>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid(ntiles, (M + BM - 1) / BM, batch);
-    kern<<<grid, 128, smem, s>>>(ma, mb, a);
+    kern<<<grid, 128, smem, s>>>(ma0, ma1, mb0, mb1, a);
     count_launch();
     DW_CHECK_CUDA(cudaGetLastError());
     return DW_OK;
@@ -273,19 +303,33 @@ bool tc_available() {
 
 int gemm_bf16_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* Wt, float* C, int ldc, int M, int N, int K,
                  const GemmEpi& epi, cudaStream_t s) {
-    return launch_tc<false>(A, lda, M, Wt, C, ldc, M, N, K, epi, 1, 0, 0, s);
+    return launch_tc<1, 0>(A, lda, M, Wt, nullptr, C, ldc, M, N, K, epi, 1, 0, 0, s);
 }
 int gemm_bf16_tc_act(const __nv_bfloat16* A, int lda, const __nv_bfloat16* Wt, __nv_bfloat16* C, int ldc, int M, int N,
                      int K, const GemmEpi& epi, cudaStream_t s) {
-    return launch_tc<true>(A, lda, M, Wt, C, ldc, M, N, K, epi, 1, 0, 0, s);
+    return launch_tc<1, 1>(A, lda, M, Wt, nullptr, C, ldc, M, N, K, epi, 1, 0, 0, s);
 }
 int gemm_bf16_tc_batched(const __nv_bfloat16* A, int lda, const __nv_bfloat16* Wt, float* C, int ldc, int M, int N, int K,
                          int batch, int64_t sA, int64_t sC, cudaStream_t s) {
     GemmEpi e;
-    // rows of batch z start sA / lda rows after A
     int64_t rows_per_batch = sA / lda;
     int64_t rows_total = rows_per_batch * (batch - 1) + M;
-    return launch_tc<false>(A, lda, rows_total, Wt, C, ldc, M, N, K, e, batch, rows_per_batch, sC, s);
+    return launch_tc<1, 0>(A, lda, rows_total, Wt, nullptr, C, ldc, M, N, K, e, batch, rows_per_batch, sC, s);
+}
+int gemm_split_tc(const Split* A, int lda, const __nv_bfloat16* Whi, const __nv_bfloat16* Wlo, float* C, int ldc, int M,
+                  int N, int K, const GemmEpi& epi, cudaStream_t s) {
+    return launch_tc<2, 0>(reinterpret_cast<const __nv_bfloat16*>(A), lda, M, Whi, Wlo, C, ldc, M, N, K, epi, 1, 0, 0, s);
+}
+int gemm_split_tc_act(const Split* A, int lda, const __nv_bfloat16* Whi, const __nv_bfloat16* Wlo, Split* C, int ldc,
+                      int M, int N, int K, const GemmEpi& epi, cudaStream_t s) {
+    return launch_tc<2, 2>(reinterpret_cast<const __nv_bfloat16*>(A), lda, M, Whi, Wlo, C, ldc, M, N, K, epi, 1, 0, 0, s);
+}
+int gemm_split_tc_batched(const Split* A, int lda, const __nv_bfloat16* Whi, const __nv_bfloat16* Wlo, float* C, int ldc,
+                          int M, int N, int K, int batch, int64_t rows_per_batch, int64_t sC, cudaStream_t s) {
+    GemmEpi e;
+    int64_t rows_total = rows_per_batch * (batch - 1) + M;
+    return launch_tc<2, 0>(reinterpret_cast<const __nv_bfloat16*>(A), lda, rows_total, Whi, Wlo, C, ldc, M, N, K, e, batch,
+                           rows_per_batch, sC, s);
 }
 
 }  // namespace dw
@@ -293,9 +337,14 @@ int gemm_bf16_tc_batched(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W
 extern "C" {
 
 // Test hook: C[M,N] (fp32) = A[M,K] (bf16, row stride lda) @ Wt[N,K]^T (bf16, row stride round_up(K,64)).
-int dw_debug_gemm_bf16(const void* A, int lda, const void* Wt, float* C, int ldc, int M, int N, int K, void* stream) {
+// With Wt_lo != NULL, A is split-BF16 ([hi | lo] rows of logical width lda) and W = Wt + Wt_lo.
+int dw_debug_gemm_bf16(const void* A, int lda, const void* Wt, const void* Wt_lo, float* C, int ldc, int M, int N, int K,
+                       void* stream) {
     if (!dw::tc_available()) return DW_ERR_UNSUPPORTED;
     dw::GemmEpi e;
+    if (Wt_lo)
+        return dw::gemm_split_tc((const dw::Split*)A, lda, (const __nv_bfloat16*)Wt, (const __nv_bfloat16*)Wt_lo, C, ldc,
+                                 M, N, K, e, (cudaStream_t)stream);
     return dw::gemm_bf16_tc((const __nv_bfloat16*)A, lda, (const __nv_bfloat16*)Wt, C, ldc, M, N, K, e, (cudaStream_t)stream);
 }
 

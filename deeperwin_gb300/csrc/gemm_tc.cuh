@@ -17,4 +17,12 @@ int gemm_bf16_tc_act(const __nv_bfloat16* A, int lda, const __nv_bfloat16* Wt, _
 int gemm_bf16_tc_batched(const __nv_bfloat16* A, int lda, const __nv_bfloat16* Wt, float* C, int ldc, int M, int N, int K,
                          int batch, int64_t sA, int64_t sC, cudaStream_t s);
 
+// Split-BF16 operands (three MMAs per K step): A is [hi | lo] rows of logical width lda.
+int gemm_split_tc(const Split* A, int lda, const __nv_bfloat16* Whi, const __nv_bfloat16* Wlo, float* C, int ldc, int M,
+                  int N, int K, const GemmEpi& epi, cudaStream_t s);
+int gemm_split_tc_act(const Split* A, int lda, const __nv_bfloat16* Whi, const __nv_bfloat16* Wlo, Split* C, int ldc,
+                      int M, int N, int K, const GemmEpi& epi, cudaStream_t s);
+int gemm_split_tc_batched(const Split* A, int lda, const __nv_bfloat16* Whi, const __nv_bfloat16* Wlo, float* C, int ldc,
+                          int M, int N, int K, int batch, int64_t rows_per_batch, int64_t sC, cudaStream_t s);
+
 }  // namespace dw

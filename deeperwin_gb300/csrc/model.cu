@@ -3,6 +3,9 @@
 // tensor order, each tensor row-major and starting at a multiple of 64 floats.
 #include "common.cuh"
 #include <string.h>
+#include <map>
+#include <string>
+#include <vector>
 
 namespace dw {
 
@@ -12,6 +15,34 @@ void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
 void count_launch(int n) { g_launches += n; }
 int64_t launch_count() { return g_launches; }
 void reset_launch_count() { g_launches = 0; }
+
+struct TimerSlot {
+    std::vector<cudaEvent_t> pending;   // start/end pairs not yet read
+    cudaEvent_t open = nullptr;
+    double ms = 0, flops = 0, bytes = 0;
+    int64_t launches = 0;
+};
+static std::map<std::string, TimerSlot> g_timers;
+static bool g_timer_on = false;
+bool timer_on() { return g_timer_on; }
+void timer_begin(const char* tag, cudaStream_t s) {
+    if (!g_timer_on) return;
+    TimerSlot& t = g_timers[tag];
+    cudaEventCreate(&t.open);
+    cudaEventRecord(t.open, s);
+}
+void timer_end(const char* tag, cudaStream_t s, double flops, double bytes) {
+    if (!g_timer_on) return;
+    TimerSlot& t = g_timers[tag];
+    if (!t.open) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, s);
+    t.pending.push_back(t.open);
+    t.pending.push_back(e);
+    t.open = nullptr;
+    t.flops += flops; t.bytes += bytes; t.launches += 1;
+}
 
 int check_arch(const DwArch* a) {
     if (!a) return DW_ERR_ARG;
@@ -140,5 +171,33 @@ int dw_param_layout(const DwArch* a, int64_t* offsets, int64_t* sizes, int max_e
 }
 
 int64_t dw_last_launch_count(void) { return dw::launch_count(); }
+
+// Enables (1) or disables (0) per-tag kernel timing and clears accumulated timings.
+int dw_timer_enable(int on) {
+    for (auto& kv : dw::g_timers)
+        for (cudaEvent_t e : kv.second.pending) cudaEventDestroy(e);
+    dw::g_timers.clear();
+    dw::g_timer_on = on != 0;
+    return DW_OK;
+}
+
+// Synchronizes the recorded events of `tag` and returns total milliseconds, launch count and
+// the algorithmic FLOPs / bytes of those launches.
+int dw_timer_read(const char* tag, double* ms, int64_t* launches, double* flops, double* bytes) {
+    auto it = dw::g_timers.find(tag);
+    if (it == dw::g_timers.end()) { *ms = 0; *launches = 0; *flops = 0; *bytes = 0; return DW_OK; }
+    dw::TimerSlot& t = it->second;
+    for (size_t k = 0; k + 1 < t.pending.size(); k += 2) {
+        float x = 0.f;
+        if (cudaEventSynchronize(t.pending[k + 1]) != cudaSuccess) return DW_ERR_CUDA;
+        cudaEventElapsedTime(&x, t.pending[k], t.pending[k + 1]);
+        t.ms += x;
+        cudaEventDestroy(t.pending[k]);
+        cudaEventDestroy(t.pending[k + 1]);
+    }
+    t.pending.clear();
+    *ms = t.ms; *launches = t.launches; *flops = t.flops; *bytes = t.bytes;
+    return DW_OK;
+}
 
 }  // extern "C"

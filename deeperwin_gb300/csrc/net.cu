@@ -68,7 +68,7 @@ __global__ void k_features(const float* __restrict__ r, const float* __restrict_
                 if (m == i) v = q == 0 ? s[c] / dd : (q - 1 == c ? 1.f : 0.f);
             }
         }
-        X0[(row0 + t) * width + col] = from_f<Act>(v);
+        ActIO<Act>::store(X0, row0 + t, width, col, v);
     }
 }
 
@@ -186,10 +186,10 @@ __global__ void k_spin_means(const Act* __restrict__ X, int ldx, int hw, Dims d,
         if (col < 2 * hw) {
             int f = col % hw;
             int i0 = col < hw ? 0 : d.nu, i1 = col < hw ? d.nu : d.n;
-            for (int i = i0; i < i1; ++i) v += to_f(X[((int64_t)(b * d.n + i) * d.Tp + t) * ldx + f]);
+            for (int i = i0; i < i1; ++i) v += ActIO<Act>::load(X, (int64_t)(b * d.n + i) * d.Tp + t, ldx, f);
             v /= (float)(i1 - i0);
         }
-        M[((int64_t)b * d.Tp + t) * mw + col] = from_f<Act>(v);
+        ActIO<Act>::store(M, (int64_t)b * d.Tp + t, mw, col, v);
     }
 }
 
@@ -203,19 +203,19 @@ __global__ void k_tanh_fl(const float* __restrict__ Zb, int ldz, int ncols, int 
     int64_t g = idx / ncols;
     int f = idx % ncols;
     const float* z = Zb + g * d.Tp * ldz + f;
-    Act* y = Y + g * d.Tp * ldy + f;
+    const int64_t r0 = g * d.Tp;
     float z0 = z[0];
     float y0 = tanhf(z0), d1 = 1.f - y0 * y0;
-    y[0] = from_f<Act>(y0);
+    ActIO<Act>::store(Y, r0, ldy, f, y0);
     if (d.Tp == 1) return;
     float s = 0.f;
     for (int t = 1; t <= 3 * d.n; ++t) {
         float zt = z[(int64_t)t * ldz];
         s += zt * zt;
-        y[(int64_t)t * ldy] = from_f<Act>(d1 * zt);
+        ActIO<Act>::store(Y, r0 + t, ldy, f, d1 * zt);
     }
-    y[(int64_t)d.lap * ldy] = from_f<Act>(d1 * z[(int64_t)d.lap * ldz] - 2.f * y0 * d1 * s);
-    for (int t = d.lap + 1; t < d.Tp; ++t) y[(int64_t)t * ldy] = from_f<Act>(0.f);
+    ActIO<Act>::store(Y, r0 + d.lap, ldy, f, d1 * z[(int64_t)d.lap * ldz] - 2.f * y0 * d1 * s);
+    for (int t = d.lap + 1; t < d.Tp; ++t) ActIO<Act>::store(Y, r0 + t, ldy, f, 0.f);
 }
 
 // ------------------------------------------------------------------ SchNet convolutions
@@ -285,7 +285,7 @@ __global__ void k_conv(const float* __restrict__ r, const float* __restrict__ WP
                 }
             }
         }
-        X[((int64_t)bi * d.Tp + t) * ldx + hw + col] = from_f<Act>(v);
+        ActIO<Act>::store(X, (int64_t)bi * d.Tp + t, ldx, hw + col, v);
     }
 }
 
@@ -345,8 +345,8 @@ __global__ void k_jastrow_out(const Act* __restrict__ J2, int ldj, const float* 
     int b = warp / d.Tp, t = warp % d.Tp;
     float acc = 0.f;
     for (int i = 0; i < d.n; ++i) {
-        const Act* row = J2 + ((int64_t)(b * d.n + i) * d.Tp + t) * ldj;
-        for (int f = lane; f < d.J1; f += 32) acc += to_f(row[f]) * w2[f];
+        const int64_t row = (int64_t)(b * d.n + i) * d.Tp + t;
+        for (int f = lane; f < d.J1; f += 32) acc += ActIO<Act>::load(J2, row, ldj, f) * w2[f];
     }
     acc = warp_sum(acc);
     if (lane == 0) jas[(int64_t)b * d.Tp + t] = acc;
@@ -403,5 +403,6 @@ void launch_jastrow_out(const Act* J2, int ldj, const float* w2, const Dims& d, 
     template void launch_jastrow_out<Act>(const Act*, int, const float*, const Dims&, int, double*, cudaStream_t);
 DW_INST(float)
 DW_INST(__nv_bfloat16)
+DW_INST(Split)
 
 }  // namespace dw

@@ -10,6 +10,34 @@ template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float
 __device__ __forceinline__ float to_f(float v) { return v; }
 __device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
 
+// Storage element of split-BF16 activations: a logical row of width ld is stored as
+// [hi(0..ld) | lo(0..ld)] with hi = bf16(x), lo = bf16(x - hi); x is recovered as hi + lo
+// to about 2^-17 relative. Tensor-core GEMMs consume hi and lo as two BF16 operands.
+struct Split { __nv_bfloat16 v; };
+
+// act_store / act_load address element (row, col) of a logical [rows, ld] activation.
+template <class Act> struct ActIO {
+    static constexpr int kParts = 1;
+    __device__ static __forceinline__ void store(Act* b, int64_t row, int ld, int col, float x) {
+        b[row * ld + col] = from_f<Act>(x);
+    }
+    __device__ static __forceinline__ float load(const Act* b, int64_t row, int ld, int col) {
+        return to_f(b[row * ld + col]);
+    }
+};
+template <> struct ActIO<Split> {
+    static constexpr int kParts = 2;
+    __device__ static __forceinline__ void store(Split* b, int64_t row, int ld, int col, float x) {
+        __nv_bfloat16 hi = __float2bfloat16_rn(x);
+        __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+        b[row * 2 * ld + col].v = hi;
+        b[row * 2 * ld + ld + col].v = lo;
+    }
+    __device__ static __forceinline__ float load(const Split* b, int64_t row, int ld, int col) {
+        return __bfloat162float(b[row * 2 * ld + col].v) + __bfloat162float(b[row * 2 * ld + ld + col].v);
+    }
+};
+
 // net.cu
 void launch_ion_maps(const float* P, const ParamLayout& L, const Dims& d, const int32_t* Z, float* him, cudaStream_t s);
 template <class Act> void launch_features(const float* r, const float* R, const Dims& d, int B, Act* X0, cudaStream_t s);

@@ -56,8 +56,10 @@ enum DwStatus {
 };
 
 enum DwPrecision {
-    DW_PRECISION_FP32 = 0,  /* plain form: FP32 end to end */
-    DW_PRECISION_MIXED = 1  /* BF16 GEMMs (FP32 accumulate) + FP64 LU / trace / reductions */
+    DW_PRECISION_FP32 = 0,  /* plain form: FP32 end to end (CUDA-core GEMMs, FP32 LU) */
+    DW_PRECISION_MIXED = 1, /* tensor-core GEMMs on split-BF16 operands (hi + lo, three BF16 MMAs per
+                               K step, FP32 accumulate) + FP64 LU / trace / reductions */
+    DW_PRECISION_BF16 = 2   /* single-pass BF16 tensor-core GEMMs + FP64 LU (fastest, least accurate) */
 };
 
 /* Human-readable text for a status code (static storage). */
@@ -162,6 +164,13 @@ int dw_log_psi_sqr_backward(const DwArch* arch, int precision, const float* para
 
 /* Number of kernel launches issued by the last call on this host thread (instrumentation). */
 int64_t dw_last_launch_count(void);
+
+/* Instrumentation: per-tag CUDA-event timing of selected kernels on their launch stream
+ * ("layer_gemm" = the widened forward-Laplacian layer GEMMs). dw_timer_enable clears the
+ * accumulators; dw_timer_read synchronizes the recorded events and returns the total time (ms),
+ * launch count, and the algorithmic FLOPs and bytes of those launches. No reference counterpart. */
+int dw_timer_enable(int on);
+int dw_timer_read(const char* tag, double* ms, int64_t* launches, double* flops, double* bytes);
 
 #ifdef __cplusplus
 }

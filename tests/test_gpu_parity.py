@@ -1,11 +1,12 @@
 """GPU parity tests: the CUDA path through the C ABI against the FP64 oracle and the golden
 vectors generated from the reference's source.
 
-Tolerances (stated per the precision forms):
-* plain FP32 form: log psi^2 and E_L within 1e-5 relative of the FP64 oracle
-  (plus a small absolute floor for values near zero);
-* mixed BF16/FP64 form: log psi^2 within 2e-3 relative, E_L per-walker error reported in mHa
-  with a bound, mean E_L within the bound stated in the test.
+Tolerances (per precision form). S is the magnitude scale of the terms summed into E_L,
+S = 1/4 |Lap log psi^2| + 1/8 |grad log psi^2|^2 + |V|, taken from the oracle:
+* plain FP32 form: log psi^2 within 1e-5 relative (+1e-4 absolute); E_L within 5e-5 S;
+* mixed form (split-BF16 tensor-core GEMMs, FP64 LU/trace): log psi^2 within 1e-4 relative
+  (+1e-3 absolute); E_L within 1e-4 S;
+* single-pass BF16 form: E_L within 2e-2 S (reported, not the production form).
 """
 import glob
 from pathlib import Path
@@ -29,25 +30,47 @@ def _fixture(f):
     return d, a, p
 
 
-def test_tc_gemm_matches_torch(cuda):
+def _split(x):
+    hi = x.to(torch.bfloat16)
+    lo = (x - hi.float()).to(torch.bfloat16)
+    return hi, lo
+
+
+@pytest.mark.parametrize("split", [False, True], ids=["bf16", "split_bf16"])
+def test_tc_gemm_matches_torch(cuda, split):
     from deeperwin_gb300 import _lib
     import ctypes
     L = _lib.lib()
     g = torch.Generator(device="cpu").manual_seed(0)
     for (M, N, K, lda) in [(300, 256, 320, 320), (129, 32, 40, 64), (1000, 160, 256, 320), (77, 48, 256, 256),
                            (512, 64, 64, 64)]:
-        A_ = torch.randn(M, lda, generator=g).to(torch.bfloat16).cuda()
+        Af = torch.randn(M, lda, generator=g, dtype=torch.float64)
         Kp = (K + 63) // 64 * 64
-        W = torch.randn(N, Kp, generator=g).to(torch.bfloat16).cuda()
+        Wf = torch.randn(N, Kp, generator=g, dtype=torch.float64)
         C = torch.full((M, N), float("nan"), device="cuda")
-        st = L.dw_debug_gemm_bf16(ctypes.c_void_p(A_.data_ptr()), lda, ctypes.c_void_p(W.data_ptr()),
+        if split:
+            ah, al = _split(Af.float())
+            A_ = torch.cat([ah, al], dim=1).cuda().contiguous()
+            wh, wl = _split(Wf.float())
+            wh, wl = wh.cuda().contiguous(), wl.cuda().contiguous()
+            lo_ptr = ctypes.c_void_p(wl.data_ptr())
+        else:
+            A_ = Af.to(torch.bfloat16).cuda()
+            wh = Wf.to(torch.bfloat16).cuda()
+            lo_ptr = ctypes.c_void_p(0)
+        st = L.dw_debug_gemm_bf16(ctypes.c_void_p(A_.data_ptr()), lda, ctypes.c_void_p(wh.data_ptr()), lo_ptr,
                                   ctypes.c_void_p(C.data_ptr()), N, M, N, K, ctypes.c_void_p(0))
         assert st == 0
         torch.cuda.synchronize()
         assert L.dw_debug_tc_error_flag() == 0
-        ref = A_[:, :K].float() @ W[:, :K].float().T
+        if split:
+            ref = (Af[:, :K] @ Wf[:, :K].T).float().cuda()      # split-BF16 tracks the FP32/FP64 product
+            tol = 2e-5
+        else:
+            ref = A_[:, :K].float() @ wh[:, :K].float().T
+            tol = 1e-5
         err = (C - ref).abs().max().item()
-        assert err <= 1e-3 * ref.abs().max().item(), (M, N, K, err)
+        assert err <= tol * ref.abs().max().item() * (K ** 0.5), (M, N, K, err)
 
 
 @pytest.mark.parametrize("f", GOLDEN, ids=lambda f: f.split("/")[-1])
@@ -67,7 +90,7 @@ def test_forward_mixed_matches_reference_golden(cuda, f):
     params = api.Params.from_dict(a, p, "mixed")
     ph, lp = api.log_psi_sqr(params, a.n_up, a.n_dn, d["r"], d["R"], d["Z"])
     lp = lp.cpu().numpy().astype(np.float64)
-    np.testing.assert_allclose(lp, d["log_psi_sqr"], rtol=2e-3, atol=2e-2)
+    np.testing.assert_allclose(lp, d["log_psi_sqr"], rtol=1e-4, atol=1e-3)
 
 
 def _le_case(name):
@@ -81,7 +104,8 @@ def _le_case(name):
     p = P.init_params(a, 0, bias_std=0.1, envelope_jitter=0.2)
     r = A.init_walkers(mol, B, seed=11)
     E, lp, g, lap = O.local_energy(O.tparams(p), a, r, mol.R, mol.Z)
-    return mol, a, p, r, E.numpy(), lp.numpy(), g.numpy()
+    S = 0.25 * np.abs(lap.numpy()) + 0.125 * (g.numpy() ** 2).sum(-1) + np.abs(O.potential_energy(r, mol.R, mol.Z).numpy())
+    return mol, a, p, r, E.numpy(), lp.numpy(), g.numpy(), S
 
 
 @pytest.fixture(scope="module")
@@ -91,25 +115,40 @@ def le_cases():
 
 @pytest.mark.parametrize("name", ["lih", "h6", "h10"])
 def test_local_energy_plain(cuda, le_cases, name):
-    mol, a, p, r, E_ref, lp_ref, g_ref = le_cases[name]
+    mol, a, p, r, E_ref, lp_ref, g_ref, S = le_cases[name]
     params = api.Params.from_dict(a, p, "fp32")
     E, lp, g = api.local_energy(params, (a.n_up, a.n_dn), r, mol.R, mol.Z, return_grad=True)
     E = E.cpu().numpy().astype(np.float64)
     np.testing.assert_allclose(lp.cpu().numpy(), lp_ref, rtol=1e-5, atol=1e-4)
     np.testing.assert_allclose(g.cpu().numpy(), g_ref, rtol=1e-4, atol=1e-3 * np.abs(g_ref).max())
-    # 1e-5 relative to the scale of the kinetic terms entering E_L
-    scale = np.maximum(np.abs(E_ref), 1.0)
-    assert np.all(np.abs(E - E_ref) <= 1e-5 * scale * 10), (E, E_ref)
+    assert np.all(np.abs(E - E_ref) <= 5e-5 * S), (E, E_ref, S)
 
 
 @pytest.mark.parametrize("name", ["lih", "h6", "h10"])
-def test_local_energy_mixed(cuda, le_cases, name):
-    mol, a, p, r, E_ref, lp_ref, g_ref = le_cases[name]
-    params = api.Params.from_dict(a, p, "mixed")
-    E = api.local_energy(params, (a.n_up, a.n_dn), r, mol.R, mol.Z).cpu().numpy().astype(np.float64)
-    err = np.abs(E - E_ref)
-    # BF16 GEMMs: per-walker error bounded by 2 % of |E_L| + 50 mHa
-    assert np.all(err <= 0.02 * np.abs(E_ref) + 0.05), (E, E_ref)
+@pytest.mark.parametrize("prec,tol", [("mixed", 1e-4), ("bf16", 2e-2)])
+def test_local_energy_tensor_core_forms(cuda, le_cases, name, prec, tol):
+    mol, a, p, r, E_ref, lp_ref, g_ref, S = le_cases[name]
+    params = api.Params.from_dict(a, p, prec)
+    E, lp, g = api.local_energy(params, (a.n_up, a.n_dn), r, mol.R, mol.Z, return_grad=True)
+    E = E.cpu().numpy().astype(np.float64)
+    assert np.all(np.abs(E - E_ref) <= tol * S), (E, E_ref, S)
+    if prec == "mixed":
+        np.testing.assert_allclose(lp.cpu().numpy(), lp_ref, rtol=1e-4, atol=1e-3)
+
+
+def test_walker_chunking_consistent(cuda):
+    """Odd walker counts and repeated calls give identical per-walker results."""
+    mol = A.h_chain(6)
+    a = A.arch_for(mol, 4)
+    p = P.init_params(a, 1)
+    r = A.init_walkers(mol, 37, seed=4)
+    for prec in ("fp32", "mixed"):
+        params = api.Params.from_dict(a, p, prec)
+        E1 = api.local_energy(params, (a.n_up, a.n_dn), r, mol.R, mol.Z).cpu()
+        E2 = api.local_energy(params, (a.n_up, a.n_dn), r[:5], mol.R, mol.Z).cpu()
+        E3 = api.local_energy(params, (a.n_up, a.n_dn), r, mol.R, mol.Z).cpu()
+        assert torch.equal(E1, E3)
+        torch.testing.assert_close(E1[:5], E2, rtol=1e-6, atol=1e-6)
 
 
 def test_potential_energy(cuda):

@@ -235,6 +235,9 @@ template <> struct MM<Split> {
     }
 };
 
+// Runs `stmt` between per-tag timer events (no-ops unless dw_timer_enable(1)).
+#define DW_TIMED(tag, stmt) do { timer_begin(tag, s); stmt; timer_end(tag, s, 0.0, 0.0); } while (0)
+
 // Element offset of row `row` in a logical-width-ld activation buffer of type Act.
 template <class Act> static inline int64_t act_off(int64_t row, int ld) { return row * ld * ActIO<Act>::kParts; }
 
@@ -259,8 +262,8 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         if (pt >= 2) w.lo = bf[1];
         return w;
     };
-    launch_features<Act>(r, R, d, Bc, p.X0, s);
-    launch_streams(r, R, P, L, d, Bc, p.WP, p.HE, s);
+    DW_TIMED("features", launch_features<Act>(r, R, d, Bc, p.X0, s));
+    DW_TIMED("streams", launch_streams(r, R, P, L, d, Bc, p.WP, p.HE, s));
     Act* xin = p.X0;
     int ldin = d.kw[0];
     int pc = tang ? 3 : 1, ec = tang ? 5 : 1;
@@ -268,19 +271,20 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         Act* xout = (l % 2 == 0) ? p.XA : p.XB;
         int hw = d.hw[l], mw = mean_width(d, l);
         // (a) spin means and their per-walker contribution (+ the layer bias on the value channel)
-        launch_spin_means<Act>(xin, ldin, hw, d, Bc, p.Mcat, mw, s);
+        DW_TIMED("spin_means", launch_spin_means<Act>(xin, ldin, hw, d, Bc, p.Mcat, mw, s));
         GemmEpi e1; e1.bias = P + L.h_el_b[l]; e1.Tp = d.Tp; e1.rows_per_walker = d.Tp;
-        DW_CHECK(MM<Act>::mm(p.Mcat, mw, wref(pre.mean[l], d.D, &pre.mean_bf[0][0], l), p.WB, d.D, Bc * d.Tp, d.D, mw,
-                             e1, s));
+        DW_TIMED("mean_gemm", DW_CHECK(MM<Act>::mm(p.Mcat, mw, wref(pre.mean[l], d.D, &pre.mean_bf[0][0], l), p.WB, d.D,
+                                                   Bc * d.Tp, d.D, mw, e1, s)));
         // (b) h_map = tanh(h_one W + b)
         GemmEpi e2; e2.bias = P + L.h_map_b[l]; e2.Tp = d.Tp; e2.rows_per_walker = d.n * d.Tp; e2.act = tang ? 0 : 1;
         float* hm_pre = tang ? p.Zb : p.HM;
-        DW_CHECK(MM<Act>::mm(xin, ldin, wref(P + L.h_map_w[l], d.E, &pre.map_bf[0][0], l), hm_pre, d.E, rows, d.E, hw,
-                             e2, s));
-        if (tang) launch_tanh_fl<float>(p.Zb, d.E, d.E, Bc * d.n, d, p.HM, d.E, s);
+        DW_TIMED("map_gemm", DW_CHECK(MM<Act>::mm(xin, ldin, wref(P + L.h_map_w[l], d.E, &pre.map_bf[0][0], l), hm_pre,
+                                                  d.E, rows, d.E, hw, e2, s)));
+        if (tang) DW_TIMED("tanh_fl", launch_tanh_fl<float>(p.Zb, d.E, d.E, Bc * d.n, d, p.HM, d.E, s));
         // (c) SchNet convolutions into the input columns [hw, hw + E + eiw)
         int64_t wp_plane = (int64_t)Bc * d.n * d.n * pc * 32, he_plane = (int64_t)Bc * d.n * d.N * ec * 32;
-        launch_conv<Act>(r, p.WP + l * wp_plane, p.HM, p.HE + l * he_plane, p.him + l * d.N * 32, d, l, Bc, xin, ldin, s);
+        DW_TIMED("conv", launch_conv<Act>(r, p.WP + l * wp_plane, p.HM, p.HE + l * he_plane, p.him + l * d.N * 32, d, l,
+                                          Bc, xin, ldin, s));
         // (d) h_el = tanh([h | conv_ee | conv_ei] W_main + per-walker mean term)
         GemmEpi e3; e3.rowbias = p.WB; e3.ldrb = d.D; e3.Tp = d.Tp; e3.rows_per_walker = d.n * d.Tp; e3.act = tang ? 0 : 1;
         WRef wm = wref(pre.main[l], d.D, &pre.main_bf[0][0], l);
@@ -293,9 +297,9 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
             timer_begin("layer_gemm", s);
             DW_CHECK(MM<Act>::mm(xin, ldin, wm, p.Zb, d.D, rows, d.D, d.kw[l], e3, s));
             timer_end("layer_gemm", s, flops, bytes);
-            launch_tanh_fl<Act>(p.Zb, d.D, d.D, Bc * d.n, d, xout, kXW, s);
+            DW_TIMED("tanh_fl", launch_tanh_fl<Act>(p.Zb, d.D, d.D, Bc * d.n, d, xout, kXW, s));
         } else {
-            DW_CHECK(MM<Act>::mm_act(xin, ldin, wm, xout, kXW, rows, d.D, d.kw[l], e3, s));
+            DW_TIMED("layer_gemm_value", DW_CHECK(MM<Act>::mm_act(xin, ldin, wm, xout, kXW, rows, d.D, d.kw[l], e3, s)));
         }
         xin = xout;
         ldin = kXW;
@@ -303,18 +307,21 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
     const Act* H = xin;   // final embedding, logical row width kXW
     // backflow (envelope_orbitals.py:46-75): up-electron rows x W_up, down-electron rows x W_dn
     const int64_t rpw = (int64_t)d.n * d.Tp, sC = (int64_t)d.n * d.Tp * d.KN;
+    timer_begin("backflow_gemm", s);
     DW_CHECK(MM<Act>::mm_bat(H, kXW, rpw, wref1(P + L.bf_up, d.KN, pre.bf_up), p.BF, d.KN, d.nu * d.Tp, d.KN, d.D, Bc,
                              sC, s));
     DW_CHECK(MM<Act>::mm_bat(H + act_off<Act>((int64_t)d.nu * d.Tp, kXW), kXW, rpw, wref1(P + L.bf_dn, d.KN, pre.bf_dn),
                              p.BF + (int64_t)d.nu * d.Tp * d.KN, d.KN, d.nd * d.Tp, d.KN, d.D, Bc, sC, s));
-    launch_envelope(r, R, P, L, d, Bc, p.BF, d.KN, p.MO, s);
-    if (precision == DW_PRECISION_FP32) launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s);
-    else launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s);
-    if (tang) launch_det_tangents(p.MO, p.Ainv, p.sign, d, Bc, p.g, p.lapdet, s);
+    timer_end("backflow_gemm", s, 0.0, 0.0);
+    DW_TIMED("envelope", launch_envelope(r, R, P, L, d, Bc, p.BF, d.KN, p.MO, s));
+    if (precision == DW_PRECISION_FP32) DW_TIMED("slogdet", launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
+    else DW_TIMED("slogdet", launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
+    if (tang) DW_TIMED("det_tangents", launch_det_tangents(p.MO, p.Ainv, p.sign, d, Bc, p.g, p.lapdet, s));
     // Jastrow MLP([64, 64, 1]) on the final embedding
     GemmEpi j0; j0.bias = P + L.jas_b[0]; j0.Tp = d.Tp; j0.rows_per_walker = d.n * d.Tp; j0.act = tang ? 0 : 1;
     GemmEpi j1 = j0; j1.bias = P + L.jas_b[1];
     WRef wj0 = wref1(P + L.jas_w[0], d.J0, pre.jas0), wj1 = wref1(P + L.jas_w[1], d.J1, pre.jas1);
+    timer_begin("jastrow", s);
     if (tang) {
         DW_CHECK(MM<Act>::mm(H, kXW, wj0, p.Zb, d.J0, rows, d.J0, d.D, j0, s));
         launch_tanh_fl<Act>(p.Zb, d.J0, d.J0, Bc * d.n, d, p.J1, d.J0, s);
@@ -325,7 +332,8 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         DW_CHECK(MM<Act>::mm_act(p.J1, d.J0, wj1, p.J2, d.J1, rows, d.J1, d.J0, j1, s));
     }
     launch_jastrow_out<Act>(p.J2, d.J1, P + L.jas_w[2], d, Bc, p.jas, s);
-    launch_combine(p.logdet, p.sign, p.g, p.lapdet, p.jas, r, R, Z, d, Bc, lp, phase, E_loc, grad, s);
+    timer_end("jastrow", s, 0.0, 0.0);
+    DW_TIMED("combine", launch_combine(p.logdet, p.sign, p.g, p.lapdet, p.jas, r, R, Z, d, Bc, lp, phase, E_loc, grad, s));
     DW_CHECK_CUDA(cudaGetLastError());
     return DW_OK;
 }
@@ -483,12 +491,12 @@ int dw_mcmc_steps(const DwArch* a, int precision, const float* params, const voi
         m.interval = cfg->stepsize_update_interval; m.target = cfg->target_acceptance_rate;
         m.min_step = cfg->min_stepsize; m.max_step = cfg->max_stepsize; m.seed = cfg->seed;
         reset_launch_count();
-        launch_mh(m, 0, s);
+        DW_TIMED("mh", launch_mh(m, 0, s));
         launches += launch_count();
         for (int k = 0; k < cfg->n_steps; ++k) {
             reset_launch_count();
             DW_CHECK(fwd_call(r_prop, lp_prop));
-            launch_mh(m, k + 1 < cfg->n_steps ? 1 : 2, s);
+            DW_TIMED("mh", launch_mh(m, k + 1 < cfg->n_steps ? 1 : 2, s));
             launches += launch_count();
         }
         reset_launch_count();

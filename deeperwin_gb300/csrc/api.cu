@@ -22,8 +22,9 @@ struct WRef {
 };
 struct Prepared {
     float* main[4]; float* mean[4];
+    float* bf_cat;                                   // [D, 2 KN] = [W_up | W_dn]
     __nv_bfloat16* main_bf[2][4]; __nv_bfloat16* mean_bf[2][4]; __nv_bfloat16* map_bf[2][4];
-    __nv_bfloat16* bf_up[2]; __nv_bfloat16* bf_dn[2]; __nv_bfloat16* jas0[2]; __nv_bfloat16* jas1[2];
+    __nv_bfloat16* bf_bf[2]; __nv_bfloat16* jas0[2]; __nv_bfloat16* jas1[2];
     size_t bytes;
 };
 static inline int tc_parts(int precision) {
@@ -40,14 +41,14 @@ static Prepared carve_prepared(const DwArch* a, int precision, void* base) {
         p.main[l] = c.take<float>((size_t)d.kw[l] * d.D);
         p.mean[l] = c.take<float>((size_t)mean_width(d, l) * d.D);
     }
+    p.bf_cat = c.take<float>((size_t)d.D * 2 * d.KN);
     for (int part = 0; part < tc_parts(precision); ++part) {
         for (int l = 0; l < 4; ++l) {
             p.main_bf[part][l] = c.take<__nv_bfloat16>((size_t)d.kw[l] * d.D);
             p.mean_bf[part][l] = c.take<__nv_bfloat16>((size_t)mean_width(d, l) * d.D);
             p.map_bf[part][l] = c.take<__nv_bfloat16>((size_t)round_up(d.hw[l], 64) * d.E);
         }
-        p.bf_up[part] = c.take<__nv_bfloat16>((size_t)d.D * round_up(d.KN, 16));
-        p.bf_dn[part] = c.take<__nv_bfloat16>((size_t)d.D * round_up(d.KN, 16));
+        p.bf_bf[part] = c.take<__nv_bfloat16>((size_t)d.D * round_up(2 * d.KN, 16));
         p.jas0[part] = c.take<__nv_bfloat16>((size_t)d.D * d.J0);
         p.jas1[part] = c.take<__nv_bfloat16>((size_t)d.J0 * d.J1);
     }
@@ -95,6 +96,11 @@ static int prepare(const DwArch* a, int precision, const float* P, void* prep, s
             count_launch();
         }
     }
+    for (int half = 0; half < 2; ++half) {
+        DW_CHECK_CUDA(cudaMemcpy2DAsync(p.bf_cat + half * d.KN, sizeof(float) * 2 * d.KN,
+                                        P + (half == 0 ? L.bf_up : L.bf_dn), sizeof(float) * d.KN,
+                                        sizeof(float) * d.KN, d.D, cudaMemcpyDeviceToDevice, s));
+    }
     for (int part = 0; part < tc_parts(precision); ++part) {
         auto tr = [&](const float* src, int rows_src, int rows_pad, int cols, int cols_pad, __nv_bfloat16* dst) {
             int64_t n = (int64_t)rows_pad * cols_pad;
@@ -106,8 +112,7 @@ static int prepare(const DwArch* a, int precision, const float* P, void* prep, s
             tr(p.mean[l], mean_width(d, l), mean_width(d, l), d.D, d.D, p.mean_bf[part][l]);
             tr(P + L.h_map_w[l], d.hw[l], round_up(d.hw[l], 64), d.E, d.E, p.map_bf[part][l]);
         }
-        tr(P + L.bf_up, d.D, d.D, d.KN, round_up(d.KN, 16), p.bf_up[part]);
-        tr(P + L.bf_dn, d.D, d.D, d.KN, round_up(d.KN, 16), p.bf_dn[part]);
+        tr(p.bf_cat, d.D, d.D, 2 * d.KN, round_up(2 * d.KN, 16), p.bf_bf[part]);
         tr(P + L.jas_w[0], d.D, d.D, d.J0, d.J0, p.jas0[part]);
         tr(P + L.jas_w[1], d.J0, d.J0, d.J1, d.J1, p.jas1[part]);
     }
@@ -151,11 +156,11 @@ static Plan<Act> carve_plan(const Dims& d, int Bc, void* ws) {
     p.Mcat = c.take<Act>(np * Bc * d.Tp * mw);
     p.WB = c.take<float>((int64_t)Bc * d.Tp * d.D);
     p.HM = c.take<float>(rows * d.E);
-    p.Zb = c.take<float>(rows * std::max(d.D, d.J0));
+    p.Zb = std::is_same<Act, float>::value ? c.take<float>(rows * std::max(d.D, d.J0)) : nullptr;
     int pc = d.Tp > 1 ? 3 : 1, ec = d.Tp > 1 ? 5 : 1;
     p.WP = c.take<float>((int64_t)4 * Bc * d.n * d.n * pc * 32);
     p.HE = c.take<float>((int64_t)4 * Bc * d.n * d.N * ec * 32);
-    p.BF = c.take<float>(rows * d.KN);
+    p.BF = c.take<float>(rows * 2 * d.KN);
     p.MO = c.take<float>((int64_t)Bc * d.K * d.T * d.n * d.n);
     p.logdet = c.take<double>((int64_t)Bc * d.K);
     p.sign = c.take<double>((int64_t)Bc * d.K);
@@ -194,46 +199,36 @@ template <> struct MM<float> {
         gemm_f32(A, lda, W.f32, W.ldw, C, ldc, M, N, K, e, 1, 0, 0, s);
         return DW_OK;
     }
-    static int mm_act(const float* A, int lda, const WRef& W, float* C, int ldc, int M, int N, int K, const GemmEpi& e,
-                      cudaStream_t s) {
-        gemm_f32(A, lda, W.f32, W.ldw, C, ldc, M, N, K, e, 1, 0, 0, s);
-        return DW_OK;
-    }
-    static int mm_bat(const float* A, int lda, int64_t rows_per_batch, const WRef& W, float* C, int ldc, int M, int N,
-                      int K, int batch, int64_t sC, cudaStream_t s) {
-        GemmEpi e;
-        gemm_f32(A, lda, W.f32, W.ldw, C, ldc, M, N, K, e, batch, rows_per_batch * lda, sC, s);
+    template <class Out>
+    static int mm_fl(const float* A, int lda, const WRef& W, Out* C, int ldc, int M, int N, int K, const GemmEpi& e,
+                     const Dims& d, float* Zb, cudaStream_t s) {
+        gemm_f32(A, lda, W.f32, W.ldw, Zb, N, M, N, K, e, 1, 0, 0, s);
+        launch_tanh_fl<Out>(Zb, N, N, M / d.Tp, d, C, ldc, s);
         return DW_OK;
     }
 };
-template <> struct MM<__nv_bfloat16> {
-    static int mm(const __nv_bfloat16* A, int lda, const WRef& W, float* C, int ldc, int M, int N, int K,
-                  const GemmEpi& e, cudaStream_t s) {
-        return gemm_bf16_tc(A, lda, W.hi, C, ldc, M, N, K, e, s);
-    }
-    static int mm_act(const __nv_bfloat16* A, int lda, const WRef& W, __nv_bfloat16* C, int ldc, int M, int N, int K,
-                      const GemmEpi& e, cudaStream_t s) {
-        return gemm_bf16_tc_act(A, lda, W.hi, C, ldc, M, N, K, e, s);
-    }
-    static int mm_bat(const __nv_bfloat16* A, int lda, int64_t rows_per_batch, const WRef& W, float* C, int ldc, int M,
-                      int N, int K, int batch, int64_t sC, cudaStream_t s) {
-        return gemm_bf16_tc_batched(A, lda, W.hi, C, ldc, M, N, K, batch, rows_per_batch * lda, sC, s);
-    }
-};
-template <> struct MM<Split> {
-    static int mm(const Split* A, int lda, const WRef& W, float* C, int ldc, int M, int N, int K, const GemmEpi& e,
+template <class Act> struct MMTC {
+    static constexpr int np = ActIO<Act>::kParts;
+    static constexpr int out_act = np == 2 ? 2 : 1;
+    static int mm(const Act* A, int lda, const WRef& W, float* C, int ldc, int M, int N, int K, const GemmEpi& e,
                   cudaStream_t s) {
-        return gemm_split_tc(A, lda, W.hi, W.lo, C, ldc, M, N, K, e, s);
+        return gemm_tc(np, 0, A, lda, W.hi, W.lo, C, ldc, M, N, K, e, 0, 0, s);
     }
-    static int mm_act(const Split* A, int lda, const WRef& W, Split* C, int ldc, int M, int N, int K, const GemmEpi& e,
-                      cudaStream_t s) {
-        return gemm_split_tc_act(A, lda, W.hi, W.lo, C, ldc, M, N, K, e, s);
+    static int mm(const Act* A, int lda, const WRef& W, Act* C, int ldc, int M, int N, int K, const GemmEpi& e,
+                  cudaStream_t s) {
+        return gemm_tc(np, out_act, A, lda, W.hi, W.lo, C, ldc, M, N, K, e, 0, 0, s);
     }
-    static int mm_bat(const Split* A, int lda, int64_t rows_per_batch, const WRef& W, float* C, int ldc, int M, int N,
-                      int K, int batch, int64_t sC, cudaStream_t s) {
-        return gemm_split_tc_batched(A, lda, W.hi, W.lo, C, ldc, M, N, K, batch, rows_per_batch, sC, s);
+    static int mm_fl(const Act* A, int lda, const WRef& W, float* C, int ldc, int M, int N, int K, const GemmEpi& e,
+                     const Dims& d, float*, cudaStream_t s) {
+        return gemm_tc(np, 0, A, lda, W.hi, W.lo, C, ldc, M, N, K, e, 1, 3 * d.n, s);
+    }
+    static int mm_fl(const Act* A, int lda, const WRef& W, Act* C, int ldc, int M, int N, int K, const GemmEpi& e,
+                     const Dims& d, float*, cudaStream_t s) {
+        return gemm_tc(np, out_act, A, lda, W.hi, W.lo, C, ldc, M, N, K, e, 1, 3 * d.n, s);
     }
 };
+template <> struct MM<__nv_bfloat16> : MMTC<__nv_bfloat16> {};
+template <> struct MM<Split> : MMTC<Split> {};
 
 // Runs `stmt` between per-tag timer events (no-ops unless dw_timer_enable(1)).
 #define DW_TIMED(tag, stmt) do { timer_begin(tag, s); stmt; timer_end(tag, s, 0.0, 0.0); } while (0)
@@ -277,10 +272,9 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
                                                    Bc * d.Tp, d.D, mw, e1, s)));
         // (b) h_map = tanh(h_one W + b)
         GemmEpi e2; e2.bias = P + L.h_map_b[l]; e2.Tp = d.Tp; e2.rows_per_walker = d.n * d.Tp; e2.act = tang ? 0 : 1;
-        float* hm_pre = tang ? p.Zb : p.HM;
-        DW_TIMED("map_gemm", DW_CHECK(MM<Act>::mm(xin, ldin, wref(P + L.h_map_w[l], d.E, &pre.map_bf[0][0], l), hm_pre,
-                                                  d.E, rows, d.E, hw, e2, s)));
-        if (tang) DW_TIMED("tanh_fl", launch_tanh_fl<float>(p.Zb, d.E, d.E, Bc * d.n, d, p.HM, d.E, s));
+        WRef wmap = wref(P + L.h_map_w[l], d.E, &pre.map_bf[0][0], l);
+        if (tang) DW_TIMED("map_gemm", DW_CHECK(MM<Act>::mm_fl(xin, ldin, wmap, p.HM, d.E, rows, d.E, hw, e2, d, p.Zb, s)));
+        else DW_TIMED("map_gemm", DW_CHECK(MM<Act>::mm(xin, ldin, wmap, p.HM, d.E, rows, d.E, hw, e2, s)));
         // (c) SchNet convolutions into the input columns [hw, hw + E + eiw)
         int64_t wp_plane = (int64_t)Bc * d.n * d.n * pc * 32, he_plane = (int64_t)Bc * d.n * d.N * ec * 32;
         DW_TIMED("conv", launch_conv<Act>(r, p.WP + l * wp_plane, p.HM, p.HE + l * he_plane, p.him + l * d.N * 32, d, l,
@@ -292,28 +286,28 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
             // algorithmic work of this launch: 2 M N K with the unpadded K, A and C streamed once
             const double kreal = hw + d.E + d.eiw[l];
             const double flops = 2.0 * rows * d.D * kreal;
-            const double bytes = (double)rows * (kreal * sizeof(Act) * ActIO<Act>::kParts + d.D * 4.0) +
-                                 kreal * d.D * sizeof(Act) * ActIO<Act>::kParts;
+            const double esz = (double)sizeof(Act) * ActIO<Act>::kParts;
+            const double bytes = (double)rows * (kreal + d.D) * esz + kreal * d.D * esz;
             timer_begin("layer_gemm", s);
-            DW_CHECK(MM<Act>::mm(xin, ldin, wm, p.Zb, d.D, rows, d.D, d.kw[l], e3, s));
+            DW_CHECK(MM<Act>::mm_fl(xin, ldin, wm, xout, kXW, rows, d.D, d.kw[l], e3, d, p.Zb, s));
             timer_end("layer_gemm", s, flops, bytes);
-            DW_TIMED("tanh_fl", launch_tanh_fl<Act>(p.Zb, d.D, d.D, Bc * d.n, d, xout, kXW, s));
         } else {
-            DW_TIMED("layer_gemm_value", DW_CHECK(MM<Act>::mm_act(xin, ldin, wm, xout, kXW, rows, d.D, d.kw[l], e3, s)));
+            DW_TIMED("layer_gemm_value", DW_CHECK(MM<Act>::mm(xin, ldin, wm, xout, kXW, rows, d.D, d.kw[l], e3, s)));
         }
         xin = xout;
         ldin = kXW;
     }
     const Act* H = xin;   // final embedding, logical row width kXW
-    // backflow (envelope_orbitals.py:46-75): up-electron rows x W_up, down-electron rows x W_dn
-    const int64_t rpw = (int64_t)d.n * d.Tp, sC = (int64_t)d.n * d.Tp * d.KN;
-    timer_begin("backflow_gemm", s);
-    DW_CHECK(MM<Act>::mm_bat(H, kXW, rpw, wref1(P + L.bf_up, d.KN, pre.bf_up), p.BF, d.KN, d.nu * d.Tp, d.KN, d.D, Bc,
-                             sC, s));
-    DW_CHECK(MM<Act>::mm_bat(H + act_off<Act>((int64_t)d.nu * d.Tp, kXW), kXW, rpw, wref1(P + L.bf_dn, d.KN, pre.bf_dn),
-                             p.BF + (int64_t)d.nu * d.Tp * d.KN, d.KN, d.nd * d.Tp, d.KN, d.D, Bc, sC, s));
-    timer_end("backflow_gemm", s, 0.0, 0.0);
-    DW_TIMED("envelope", launch_envelope(r, R, P, L, d, Bc, p.BF, d.KN, p.MO, s));
+    // backflow (envelope_orbitals.py:46-75): every row times [W_up | W_dn]; the envelope kernel
+    // takes the half that matches the electron's spin
+    {
+        GemmEpi e0; e0.Tp = d.Tp; e0.rows_per_walker = d.n * d.Tp;
+        WRef wb; wb.f32 = pre.bf_cat; wb.ldw = 2 * d.KN;
+        if (pt >= 1) wb.hi = pre.bf_bf[0];
+        if (pt >= 2) wb.lo = pre.bf_bf[1];
+        DW_TIMED("backflow_gemm", DW_CHECK(MM<Act>::mm(H, kXW, wb, p.BF, 2 * d.KN, rows, 2 * d.KN, d.D, e0, s)));
+    }
+    DW_TIMED("envelope", launch_envelope(r, R, P, L, d, Bc, p.BF, 2 * d.KN, p.MO, s));
     if (precision == DW_PRECISION_FP32) DW_TIMED("slogdet", launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
     else DW_TIMED("slogdet", launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
     if (tang) DW_TIMED("det_tangents", launch_det_tangents(p.MO, p.Ainv, p.sign, d, Bc, p.g, p.lapdet, s));
@@ -323,13 +317,11 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
     WRef wj0 = wref1(P + L.jas_w[0], d.J0, pre.jas0), wj1 = wref1(P + L.jas_w[1], d.J1, pre.jas1);
     timer_begin("jastrow", s);
     if (tang) {
-        DW_CHECK(MM<Act>::mm(H, kXW, wj0, p.Zb, d.J0, rows, d.J0, d.D, j0, s));
-        launch_tanh_fl<Act>(p.Zb, d.J0, d.J0, Bc * d.n, d, p.J1, d.J0, s);
-        DW_CHECK(MM<Act>::mm(p.J1, d.J0, wj1, p.Zb, d.J1, rows, d.J1, d.J0, j1, s));
-        launch_tanh_fl<Act>(p.Zb, d.J1, d.J1, Bc * d.n, d, p.J2, d.J1, s);
+        DW_CHECK(MM<Act>::mm_fl(H, kXW, wj0, p.J1, d.J0, rows, d.J0, d.D, j0, d, p.Zb, s));
+        DW_CHECK(MM<Act>::mm_fl(p.J1, d.J0, wj1, p.J2, d.J1, rows, d.J1, d.J0, j1, d, p.Zb, s));
     } else {
-        DW_CHECK(MM<Act>::mm_act(H, kXW, wj0, p.J1, d.J0, rows, d.J0, d.D, j0, s));
-        DW_CHECK(MM<Act>::mm_act(p.J1, d.J0, wj1, p.J2, d.J1, rows, d.J1, d.J0, j1, s));
+        DW_CHECK(MM<Act>::mm(H, kXW, wj0, p.J1, d.J0, rows, d.J0, d.D, j0, s));
+        DW_CHECK(MM<Act>::mm(p.J1, d.J0, wj1, p.J2, d.J1, rows, d.J1, d.J0, j1, s));
     }
     launch_jastrow_out<Act>(p.J2, d.J1, P + L.jas_w[2], d, Bc, p.jas, s);
     timer_end("jastrow", s, 0.0, 0.0);
@@ -379,6 +371,8 @@ static int forward_all(const DwArch* a, int precision, const float* P, const voi
                        const float* R, const int32_t* Z, float* lp, float* phase, float* E, float* grad, bool tang,
                        void* ws, size_t ws_bytes, cudaStream_t s) {
     Dims d = make_dims(a, tang);
+    // the fused forward-Laplacian epilogue keeps one electron's channels inside a 128-row tile
+    if (tang && !std::is_same<Act, float>::value && d.Tp > 128) return DW_ERR_ARCH;
     ParamLayout L;
     make_layout(a, &L);
     Prepared pre = carve_prepared(a, precision, const_cast<void*>(prepared));

@@ -1,11 +1,20 @@
-// tcgen05 tensor-core GEMM for sm_103a: TMA (128-byte swizzle) loads A and B tiles into a
-// multi-stage shared-memory ring, one elected thread issues tcgen05.mma (kind::f16, BF16 in,
-// FP32 accumulate in TMEM), and four warps drain TMEM with tcgen05.ld into the fused
-// epilogue (value-channel bias, per-walker-channel bias, tanh).
+// Persistent tcgen05 tensor-core GEMM for sm_103a.
 //
-// Warp roles: warp 0 lane 0 = TMA producer, warp 1 lane 0 = MMA issuer, warps 0-3 = epilogue.
+//   C[M, N] = epilogue( A[M, K] @ W[N, K]^T )
+//
+// * A and W are BF16 (NP = 1) or split-BF16 (NP = 2: x = hi + lo, three MMAs per K step:
+//   A_hi W_hi + A_hi W_lo + A_lo W_hi, all accumulated in FP32 in TMEM).
+// * Warp roles (192 threads): warp 0 = TMA producer, warp 1 = MMA issuer (one elected lane),
+//   warps 2-5 = epilogue (warp w drains TMEM lanes 32 (w % 4) .. +31).
+// * Shared-memory ring of S stages (128-byte swizzled K-major tiles), two TMEM accumulators
+//   so the epilogue of tile i overlaps the main loop of tile i + 1, one CTA per SM looping
+//   over output tiles.
+// * Epilogue: value-channel bias, per-(walker, channel) row bias, and either tanh on value
+//   rows or the forward-Laplacian tanh across the Tp channel rows of each electron
+//   (y = tanh z; y_t = (1 - y^2) z_t; y_lap = (1 - y^2) z_lap - 2 y (1 - y^2) sum_t z_t^2).
+//   Results are written to swizzled shared-memory staging tiles and stored with TMA.
 // Every mbarrier wait is bounded; on timeout the kernel records an error flag, stops
-// issuing, drains, frees its TMEM and returns.
+// issuing, waits (bounded) for its TMA loads in flight, frees its TMEM and returns.
 #include "gemm_tc.cuh"
 #include <cuda.h>
 #include <stdlib.h>
@@ -19,6 +28,7 @@ __device__ int g_tc_error = 0;
 namespace {
 
 constexpr int BM = 128, BK = 64;
+constexpr int kThreads = 192;
 constexpr uint32_t kSpinLimit = 1u << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -29,7 +39,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
-// Bounded parity wait: returns false after kSpinLimit unsuccessful probes.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Bounded parity wait: true once the phase with the given parity has completed.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     uint32_t addr = smem_u32(bar);
     for (uint32_t it = 0; it < kSpinLimit; ++it) {
@@ -46,6 +59,16 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
         ::"r"(smem_u32(dst)), "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1) : "memory");
 }
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void* src, int c0, int c1) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%2, %3}], [%1];"
+                 ::"l"(map), "r"(smem_u32(src)), "r"(c0), "r"(c1) : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
 // UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart.
 __device__ __forceinline__ uint64_t smem_desc_sw128(const void* p) {
     uint64_t addr = smem_u32(p);
@@ -66,59 +89,64 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     uint32_t r[16];
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     #pragma unroll
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// 16-byte chunk j of row r in a 128-byte-swizzled staging tile (1024-byte aligned).
+__device__ __forceinline__ uint32_t swz(int r, int j) { return (uint32_t)(r * 128 + ((j ^ (r & 7)) << 4)); }
 
 struct TcArgs {
-    void* C; int ldc; int M; int N; int K; int BN;
-    int64_t a_rows_per_batch;   // row offset of batch z in the A tensor map
-    int64_t sC;                 // element offset of batch z in C
+    int M, N, K, BN;
     GemmEpi epi;
+    int fl;             // forward-Laplacian epilogue (rows grouped by Tp channels)
+    int n3;             // 3 n_el: channels 1..n3 are gradients, n3 + 1 the Laplacian
     int stages;
     uint32_t tmem_cols;
+    int n_tiles_n, n_tiles;
 };
 
-// NP = 1: plain BF16 operands, one MMA per 16-wide K step.
-// NP = 2: split-BF16 operands A = A_hi + A_lo, W = W_hi + W_lo; three MMAs per K step
-//         (A_hi W_hi + A_hi W_lo + A_lo W_hi) into the same FP32 TMEM accumulator.
-// OUT = 0: fp32 C; 1: bf16 C; 2: split-BF16 C ([hi | lo] rows of logical width ldc).
+// OUT: 0 = fp32 C, 1 = bf16 C, 2 = split-BF16 C.
 template <int NP, int OUT>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kThreads, 1)
 k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
-          const __grid_constant__ CUtensorMap tmB0, const __grid_constant__ CUtensorMap tmB1, TcArgs a) {
+          const __grid_constant__ CUtensorMap tmB0, const __grid_constant__ CUtensorMap tmB1,
+          const __grid_constant__ CUtensorMap tmC0, const __grid_constant__ CUtensorMap tmC1, TcArgs a) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    constexpr int CW = OUT == 0 ? 32 : 64;             // columns per staged store box (128 bytes per row)
+    constexpr int NPO = OUT == 2 ? 2 : 1;              // output parts
     const int S = a.stages, BN = a.BN;
     const uint32_t a_bytes = BM * BK * 2, b_bytes = (uint32_t)BN * BK * 2;
     const uint32_t stage_bytes = NP * (a_bytes + b_bytes);
-    // stage s: [A_0 | A_1 | B_0 | B_1]
     auto sA = [&](int s, int part) { return smem + (size_t)s * stage_bytes + (size_t)part * a_bytes; };
     auto sB = [&](int s, int part) { return smem + (size_t)s * stage_bytes + (size_t)NP * a_bytes + (size_t)part * b_bytes; };
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)S * stage_bytes);
+    uint8_t* stage_out = smem + (size_t)S * stage_bytes;                   // [4 warps][NPO][4096]
+    float* xchg = reinterpret_cast<float*>(stage_out + 4 * NPO * 4096);    // [2 bufs][2 arrays][4][64]
+    uint64_t* full = reinterpret_cast<uint64_t*>(xchg + 2 * 2 * 4 * 64);
     uint64_t* empty = full + S;
-    uint64_t* done = empty + S;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    uint64_t* tfull = empty + S;     // [2]
+    uint64_t* tempty = tfull + 2;    // [2]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
     __shared__ int s_err;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN, z = blockIdx.z;
     const int nk = (a.K + BK - 1) / BK;
 
     if (threadIdx.x == 0) {
         s_err = 0;
         for (int s = 0; s < S; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-        mbar_init(done, 1);
+        for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 4); }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        fence_async_smem();
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -130,85 +158,185 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 0 && lane == 0) {
-        // TMA producer
-        const int row_a = (int)(z * a.a_rows_per_batch) + m0;
-        for (int kt = 0; kt < nk; ++kt) {
-            int s = kt % S;
-            if (kt >= S && !mbar_wait(&empty[s], ((kt / S) - 1) & 1)) { atomicExch(&s_err, 1); break; }
-            mbar_expect_tx(&full[s], stage_bytes);
-            tma_load_2d(sA(s, 0), &tmA0, &full[s], kt * BK, row_a);
-            tma_load_2d(sB(s, 0), &tmB0, &full[s], kt * BK, n0);
-            if (NP == 2) {
-                tma_load_2d(sA(s, 1), &tmA1, &full[s], kt * BK, row_a);
-                tma_load_2d(sB(s, 1), &tmB1, &full[s], kt * BK, n0);
-            }
-        }
-    } else if (warp == 1 && lane == 0) {
-        // MMA issuer
-        const uint32_t idesc = idesc_bf16(BN);
-        for (int kt = 0; kt < nk; ++kt) {
-            int s = kt % S;
-            if (!mbar_wait(&full[s], (kt / S) & 1)) { atomicExch(&s_err, 1); break; }
-            tc_fence_after();
-            uint64_t a0 = smem_desc_sw128(sA(s, 0)), b0 = smem_desc_sw128(sB(s, 0));
-            uint64_t a1 = smem_desc_sw128(sA(s, NP - 1)), b1 = smem_desc_sw128(sB(s, NP - 1));
-            #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk) {
-                const uint64_t o = (uint64_t)(kk * 2);
-                umma_bf16(tmem, a0 + o, b0 + o, idesc, (kt | kk) ? 1u : 0u);
-                if (NP == 2) {
-                    umma_bf16(tmem, a0 + o, b1 + o, idesc, 1u);
-                    umma_bf16(tmem, a1 + o, b0 + o, idesc, 1u);
+    if (warp == 0) {
+        // ---------------- TMA producer
+        if (lane == 0) {
+            uint32_t cnt = 0;
+            uint32_t issued[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            bool err = false;
+            for (int tile = blockIdx.x; tile < a.n_tiles && !err; tile += gridDim.x) {
+                const int m0 = (tile / a.n_tiles_n) * BM, n0 = (tile % a.n_tiles_n) * BN;
+                for (int kt = 0; kt < nk; ++kt, ++cnt) {
+                    const int s = cnt % S;
+                    const uint32_t use = cnt / S;
+                    if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1)) { err = true; break; }
+                    mbar_expect_tx(&full[s], stage_bytes);
+                    tma_load_2d(sA(s, 0), &tmA0, &full[s], kt * BK, m0);
+                    tma_load_2d(sB(s, 0), &tmB0, &full[s], kt * BK, n0);
+                    if (NP == 2) {
+                        tma_load_2d(sA(s, 1), &tmA1, &full[s], kt * BK, m0);
+                        tma_load_2d(sB(s, 1), &tmB1, &full[s], kt * BK, n0);
+                    }
+                    issued[s] = use + 1;
                 }
             }
-            umma_commit(&empty[s]);
+            if (err) {
+                atomicExch(&s_err, 1);
+                for (int s = 0; s < S; ++s)          // drain loads still in flight
+                    if (issued[s]) mbar_wait(&full[s], (issued[s] - 1) & 1);
+            }
         }
-        umma_commit(done);
-    }
-    __syncwarp();
-    bool ok = mbar_wait(done, 0);
-    tc_fence_after();
-    if (!ok) atomicExch(&s_err, 1);
-
-    // Epilogue: warp w owns TMEM lanes (rows) 32w..32w+31.
-    const int m = m0 + warp * 32 + lane;
-    const GemmEpi& e = a.epi;
-    const int t = m % e.Tp;
-    const float* rb = (e.rowbias && m < a.M) ? e.rowbias + ((int64_t)(m / e.rows_per_walker) * e.Tp + t) * e.ldrb : nullptr;
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-        if (m < a.M && ok) {
-            #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                int n = n0 + c0 + j;
-                if (n < a.N) {
+    } else if (warp == 1) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(BN);
+            uint32_t cnt = 0, it = 0;
+            bool err = false;
+            for (int tile = blockIdx.x; tile < a.n_tiles && !err; tile += gridDim.x, ++it) {
+                const uint32_t acc = it & 1;
+                if (!mbar_wait(&tempty[acc], ((it >> 1) & 1) ^ 1)) { err = true; break; }
+                tc_fence_after();
+                const uint32_t d = tmem + acc * (uint32_t)BN;
+                for (int kt = 0; kt < nk; ++kt, ++cnt) {
+                    const int s = cnt % S;
+                    if (!mbar_wait(&full[s], (cnt / S) & 1)) { err = true; break; }
+                    tc_fence_after();
+                    const uint64_t a0 = smem_desc_sw128(sA(s, 0)), b0 = smem_desc_sw128(sB(s, 0));
+                    const uint64_t a1 = smem_desc_sw128(sA(s, NP - 1)), b1 = smem_desc_sw128(sB(s, NP - 1));
+                    #pragma unroll
+                    for (int kk = 0; kk < BK / 16; ++kk) {
+                        const uint64_t o = (uint64_t)(kk * 2);
+                        umma_bf16(d, a0 + o, b0 + o, idesc, (kt | kk) ? 1u : 0u);
+                        if (NP == 2) {
+                            umma_bf16(d, a0 + o, b1 + o, idesc, 1u);
+                            umma_bf16(d, a1 + o, b0 + o, idesc, 1u);
+                        }
+                    }
+                    umma_commit(&empty[s]);
+                }
+                umma_commit(&tfull[acc]);
+            }
+            if (err) atomicExch(&s_err, 1);
+        }
+    } else {
+        // ---------------- epilogue warps
+        const int q = warp & 3;                      // TMEM lane quarter
+        const GemmEpi& e = a.epi;
+        const int Tp = e.Tp;
+        uint8_t* my_out = stage_out + (size_t)q * NPO * 4096;
+        uint32_t it = 0;
+        int xbuf = 0;
+        for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++it) {
+            const int m0 = (tile / a.n_tiles_n) * BM, n0 = (tile % a.n_tiles_n) * BN;
+            const uint32_t acc = it & 1;
+            if (!mbar_wait(&tfull[acc], (it >> 1) & 1)) { atomicExch(&s_err, 1); break; }
+            tc_fence_after();
+            const int row = q * 32 + lane;           // row within the tile
+            const int m = m0 + row;
+            const int t = m % Tp;
+            const float* rb = (e.rowbias && m < a.M) ? e.rowbias + ((int64_t)(m / e.rows_per_walker) * Tp + t) * e.ldrb
+                                                     : nullptr;
+            const bool is_val = t == 0, is_grad = t >= 1 && t <= a.n3, is_lap = a.fl && t == a.n3 + 1;
+            for (int c0 = 0; c0 < BN; c0 += CW) {
+                float v[CW];
+                const uint32_t base = tmem + acc * (uint32_t)BN + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+                #pragma unroll
+                for (int j = 0; j < CW; j += 16) tmem_ld16(base + j, v + j);
+                tmem_wait_ld();
+                #pragma unroll
+                for (int j = 0; j < CW; ++j) {
+                    const int n = n0 + c0 + j;
                     float x = v[j];
-                    if (e.bias && t == 0) x += e.bias[n];
-                    if (rb) x += rb[n];
-                    if (e.act == 1) x = tanhf(x);
-                    if (OUT == 0) {
-                        reinterpret_cast<float*>(a.C)[z * a.sC + (int64_t)m * a.ldc + n] = x;
-                    } else if (OUT == 1) {
-                        reinterpret_cast<__nv_bfloat16*>(a.C)[z * a.sC + (int64_t)m * a.ldc + n] = __float2bfloat16_rn(x);
+                    if (n < a.N) {
+                        if (e.bias && is_val) x += __ldg(e.bias + n);
+                        if (rb) x += __ldg(rb + n);
+                    }
+                    v[j] = x;
+                }
+                if (a.fl) {
+                    // forward-Laplacian tanh over the Tp channel rows of each electron
+                    if (Tp <= 32) {
+                        #pragma unroll
+                        for (int j = 0; j < CW; ++j) {
+                            float sq = is_grad ? v[j] * v[j] : 0.f;
+                            for (int o = 1; o < Tp; o <<= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+                            const float z0 = __shfl_sync(0xffffffffu, v[j], lane & ~(Tp - 1));
+                            const float y0 = tanhf(z0), d1 = 1.f - y0 * y0;
+                            v[j] = is_val ? y0 : (is_grad ? d1 * v[j] : (is_lap ? d1 * v[j] - 2.f * y0 * d1 * sq : 0.f));
+                        }
                     } else {
-                        ActIO<Split>::store(reinterpret_cast<Split*>(a.C) + z * a.sC, m, a.ldc, n, x);
+                        float* xs = xchg + (size_t)xbuf * 2 * 4 * 64;    // [2 arrays][4 quarters][64]
+                        #pragma unroll
+                        for (int j = 0; j < CW; ++j) {
+                            float sq = is_grad ? v[j] * v[j] : 0.f;
+                            #pragma unroll
+                            for (int o = 1; o < 32; o <<= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+                            const float z0 = __shfl_sync(0xffffffffu, v[j], 0);
+                            if (lane == 0) { xs[q * 64 + j] = sq; xs[4 * 64 + q * 64 + j] = z0; }
+                        }
+                        epi_bar();
+                        const int qs = Tp / 32, g0 = (q / qs) * qs;
+                        #pragma unroll
+                        for (int j = 0; j < CW; ++j) {
+                            float sq = 0.f;
+                            for (int k = 0; k < qs; ++k) sq += xs[(g0 + k) * 64 + j];
+                            const float z0 = xs[4 * 64 + g0 * 64 + j];
+                            const float y0 = tanhf(z0), d1 = 1.f - y0 * y0;
+                            v[j] = is_val ? y0 : (is_grad ? d1 * v[j] : (is_lap ? d1 * v[j] - 2.f * y0 * d1 * sq : 0.f));
+                        }
+                        xbuf ^= 1;   // the other exchange buffer is written only after the next barrier
+                    }
+                } else if (e.act == 1) {
+                    #pragma unroll
+                    for (int j = 0; j < CW; ++j) v[j] = tanhf(v[j]);
+                }
+                // stage the 32 x CW sub-tile (128-byte swizzle) and store it with TMA
+                if (lane == 0) bulk_wait_read0();
+                __syncwarp();
+                if (OUT == 0) {
+                    #pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        *reinterpret_cast<float4*>(my_out + swz(lane, j)) =
+                            make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                } else {
+                    #pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        uint32_t hw_[4], lw_[4];
+                        #pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            float x0 = v[8 * j + 2 * k], x1 = v[8 * j + 2 * k + 1];
+                            __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
+                            hw_[k] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                            if (OUT == 2) {
+                                __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
+                                __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
+                                lw_[k] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                            } else {
+                                lw_[k] = 0u;
+                            }
+                        }
+                        *reinterpret_cast<uint4*>(my_out + swz(lane, j)) = make_uint4(hw_[0], hw_[1], hw_[2], hw_[3]);
+                        if (OUT == 2)
+                            *reinterpret_cast<uint4*>(my_out + 4096 + swz(lane, j)) = make_uint4(lw_[0], lw_[1], lw_[2], lw_[3]);
                     }
                 }
+                fence_async_smem();
+                __syncwarp();
+                if (lane == 0) {
+                    tma_store_2d(&tmC0, my_out, n0 + c0, m0 + q * 32);
+                    if (OUT == 2) tma_store_2d(&tmC1, my_out + 4096, n0 + c0, m0 + q * 32);
+                    bulk_commit();
+                }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[acc]);
         }
+        if (lane == 0) bulk_wait0();
     }
     tc_fence_before();
     __syncthreads();
-    if (s_err && threadIdx.x == 0) {
-        // drain: wait (bounded) for any TMA still in flight before the shared memory is released
-        for (int s = 0; s < S; ++s) {
-            int last = nk - 1 - ((nk - 1 - s) % S);
-            if (last >= s) mbar_wait(&full[s], (last / S) & 1);
-        }
-        atomicExch(&g_tc_error, 1);
-    }
+    if (s_err && threadIdx.x == 0) atomicExch(&g_tc_error, 1);
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
     }
@@ -233,54 +361,82 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 2-D bf16 tensor map: dims {cols (inner), rows}, row stride ld elements, box {64, box_rows}.
-int make_map(CUtensorMap* map, const void* base, int64_t rows, int cols, int ld, int box_rows) {
+// 2-D tensor map: dims {cols (inner), rows}, row stride ld elements, box {box_cols, box_rows},
+// 128-byte swizzle (box_cols * element size must be 128 bytes).
+int make_map(CUtensorMap* map, const void* base, int64_t rows, int cols, int64_t ld, int box_cols, int box_rows,
+             bool f32) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return DW_ERR_UNSUPPORTED;
-    if (((uintptr_t)base & 15) || (ld * 2) % 16) return DW_ERR_ARG;
+    const int es = f32 ? 4 : 2;
+    if (((uintptr_t)base & 15) || (ld * es) % 16 || box_cols * es != 128) return DW_ERR_ARG;
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
-    cuuint32_t es[2] = {1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    cuuint64_t strides[1] = {(cuuint64_t)ld * es};
+    cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                    const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? DW_OK : DW_ERR_ARG;
 }
 
-// A: np parts of a logical [rows, lda] activation (np = 2: [hi | lo] rows of width 2 lda).
-// W0/W1: [N, round_up(K, 64)] K-major weight parts.
+int num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 148;
+    }
+    return n;
+}
+
+// A: NP parts of a logical [M, lda] activation (NP = 2: [hi | lo] rows of width 2 lda).
+// W0/W1: [N, round_up(K, 64)] K-major weight parts. C: logical [M, ldc].
 template <int NP, int OUT>
-int launch_tc(const __nv_bfloat16* A, int lda, int64_t a_rows_total, const __nv_bfloat16* W0, const __nv_bfloat16* W1,
-              void* C, int ldc, int M, int N, int K, const GemmEpi& epi, int batch, int64_t a_rows_per_batch, int64_t sC,
-              cudaStream_t s) {
+int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __nv_bfloat16* W1, void* C, int ldc,
+              int M, int N, int K, const GemmEpi& epi, int fl, int n3, cudaStream_t s) {
     if (M <= 0 || N <= 0 || K <= 0) return DW_OK;
-    const int bn_max = NP == 2 ? 128 : 256;
-    int ntiles = (N + bn_max - 1) / bn_max;
-    int BN = round_up((N + ntiles - 1) / ntiles, 16);
-    int Kp = round_up(K, 64);
-    CUtensorMap ma0, ma1, mb0, mb1;
-    const int phys_ld = NP * lda;
-    DW_CHECK(make_map(&ma0, A, a_rows_total, K, phys_ld, BM));
-    DW_CHECK(make_map(&mb0, W0, N, K, Kp, BN));
+    constexpr int CW = OUT == 0 ? 32 : 64;
+    int ntn = (N + 255) / 256;
+    int BN = round_up((N + ntn - 1) / ntn, CW);
+    if (BN > 256) { ntn += 1; BN = round_up((N + ntn - 1) / ntn, CW); }
+    const int Kp = round_up(K, 64);
+    CUtensorMap ma0, ma1, mb0, mb1, mc0, mc1;
+    DW_CHECK(make_map(&ma0, A, M, K, (int64_t)NP * lda, 64, BM, false));
+    DW_CHECK(make_map(&mb0, W0, N, K, Kp, 64, BN, false));
     if (NP == 2) {
-        DW_CHECK(make_map(&ma1, A + lda, a_rows_total, K, phys_ld, BM));
-        DW_CHECK(make_map(&mb1, W1, N, K, Kp, BN));
+        DW_CHECK(make_map(&ma1, A + lda, M, K, (int64_t)NP * lda, 64, BM, false));
+        DW_CHECK(make_map(&mb1, W1, N, K, Kp, 64, BN, false));
     } else {
         ma1 = ma0; mb1 = mb0;
     }
+    if (OUT == 0) {
+        DW_CHECK(make_map(&mc0, C, M, N, ldc, 32, 32, true));
+        mc1 = mc0;
+    } else if (OUT == 1) {
+        DW_CHECK(make_map(&mc0, C, M, N, ldc, 64, 32, false));
+        mc1 = mc0;
+    } else {
+        DW_CHECK(make_map(&mc0, C, M, N, (int64_t)2 * ldc, 64, 32, false));
+        DW_CHECK(make_map(&mc1, reinterpret_cast<const __nv_bfloat16*>(C) + ldc, M, N, (int64_t)2 * ldc, 64, 32, false));
+    }
     TcArgs a;
-    a.C = C; a.ldc = ldc; a.M = M; a.N = N; a.K = K; a.BN = BN;
-    a.a_rows_per_batch = a_rows_per_batch; a.sC = sC; a.epi = epi;
-    int stage_bytes = NP * (BM * BK * 2 + BN * BK * 2);
-    a.stages = std::min(4, (200 * 1024) / stage_bytes);
+    a.M = M; a.N = N; a.K = K; a.BN = BN; a.epi = epi; a.fl = fl; a.n3 = n3;
+    const int stage_bytes = NP * (BM * BK * 2 + BN * BK * 2);
+    const int npo = OUT == 2 ? 2 : 1;
+    const int fixed = 1024 + 4 * npo * 4096 + 2 * 2 * 4 * 64 * 4 + 256;
+    a.stages = std::min(8, (220 * 1024 - fixed) / stage_bytes);
+    if (a.stages < 2) return DW_ERR_ARCH;
     a.tmem_cols = 32;
-    while ((int)a.tmem_cols < BN) a.tmem_cols <<= 1;
-    size_t smem = 1024 + (size_t)a.stages * stage_bytes + (2 * a.stages + 1) * 8 + 16;
+    while ((int)a.tmem_cols < 2 * BN) a.tmem_cols <<= 1;
+    const int mt = (M + BM - 1) / BM;
+    a.n_tiles_n = ntn;
+    a.n_tiles = mt * ntn;
+    size_t smem = (size_t)fixed + (size_t)a.stages * stage_bytes;
     auto kern = k_gemm_tc<NP, OUT>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid(ntiles, (M + BM - 1) / BM, batch);
-    kern<<<grid, 128, smem, s>>>(ma0, ma1, mb0, mb1, a);
+    int grid = std::min(a.n_tiles, num_sms());
+    kern<<<grid, kThreads, smem, s>>>(ma0, ma1, mb0, mb1, mc0, mc1, a);
     count_launch();
     DW_CHECK_CUDA(cudaGetLastError());
     return DW_OK;
@@ -301,35 +457,14 @@ bool tc_available() {
     return cached == 1;
 }
 
-int gemm_bf16_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* Wt, float* C, int ldc, int M, int N, int K,
-                 const GemmEpi& epi, cudaStream_t s) {
-    return launch_tc<1, 0>(A, lda, M, Wt, nullptr, C, ldc, M, N, K, epi, 1, 0, 0, s);
-}
-int gemm_bf16_tc_act(const __nv_bfloat16* A, int lda, const __nv_bfloat16* Wt, __nv_bfloat16* C, int ldc, int M, int N,
-                     int K, const GemmEpi& epi, cudaStream_t s) {
-    return launch_tc<1, 1>(A, lda, M, Wt, nullptr, C, ldc, M, N, K, epi, 1, 0, 0, s);
-}
-int gemm_bf16_tc_batched(const __nv_bfloat16* A, int lda, const __nv_bfloat16* Wt, float* C, int ldc, int M, int N, int K,
-                         int batch, int64_t sA, int64_t sC, cudaStream_t s) {
-    GemmEpi e;
-    int64_t rows_per_batch = sA / lda;
-    int64_t rows_total = rows_per_batch * (batch - 1) + M;
-    return launch_tc<1, 0>(A, lda, rows_total, Wt, nullptr, C, ldc, M, N, K, e, batch, rows_per_batch, sC, s);
-}
-int gemm_split_tc(const Split* A, int lda, const __nv_bfloat16* Whi, const __nv_bfloat16* Wlo, float* C, int ldc, int M,
-                  int N, int K, const GemmEpi& epi, cudaStream_t s) {
-    return launch_tc<2, 0>(reinterpret_cast<const __nv_bfloat16*>(A), lda, M, Whi, Wlo, C, ldc, M, N, K, epi, 1, 0, 0, s);
-}
-int gemm_split_tc_act(const Split* A, int lda, const __nv_bfloat16* Whi, const __nv_bfloat16* Wlo, Split* C, int ldc,
-                      int M, int N, int K, const GemmEpi& epi, cudaStream_t s) {
-    return launch_tc<2, 2>(reinterpret_cast<const __nv_bfloat16*>(A), lda, M, Whi, Wlo, C, ldc, M, N, K, epi, 1, 0, 0, s);
-}
-int gemm_split_tc_batched(const Split* A, int lda, const __nv_bfloat16* Whi, const __nv_bfloat16* Wlo, float* C, int ldc,
-                          int M, int N, int K, int batch, int64_t rows_per_batch, int64_t sC, cudaStream_t s) {
-    GemmEpi e;
-    int64_t rows_total = rows_per_batch * (batch - 1) + M;
-    return launch_tc<2, 0>(reinterpret_cast<const __nv_bfloat16*>(A), lda, rows_total, Whi, Wlo, C, ldc, M, N, K, e, batch,
-                           rows_per_batch, sC, s);
+int gemm_tc(int np, int out, const void* A, int lda, const __nv_bfloat16* W0, const __nv_bfloat16* W1, void* C, int ldc,
+            int M, int N, int K, const GemmEpi& epi, int fl, int n3, cudaStream_t s) {
+    const __nv_bfloat16* a = reinterpret_cast<const __nv_bfloat16*>(A);
+    if (np == 1 && out == 0) return launch_tc<1, 0>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
+    if (np == 1 && out == 1) return launch_tc<1, 1>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
+    if (np == 2 && out == 0) return launch_tc<2, 0>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
+    if (np == 2 && out == 2) return launch_tc<2, 2>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
+    return DW_ERR_ARG;
 }
 
 }  // namespace dw
@@ -342,10 +477,8 @@ int dw_debug_gemm_bf16(const void* A, int lda, const void* Wt, const void* Wt_lo
                        void* stream) {
     if (!dw::tc_available()) return DW_ERR_UNSUPPORTED;
     dw::GemmEpi e;
-    if (Wt_lo)
-        return dw::gemm_split_tc((const dw::Split*)A, lda, (const __nv_bfloat16*)Wt, (const __nv_bfloat16*)Wt_lo, C, ldc,
-                                 M, N, K, e, (cudaStream_t)stream);
-    return dw::gemm_bf16_tc((const __nv_bfloat16*)A, lda, (const __nv_bfloat16*)Wt, C, ldc, M, N, K, e, (cudaStream_t)stream);
+    return dw::gemm_tc(Wt_lo ? 2 : 1, 0, A, lda, (const __nv_bfloat16*)Wt, (const __nv_bfloat16*)Wt_lo, C, ldc, M, N, K,
+                       e, 0, 0, (cudaStream_t)stream);
 }
 
 // Reads and clears the device-side error flag of the tensor-core kernels (1 = a bounded wait timed out).

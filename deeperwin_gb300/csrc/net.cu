@@ -318,7 +318,7 @@ __global__ void k_envelope(const float* __restrict__ r, const float* __restrict_
             lapv += e * (a * a - 2.f * a / dd);
         }
     }
-    const float* bf = BF + bi * d.Tp * ldbf + col;
+    const float* bf = BF + bi * d.Tp * ldbf + (up ? 0 : d.KN) + col;
     int64_t mstride = (int64_t)d.n * d.n;                    // per channel
     float* mo = MO + (((int64_t)b * d.K + k) * d.T) * mstride + i * d.n + o;
     float bf0 = bf[0];

@@ -137,12 +137,14 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
     uint64_t* tempty = tfull + 2;    // [2]
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
     __shared__ int s_err;
+    __shared__ int s_epi_err;   // written only by epilogue warps, read after their named barrier
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nk = (a.K + BK - 1) / BK;
 
     if (threadIdx.x == 0) {
         s_err = 0;
+        s_epi_err = 0;
         for (int s = 0; s < S; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
         for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 4); }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -229,7 +231,10 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
         for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++it) {
             const int m0 = (tile / a.n_tiles_n) * BM, n0 = (tile % a.n_tiles_n) * BN;
             const uint32_t acc = it & 1;
-            if (!mbar_wait(&tfull[acc], (it >> 1) & 1)) { atomicExch(&s_err, 1); break; }
+            const bool ready = mbar_wait(&tfull[acc], (it >> 1) & 1);
+            if (!ready && lane == 0) s_epi_err = 1;
+            epi_bar();                               // all four epilogue warps agree before leaving
+            if (*(volatile int*)&s_epi_err) { if (lane == 0) atomicExch(&s_err, 1); break; }
             tc_fence_after();
             const int row = q * 32 + lane;           // row within the tile
             const int m = m0 + row;

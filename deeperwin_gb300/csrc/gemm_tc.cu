@@ -402,9 +402,10 @@ int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __
               int M, int N, int K, const GemmEpi& epi, int fl, int n3, cudaStream_t s) {
     if (M <= 0 || N <= 0 || K <= 0) return DW_OK;
     constexpr int CW = OUT == 0 ? 32 : 64;
-    int ntn = (N + 255) / 256;
+    constexpr int BN_MAX = NP == 2 ? 128 : 256;      // keeps >= 2 pipeline stages in shared memory
+    int ntn = (N + BN_MAX - 1) / BN_MAX;
     int BN = round_up((N + ntn - 1) / ntn, CW);
-    if (BN > 256) { ntn += 1; BN = round_up((N + ntn - 1) / ntn, CW); }
+    while (BN > BN_MAX) { ntn += 1; BN = round_up((N + ntn - 1) / ntn, CW); }
     const int Kp = round_up(K, 64);
     CUtensorMap ma0, ma1, mb0, mb1, mc0, mc1;
     DW_CHECK(make_map(&ma0, A, M, K, (int64_t)NP * lda, 64, BM, false));

@@ -75,14 +75,112 @@ __global__ void k_slogdet(const float* __restrict__ MO, int n, int T, int nmat, 
     }
 }
 
+// Register-resident variant for n <= NMAX <= 32: a team of NMAX lanes per matrix, lane c owns
+// column c of [A | I] in registers. Partial pivoting: the owner of the pivot column finds the
+// first row of maximal |a| at or below the diagonal; every lane swaps and eliminates its own
+// column with the broadcast pivot-column entries.
+template <class S, int NMAX>
+__global__ void __launch_bounds__(128)
+k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, int want_inv,
+              double* __restrict__ logdet, double* __restrict__ sign, float* __restrict__ Ainv) {
+    const int lane = threadIdx.x & 31;
+    const int team = lane / NMAX, c = lane % NMAX;            // team within the warp, owned column
+    const int teams_per_warp = 32 / NMAX;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int mat = gw * teams_per_warp + team;
+    const bool active = mat < nmat;
+    S col[NMAX], icol[NMAX];
+    const float* A = MO + (int64_t)(active ? mat : 0) * T * n * n;
+    #pragma unroll
+    for (int r = 0; r < NMAX; ++r) {
+        col[r] = (active && r < n && c < n) ? (S)A[r * n + c] : (S)0;
+        icol[r] = (r == c) ? (S)1 : (S)0;
+    }
+    double ld = 0.0, sg = 1.0;
+    bool singular = false;
+    // every lane runs all n steps (teams of one warp share the shuffles); a singular matrix
+    // only sets its flag and continues with a unit pivot
+    for (int k = 0; k < n; ++k) {
+        // pivot search by the owner of column k
+        S best = (S)-1; int p = k;
+        #pragma unroll
+        for (int r = 0; r < NMAX; ++r) {
+            S v = col[r] < (S)0 ? -col[r] : col[r];
+            if (r >= k && r < n && v > best) { best = v; p = r; }
+        }
+        p = __shfl_sync(0xffffffffu, p, team * NMAX + k);
+        best = __shfl_sync(0xffffffffu, best, team * NMAX + k);
+        if (!(best > (S)0)) singular = true;
+        if (p != k) {
+            S xk = 0, xp = 0, ik = 0, ip = 0;
+            #pragma unroll
+            for (int r = 0; r < NMAX; ++r) {
+                if (r == k) { xk = col[r]; ik = icol[r]; }
+                if (r == p) { xp = col[r]; ip = icol[r]; }
+            }
+            #pragma unroll
+            for (int r = 0; r < NMAX; ++r) {
+                if (r == k) { col[r] = xp; icol[r] = ip; }
+                if (r == p) { col[r] = xk; icol[r] = ik; }
+            }
+            sg = -sg;
+        }
+        // pivot-column entries (after the swap), broadcast from the owner of column k
+        S pivcol[NMAX];
+        #pragma unroll
+        for (int r = 0; r < NMAX; ++r) pivcol[r] = __shfl_sync(0xffffffffu, col[r], team * NMAX + k);
+        S pk = 0;
+        #pragma unroll
+        for (int r = 0; r < NMAX; ++r) if (r == k) pk = pivcol[r];
+        if (singular) pk = (S)1;
+        ld += log(fabs((double)pk));
+        if (pk < (S)0) sg = -sg;
+        const S inv = (S)1 / pk;
+        // scale row k of this lane's columns, then eliminate the other rows
+        S rk = 0, irk = 0;
+        #pragma unroll
+        for (int r = 0; r < NMAX; ++r) if (r == k) { col[r] *= inv; icol[r] *= inv; rk = col[r]; irk = icol[r]; }
+        #pragma unroll
+        for (int r = 0; r < NMAX; ++r) {
+            if (r == k || r >= n) continue;
+            if (!want_inv && r < k) continue;
+            const S f = pivcol[r];
+            col[r] -= f * rk;
+            icol[r] -= f * irk;
+        }
+    }
+    if (active && c == 0) {
+        logdet[mat] = singular ? -INFINITY : ld;
+        sign[mat] = singular ? 0.0 : sg;
+    }
+    if (active && want_inv && c < n) {
+        float* out = Ainv + (int64_t)mat * n * n;
+        #pragma unroll
+        for (int r = 0; r < NMAX; ++r)
+            if (r < n) out[r * n + c] = singular ? 0.f : (float)icol[r];
+    }
+}
+
 template <class S>
 void launch_slogdet(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, cudaStream_t s) {
     int n = d.n, want_inv = d.Tp > 1 ? 1 : 0;
+    int nmat = B * d.K;
+    if (n <= 32) {
+        auto go = [&](auto kern, int nmax) {
+            int teams = 32 / nmax;
+            int64_t warps = (nmat + teams - 1) / teams;
+            kern<<<(unsigned)((warps * 32 + 127) / 128), 128, 0, s>>>(MO, n, d.T, nmat, want_inv, logdet, sign, Ainv);
+        };
+        if (n <= 8) go(k_slogdet_reg<S, 8>, 8);
+        else if (n <= 16) go(k_slogdet_reg<S, 16>, 16);
+        else go(k_slogdet_reg<S, 32>, 32);
+        count_launch();
+        return;
+    }
     int nc = want_inv ? 2 * n : n;
     size_t per = (size_t)n * nc * sizeof(S);
     int wpb = (int)(96 * 1024 / per);
     wpb = wpb < 1 ? 1 : (wpb > 8 ? 8 : wpb);
-    int nmat = B * d.K;
     size_t sm = per * wpb;
     if (sm > 48 * 1024) cudaFuncSetAttribute(k_slogdet<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_slogdet<S><<<(nmat + wpb - 1) / wpb, wpb * 32, sm, s>>>(MO, n, d.T, nmat, want_inv, logdet, sign, Ainv);
@@ -143,9 +241,83 @@ __global__ void k_det_tangents(const float* __restrict__ MO, const float* __rest
     if (tid == 0) lapdet[mat] = lap_acc;
 }
 
+// Warp per (walker, determinant) for n <= 32: A^-1 staged in shared memory, lanes split into
+// G = 32 / n groups, each group takes one tangent channel at a time and lane j of a group owns
+// column j of dA_t and of C_t = A^-1 dA_t. tr(C_t) and tr(C_t^2) are accumulated in FP64.
+__global__ void __launch_bounds__(128)
+k_det_tangents_warp(const float* __restrict__ MO, const float* __restrict__ Ainv, const double* __restrict__ sign,
+                    int n, int T, int nmat, double* __restrict__ g, double* __restrict__ lapdet) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    const int mat = blockIdx.x * wpb + wid;
+    const int G = 32 / n;                 // channel groups per warp
+    // per warp: A^-1 (ais floats) then G group areas of cgs floats (C_t with row pitch n + 1, later
+    // reused for 2 n double partials); both sizes are even so the doubles stay 8-byte aligned
+    const int ais = (n * n + 1) & ~1, cgs = ((n * (n + 1) > 4 * n ? n * (n + 1) : 4 * n) + 1) & ~1;
+    float* Ai = reinterpret_cast<float*>(smem_raw) + (size_t)wid * (ais + G * cgs);
+    float* Cs = Ai + ais;
+    if (mat >= nmat) return;
+    if (sign[mat] == 0.0) {
+        for (int t = lane; t < 3 * n; t += 32) g[(int64_t)mat * 3 * n + t] = 0.0;
+        if (lane == 0) lapdet[mat] = 0.0;
+        return;
+    }
+    for (int e = lane; e < n * n; e += 32) Ai[e] = Ainv[(int64_t)mat * n * n + e];
+    __syncwarp();
+    const int grp = lane / n, j = lane % n;
+    const bool on = grp < G;
+    float* Cg = Cs + (size_t)(on ? grp : 0) * cgs;
+    double lap_acc = 0.0;
+    for (int t0 = 1; t0 < T; t0 += G) {
+        const int t = t0 + grp;
+        const bool valid = on && t < T;
+        float col[32];
+        const float* src = MO + ((int64_t)mat * T + (valid ? t : 0)) * n * n;
+        #pragma unroll
+        for (int m = 0; m < 32; ++m) col[m] = (valid && m < n) ? src[m * n + j] : 0.f;
+        for (int a = 0; a < n; ++a) {
+            float acc = 0.f;
+            #pragma unroll
+            for (int m = 0; m < 32; ++m) if (m < n) acc = fmaf(Ai[a * n + m], col[m], acc);
+            if (valid) Cg[a * (n + 1) + j] = acc;
+        }
+        __syncwarp();
+        // lane j: C[j][j] and sum_a C[a][j] C[j][a]; the group leader adds the n lane partials
+        double p0 = 0.0, p1 = 0.0;
+        if (valid) {
+            p0 = (double)Cg[j * (n + 1) + j];
+            if (t != T - 1)
+                for (int a = 0; a < n; ++a) p1 += (double)Cg[a * (n + 1) + j] * (double)Cg[j * (n + 1) + a];
+        }
+        __syncwarp();
+        double* part = reinterpret_cast<double*>(Cg);     // reuse the C area as [n][2] doubles
+        if (valid) { part[2 * j] = p0; part[2 * j + 1] = p1; }
+        __syncwarp();
+        if (valid && j == 0) {
+            double s0 = 0.0, s1 = 0.0;
+            for (int jj = 0; jj < n; ++jj) { s0 += part[2 * jj]; s1 += part[2 * jj + 1]; }
+            if (t == T - 1) lap_acc += s0;
+            else { g[(int64_t)mat * 3 * n + (t - 1)] = s0; lap_acc -= s1; }
+        }
+        __syncwarp();
+    }
+    // combine the group-leader partial Laplacian sums
+    for (int o = 16; o > 0; o >>= 1) lap_acc += __shfl_xor_sync(0xffffffffu, lap_acc, o);
+    if (lane == 0) lapdet[mat] = lap_acc;
+}
+
 void launch_det_tangents(const float* MO, const float* Ainv, const double* sign, const Dims& d, int B,
                          double* g, double* lapdet, cudaStream_t s) {
     int nmat = B * d.K;
+    if (d.n <= 32) {
+        const int n = d.n, G = 32 / n, wpb = 4;
+        const int ais = (n * n + 1) & ~1, cgs = ((n * (n + 1) > 4 * n ? n * (n + 1) : 4 * n) + 1) & ~1;
+        size_t sm = (size_t)wpb * (ais + G * cgs) * sizeof(float);
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k_det_tangents_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_det_tangents_warp<<<(nmat + wpb - 1) / wpb, wpb * 32, sm, s>>>(MO, Ainv, sign, n, d.T, nmat, g, lapdet);
+        count_launch();
+        return;
+    }
     size_t sm = 3 * (size_t)d.n * d.n * sizeof(float);
     if (sm > 48 * 1024) cudaFuncSetAttribute(k_det_tangents, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_det_tangents<<<nmat, 128, sm, s>>>(MO, Ainv, sign, d.n, d.T, nmat, g, lapdet);

@@ -244,30 +244,56 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
             const bool is_val = t == 0, is_grad = t >= 1 && t <= a.n3, is_lap = a.fl && t == a.n3 + 1;
             for (int c0 = 0; c0 < BN; c0 += CW) {
                 float v[CW];
+                float rbv[CW];
+                // vectorized bias / row-bias loads for this chunk, issued before the TMEM reads
+                // (rows of one walker share their row-bias rows, so neighbouring warps hit in L1)
+                const bool full_chunk = n0 + c0 + CW <= a.N;
+                #pragma unroll
+                for (int j = 0; j < CW; j += 4) {
+                    float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+                    const int n = n0 + c0 + j;
+                    if (rb) {
+                        if (full_chunk) x = __ldg(reinterpret_cast<const float4*>(rb + n));
+                        else {
+                            if (n < a.N) x.x = __ldg(rb + n);
+                            if (n + 1 < a.N) x.y = __ldg(rb + n + 1);
+                            if (n + 2 < a.N) x.z = __ldg(rb + n + 2);
+                            if (n + 3 < a.N) x.w = __ldg(rb + n + 3);
+                        }
+                    }
+                    if (e.bias && is_val) {
+                        if (full_chunk) {
+                            float4 b4 = __ldg(reinterpret_cast<const float4*>(e.bias + n));
+                            x.x += b4.x; x.y += b4.y; x.z += b4.z; x.w += b4.w;
+                        } else {
+                            if (n < a.N) x.x += __ldg(e.bias + n);
+                            if (n + 1 < a.N) x.y += __ldg(e.bias + n + 1);
+                            if (n + 2 < a.N) x.z += __ldg(e.bias + n + 2);
+                            if (n + 3 < a.N) x.w += __ldg(e.bias + n + 3);
+                        }
+                    }
+                    rbv[j] = x.x; rbv[j + 1] = x.y; rbv[j + 2] = x.z; rbv[j + 3] = x.w;
+                }
                 const uint32_t base = tmem + acc * (uint32_t)BN + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
                 #pragma unroll
                 for (int j = 0; j < CW; j += 16) tmem_ld16(base + j, v + j);
                 tmem_wait_ld();
                 #pragma unroll
-                for (int j = 0; j < CW; ++j) {
-                    const int n = n0 + c0 + j;
-                    float x = v[j];
-                    if (n < a.N) {
-                        if (e.bias && is_val) x += __ldg(e.bias + n);
-                        if (rb) x += __ldg(rb + n);
-                    }
-                    v[j] = x;
-                }
+                for (int j = 0; j < CW; ++j) v[j] += rbv[j];
                 if (a.fl) {
                     // forward-Laplacian tanh over the Tp channel rows of each electron
                     if (Tp <= 32) {
+                        const int src0 = lane & ~(Tp - 1);
                         #pragma unroll
                         for (int j = 0; j < CW; ++j) {
                             float sq = is_grad ? v[j] * v[j] : 0.f;
-                            for (int o = 1; o < Tp; o <<= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-                            const float z0 = __shfl_sync(0xffffffffu, v[j], lane & ~(Tp - 1));
-                            const float y0 = tanhf(z0), d1 = 1.f - y0 * y0;
-                            v[j] = is_val ? y0 : (is_grad ? d1 * v[j] : (is_lap ? d1 * v[j] - 2.f * y0 * d1 * sq : 0.f));
+                            #pragma unroll
+                            for (int o = 1; o < 32; o <<= 1)
+                                if (o < Tp) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+                            const float y0 = __shfl_sync(0xffffffffu, tanhf(v[j]), src0);
+                            const float d1 = 1.f - y0 * y0;
+                            const float g = d1 * v[j];
+                            v[j] = is_val ? y0 : (is_lap ? g - 2.f * y0 * d1 * sq : (is_grad ? g : 0.f));
                         }
                     } else {
                         float* xs = xchg + (size_t)xbuf * 2 * 4 * 64;    // [2 arrays][4 quarters][64]
@@ -276,8 +302,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                             float sq = is_grad ? v[j] * v[j] : 0.f;
                             #pragma unroll
                             for (int o = 1; o < 32; o <<= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-                            const float z0 = __shfl_sync(0xffffffffu, v[j], 0);
-                            if (lane == 0) { xs[q * 64 + j] = sq; xs[4 * 64 + q * 64 + j] = z0; }
+                            if (lane == 0) { xs[q * 64 + j] = sq; xs[4 * 64 + q * 64 + j] = v[j]; }
                         }
                         epi_bar();
                         const int qs = Tp / 32, g0 = (q / qs) * qs;
@@ -285,9 +310,9 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                         for (int j = 0; j < CW; ++j) {
                             float sq = 0.f;
                             for (int k = 0; k < qs; ++k) sq += xs[(g0 + k) * 64 + j];
-                            const float z0 = xs[4 * 64 + g0 * 64 + j];
-                            const float y0 = tanhf(z0), d1 = 1.f - y0 * y0;
-                            v[j] = is_val ? y0 : (is_grad ? d1 * v[j] : (is_lap ? d1 * v[j] - 2.f * y0 * d1 * sq : 0.f));
+                            const float y0 = tanhf(xs[4 * 64 + g0 * 64 + j]), d1 = 1.f - y0 * y0;
+                            const float g = d1 * v[j];
+                            v[j] = is_val ? y0 : (is_lap ? g - 2.f * y0 * d1 * sq : (is_grad ? g : 0.f));
                         }
                         xbuf ^= 1;   // the other exchange buffer is written only after the next barrier
                     }

@@ -73,104 +73,169 @@ __global__ void k_features(const float* __restrict__ r, const float* __restrict_
 }
 
 // ------------------------------------------------------------------ 2-el and el-ion streams
-// One warp per unordered electron pair (pair streams) or per (electron, ion) (el-ion stream);
-// lane f owns output feature f. Pair streams: ferminet_embedding.py:137-150 (w maps) and
-// :247-253 (h_same / h_diff MLPs, residual (x+y)/sqrt2 on equal widths, mlp.py:13-17).
+// One thread per unordered electron pair (pair streams) or per (electron, ion) (el-ion stream),
+// its CH x 32 activations in registers. Pair streams: ferminet_embedding.py:137-150 (w maps)
+// and :247-253 (h_same / h_diff MLPs, residual (x+y)/sqrt2 on equal widths, mlp.py:13-17).
 // El-ion stream: ferminet_embedding.py:259-262.
 //
-// WP[l][b][i*n+j][ch][32], ch = (f, f', f'') in tangent mode, (f) in value mode.
-// HE[l][b][i*N+I][ch][32], ch = (f, dx, dy, dz, lap) or (f).
+// The 2-el features depend on r only through d = |r_j - r_i| (use_el_el_differences=False),
+// so they carry CH = 3 Taylor channels (f, df/dd, d2f/dd2); the el-ion stream carries
+// CH = 5 channels (f, d/dx_i, d/dy_i, d/dz_i, Laplacian_i). Value-only mode: CH = 1.
+//
+// WP[l][b][i*n+j][ch][32] and HE[l][b][i*N+I][ch][32].
+
+// y = tanh(z) with Taylor / Laplacian channels; CH = 3: 1-D Taylor (f, f', f''), CH = 5:
+// (f, 3 gradients, Laplacian), CH = 1: value only.
 template <int CH>
-__device__ __forceinline__ void dense32(const float (&x)[CH], int in_w, const float* __restrict__ W,
-                                        const float* __restrict__ bias, float (&z)[CH], int lane) {
-    #pragma unroll
-    for (int c = 0; c < CH; ++c) z[c] = 0.f;
-    z[0] = __ldg(bias + lane);
-    for (int k = 0; k < in_w; ++k) {
-        float w = __ldg(W + k * 32 + lane);
-        #pragma unroll
-        for (int c = 0; c < CH; ++c) z[c] += __shfl_sync(0xffffffffu, x[c], k) * w;
+__device__ __forceinline__ void tanh_taylor(const float (&z)[CH], float (&y)[CH]) {
+    const float t = tanhf(z[0]), d1 = 1.f - t * t;
+    y[0] = t;
+    if (CH == 3) { y[1] = d1 * z[1]; y[2] = d1 * z[2] - 2.f * t * d1 * z[1] * z[1]; }
+    if (CH == 5) {
+        const float sq = z[1] * z[1] + z[2] * z[2] + z[3] * z[3];
+        y[1] = d1 * z[1]; y[2] = d1 * z[2]; y[3] = d1 * z[3]; y[4] = d1 * z[4] - 2.f * t * d1 * sq;
     }
 }
 
-__global__ void k_pair_streams(const float* __restrict__ r, const float* __restrict__ P, ParamLayout L, Dims d,
-                               int B, int tangent, float* __restrict__ WP) {
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    int npair = d.n * (d.n + 1) / 2;
-    if (warp >= B * npair) return;
-    int b = warp / npair, p = warp % npair;
-    // unordered pair (i <= j) from linear index
+// out[c][f] = tanh-Taylor(sum_k h[c][k] W[k][f] + b[f] [c == 0]) for four output features at a time.
+template <int CH>
+__device__ __forceinline__ void dense_quad(const float (&h)[CH][32], int in_w, const float* __restrict__ W,
+                                           const float* __restrict__ bias, int f, float (&y)[CH][4]) {
+    float z[CH][4];
+    const float4 b4 = __ldg(reinterpret_cast<const float4*>(bias + f));
+    #pragma unroll
+    for (int c = 0; c < CH; ++c) { z[c][0] = z[c][1] = z[c][2] = z[c][3] = 0.f; }
+    z[0][0] = b4.x; z[0][1] = b4.y; z[0][2] = b4.z; z[0][3] = b4.w;
+    #pragma unroll
+    for (int k = 0; k < 32; ++k) {
+        if (k < in_w) {
+            const float4 w = __ldg(reinterpret_cast<const float4*>(W + k * 32 + f));
+            #pragma unroll
+            for (int c = 0; c < CH; ++c) {
+                z[c][0] = fmaf(h[c][k], w.x, z[c][0]); z[c][1] = fmaf(h[c][k], w.y, z[c][1]);
+                z[c][2] = fmaf(h[c][k], w.z, z[c][2]); z[c][3] = fmaf(h[c][k], w.w, z[c][3]);
+            }
+        }
+    }
+    #pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        float zz[CH], yy[CH];
+        #pragma unroll
+        for (int c = 0; c < CH; ++c) zz[c] = z[c][u];
+        tanh_taylor<CH>(zz, yy);
+        #pragma unroll
+        for (int c = 0; c < CH; ++c) y[c][u] = yy[c];
+    }
+}
+
+// h <- residual(dense(h)) through one shared-memory row per thread (row pitch CH*32 + 1).
+template <int CH>
+__device__ __forceinline__ void stream_layer(float (&h)[CH][32], int in_w, const float* __restrict__ W,
+                                             const float* __restrict__ bias, bool resid, float* row) {
+    for (int f = 0; f < 32; f += 4) {
+        float y[CH][4];
+        dense_quad<CH>(h, in_w, W, bias, f, y);
+        #pragma unroll
+        for (int c = 0; c < CH; ++c)
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) row[c * 32 + f + u] = y[c][u];
+    }
+    const float rs = 0.70710678118654752f;
+    #pragma unroll
+    for (int c = 0; c < CH; ++c)
+        #pragma unroll
+        for (int k = 0; k < 32; ++k) h[c][k] = resid ? (h[c][k] + row[c * 32 + k]) * rs : row[c * 32 + k];
+}
+
+template <int CH>
+__global__ void __launch_bounds__(128)
+k_pair_streams(const float* __restrict__ r, const float* __restrict__ P, ParamLayout L, Dims d, int B,
+               float* __restrict__ WP) {
+    extern __shared__ float srow[];
+    float* row = srow + threadIdx.x * (CH * 32 + 1);
+    const int npair = d.n * (d.n + 1) / 2;
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (int64_t)B * npair) return;
+    const int b = (int)(gid / npair), p = (int)(gid % npair);
     int i = 0, rem = p;
     while (rem >= d.n - i) { rem -= d.n - i; ++i; }
-    int j = i + rem;
-    bool same = (i < d.nu) == (j < d.nu);
+    const int j = i + rem;
+    const bool same = (i < d.nu) == (j < d.nu);
     const float* rb = r + (int64_t)b * d.n * 3;
     float dd = 0.f;
     if (i != j) {
-        float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
+        const float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
         dd = sqrtf(dx * dx + dy * dy + dz * dz);
     }
-    const int CH = 3;
-    float h[CH], z[CH], w[CH];
-    // input feature [dist]: value d, d' = 1, d'' = 0 (diagonal: constant 0, utils.py:297-300)
-    h[0] = lane == 0 ? dd : 0.f;
-    h[1] = (lane == 0 && i != j) ? 1.f : 0.f;
-    h[2] = 0.f;
-    int64_t plane = (int64_t)B * d.n * d.n;      // elements per l (in units of pair records)
-    int chs = tangent ? 3 : 1;
+    float h[CH][32];
+    #pragma unroll
+    for (int c = 0; c < CH; ++c)
+        #pragma unroll
+        for (int k = 0; k < 32; ++k) h[c][k] = 0.f;
+    // input feature [dist]: value d, d' = 1, d'' = 0; the diagonal is the constant 0 (utils.py:297-300)
+    h[0][0] = dd;
+    if (CH == 3) h[1][0] = (i != j) ? 1.f : 0.f;
+    const int64_t plane = (int64_t)B * d.n * d.n;
     for (int l = 0; l < 4; ++l) {
-        int in_w = d.eew[l];
+        const int in_w = d.eew[l];
         const float* Wm = P + (same ? L.w_same_w[l] : L.w_diff_w[l]);
         const float* bm = P + (same ? L.w_same_b[l] : L.w_diff_b[l]);
-        dense32<CH>(h, in_w, Wm, bm, z, lane);
-        float y = tanhf(z[0]), d1 = 1.f - y * y;
-        w[0] = y; w[1] = d1 * z[1]; w[2] = d1 * z[2] - 2.f * y * d1 * z[1] * z[1];
-        float* o1 = WP + ((int64_t)l * plane + (int64_t)b * d.n * d.n + i * d.n + j) * chs * 32;
-        float* o2 = WP + ((int64_t)l * plane + (int64_t)b * d.n * d.n + j * d.n + i) * chs * 32;
-        for (int c = 0; c < chs; ++c) { o1[c * 32 + lane] = w[c]; o2[c * 32 + lane] = w[c]; }
+        float* o1 = WP + ((int64_t)l * plane + (int64_t)b * d.n * d.n + i * d.n + j) * CH * 32;
+        float* o2 = WP + ((int64_t)l * plane + (int64_t)b * d.n * d.n + j * d.n + i) * CH * 32;
+        for (int f = 0; f < 32; f += 4) {
+            float y[CH][4];
+            dense_quad<CH>(h, in_w, Wm, bm, f, y);
+            #pragma unroll
+            for (int c = 0; c < CH; ++c) {
+                const float4 v = make_float4(y[c][0], y[c][1], y[c][2], y[c][3]);
+                *reinterpret_cast<float4*>(o1 + c * 32 + f) = v;
+                if (i != j) *reinterpret_cast<float4*>(o2 + c * 32 + f) = v;
+            }
+        }
         if (l < 3) {
             const float* Ws = P + (same ? L.h_same_w[l] : L.h_diff_w[l]);
             const float* bs = P + (same ? L.h_same_b[l] : L.h_diff_b[l]);
-            dense32<CH>(h, in_w, Ws, bs, z, lane);
-            float yy = tanhf(z[0]), e1 = 1.f - yy * yy;
-            float hn[CH] = {yy, e1 * z[1], e1 * z[2] - 2.f * yy * e1 * z[1] * z[1]};
-            const float rs = 0.70710678118654752f;
-            #pragma unroll
-            for (int c = 0; c < CH; ++c) h[c] = (l == 0) ? hn[c] : (h[c] + hn[c]) * rs;
+            stream_layer<CH>(h, in_w, Ws, bs, l > 0, row);
         }
     }
 }
 
-__global__ void k_ei_streams(const float* __restrict__ r, const float* __restrict__ R, const float* __restrict__ P,
-                             ParamLayout L, Dims d, int B, int tangent, float* __restrict__ HE) {
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    int nei = d.n * d.N;
-    if (warp >= B * nei) return;
-    int b = warp / nei, p = warp % nei;
-    int i = p / d.N, I = p % d.N;
+template <int CH>
+__global__ void __launch_bounds__(128)
+k_ei_streams(const float* __restrict__ r, const float* __restrict__ R, const float* __restrict__ P, ParamLayout L,
+             Dims d, int B, float* __restrict__ HE) {
+    extern __shared__ float srow[];
+    float* row = srow + threadIdx.x * (CH * 32 + 1);
+    const int nei = d.n * d.N;
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (int64_t)B * nei) return;
+    const int b = (int)(gid / nei), p = (int)(gid % nei);
+    const int i = p / d.N, I = p % d.N;
     const float* ri = r + ((int64_t)b * d.n + i) * 3;
-    float s[3] = {ri[0] - R[I * 3], ri[1] - R[I * 3 + 1], ri[2] - R[I * 3 + 2]};
-    float dd = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
-    const int CH = 5;
-    float h[CH];
-    // [d, sx, sy, sz] (input_features.py:56-66)
-    h[0] = lane == 0 ? dd : (lane < 4 ? s[lane - 1] : 0.f);
-    for (int c = 0; c < 3; ++c) h[1 + c] = lane == 0 ? s[c] / dd : (lane == c + 1 ? 1.f : 0.f);
-    h[4] = lane == 0 ? 2.f / dd : 0.f;
-    int chs = tangent ? 5 : 1;
-    int64_t plane = (int64_t)B * nei;
-    for (int l = 0; l < 4; ++l) {
-        float* o = HE + ((int64_t)l * plane + (int64_t)b * nei + p) * chs * 32;
-        for (int c = 0; c < chs; ++c) o[c * 32 + lane] = h[c];
-        if (l == 3) break;
-        float z[CH];
-        dense32<CH>(h, d.eiw[l], P + L.h_ei_w[l], P + L.h_ei_b[l], z, lane);
-        float y = tanhf(z[0]), d1 = 1.f - y * y;
-        float sq = z[1] * z[1] + z[2] * z[2] + z[3] * z[3];
-        float hn[CH] = {y, d1 * z[1], d1 * z[2], d1 * z[3], d1 * z[4] - 2.f * y * d1 * sq};
-        const float rs = 0.70710678118654752f;
+    const float s[3] = {ri[0] - R[I * 3], ri[1] - R[I * 3 + 1], ri[2] - R[I * 3 + 2]};
+    const float dd = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    float h[CH][32];
+    #pragma unroll
+    for (int c = 0; c < CH; ++c)
         #pragma unroll
-        for (int c = 0; c < CH; ++c) h[c] = (l == 0) ? hn[c] : (h[c] + hn[c]) * rs;
+        for (int k = 0; k < 32; ++k) h[c][k] = 0.f;
+    // [d, sx, sy, sz] (input_features.py:56-66)
+    h[0][0] = dd; h[0][1] = s[0]; h[0][2] = s[1]; h[0][3] = s[2];
+    if (CH == 5) {
+        #pragma unroll
+        for (int c = 0; c < 3; ++c) { h[1 + c][0] = s[c] / dd; h[1 + c][1 + c] = 1.f; }
+        h[4][0] = 2.f / dd;
+    }
+    const int64_t plane = (int64_t)B * nei;
+    for (int l = 0; l < 4; ++l) {
+        float* o = HE + ((int64_t)l * plane + (int64_t)b * nei + p) * CH * 32;
+        #pragma unroll
+        for (int c = 0; c < CH; ++c)
+            #pragma unroll
+            for (int k = 0; k < 32; k += 4)
+                *reinterpret_cast<float4*>(o + c * 32 + k) = make_float4(h[c][k], h[c][k + 1], h[c][k + 2], h[c][k + 3]);
+        if (l == 3) break;
+        stream_layer<CH>(h, d.eiw[l], P + L.h_ei_w[l], P + L.h_ei_b[l], l > 0, row);
     }
 }
 
@@ -362,12 +427,20 @@ void launch_features(const float* r, const float* R, const Dims& d, int B, Act* 
 }
 void launch_streams(const float* r, const float* R, const float* P, const ParamLayout& L, const Dims& d, int B,
                     float* WP, float* HE, cudaStream_t s) {
-    int tang = d.Tp > 1;
-    int npair = d.n * (d.n + 1) / 2;
-    int64_t warps = (int64_t)B * npair;
-    k_pair_streams<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(r, P, L, d, B, tang, WP); count_launch();
-    warps = (int64_t)B * d.n * d.N;
-    k_ei_streams<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(r, R, P, L, d, B, tang, HE); count_launch();
+    const bool tang = d.Tp > 1;
+    const int64_t npair = (int64_t)B * d.n * (d.n + 1) / 2, nei = (int64_t)B * d.n * d.N;
+    auto blocks = [](int64_t n) { return (unsigned)((n + 127) / 128); };
+    if (tang) {
+        size_t sm3 = 128 * (3 * 32 + 1) * sizeof(float), sm5 = 128 * (5 * 32 + 1) * sizeof(float);
+        cudaFuncSetAttribute(k_ei_streams<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm5);
+        k_pair_streams<3><<<blocks(npair), 128, sm3, s>>>(r, P, L, d, B, WP);
+        k_ei_streams<5><<<blocks(nei), 128, sm5, s>>>(r, R, P, L, d, B, HE);
+    } else {
+        size_t sm1 = 128 * (32 + 1) * sizeof(float);
+        k_pair_streams<1><<<blocks(npair), 128, sm1, s>>>(r, P, L, d, B, WP);
+        k_ei_streams<1><<<blocks(nei), 128, sm1, s>>>(r, R, P, L, d, B, HE);
+    }
+    count_launch(2);
 }
 template <class Act>
 void launch_spin_means(const Act* X, int ldx, int hw, const Dims& d, int B, Act* M, int mw, cudaStream_t s) {

@@ -75,85 +75,109 @@ __global__ void k_slogdet(const float* __restrict__ MO, int n, int T, int nmat, 
     }
 }
 
-// Register-resident variant for n <= NMAX <= 32: a team of NMAX lanes per matrix, lane c owns
-// column c of [A | I] in registers. Partial pivoting: the owner of the pivot column finds the
-// first row of maximal |a| at or below the diagonal; every lane swaps and eliminates its own
-// column with the broadcast pivot-column entries.
-template <class S, int NMAX>
+// Register-resident variant for n <= NMAX <= 32: a team of n lanes per matrix (32 / n
+// matrices per warp), lane c owning column c of A (and of the identity block when INV).
+// Partial pivoting: the owner of the pivot column finds the first row of maximal |a| at or
+// below the diagonal (as LAPACK getrf) and broadcasts it; every lane swaps and eliminates
+// its own column. The pivot product is kept as an FP64 mantissa and a binary exponent
+// (frexp) so only one log is taken per matrix; divisions happen on the pivot owner only.
+template <class S, int NMAX, bool INV>
 __global__ void __launch_bounds__(128)
-k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, int want_inv,
-              double* __restrict__ logdet, double* __restrict__ sign, float* __restrict__ Ainv) {
+k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
+              double* __restrict__ sign, float* __restrict__ Ainv) {
     const int lane = threadIdx.x & 31;
-    const int team = lane / NMAX, c = lane % NMAX;            // team within the warp, owned column
-    const int teams_per_warp = 32 / NMAX;
+    const int teams = 32 / n;
+    const int team = lane / n, c = lane % n;
+    const bool lane_on = team < teams;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int mat = gw * teams_per_warp + team;
-    const bool active = mat < nmat;
+    const int mat = gw * teams + (lane_on ? team : 0);
+    const bool active = lane_on && mat < nmat;
+    const int src_base = (lane_on ? team : 0) * n;
     S col[NMAX], icol[NMAX];
     const float* A = MO + (int64_t)(active ? mat : 0) * T * n * n;
     #pragma unroll
     for (int r = 0; r < NMAX; ++r) {
-        col[r] = (active && r < n && c < n) ? (S)A[r * n + c] : (S)0;
-        icol[r] = (r == c) ? (S)1 : (S)0;
+        col[r] = (active && r < n) ? (S)A[r * n + c] : (S)0;
+        if (INV) icol[r] = (r == c) ? (S)1 : (S)0;
     }
-    double ld = 0.0, sg = 1.0;
+    double mant = 1.0, sg = 1.0;
+    int expo = 0;
     bool singular = false;
     // every lane runs all n steps (teams of one warp share the shuffles); a singular matrix
     // only sets its flag and continues with a unit pivot
     for (int k = 0; k < n; ++k) {
-        // pivot search by the owner of column k
+        const int owner = src_base + k;
         S best = (S)-1; int p = k;
         #pragma unroll
         for (int r = 0; r < NMAX; ++r) {
-            S v = col[r] < (S)0 ? -col[r] : col[r];
+            const S v = col[r] < (S)0 ? -col[r] : col[r];
             if (r >= k && r < n && v > best) { best = v; p = r; }
         }
-        p = __shfl_sync(0xffffffffu, p, team * NMAX + k);
-        best = __shfl_sync(0xffffffffu, best, team * NMAX + k);
-        if (!(best > (S)0)) singular = true;
+        p = __shfl_sync(0xffffffffu, p, owner);
+        best = __shfl_sync(0xffffffffu, best, owner);
+        const bool sing_now = !(best > (S)0);
+        singular = singular || sing_now;
         if (p != k) {
             S xk = 0, xp = 0, ik = 0, ip = 0;
             #pragma unroll
             for (int r = 0; r < NMAX; ++r) {
-                if (r == k) { xk = col[r]; ik = icol[r]; }
-                if (r == p) { xp = col[r]; ip = icol[r]; }
+                if (r == k) { xk = col[r]; if (INV) ik = icol[r]; }
+                if (r == p) { xp = col[r]; if (INV) ip = icol[r]; }
             }
             #pragma unroll
             for (int r = 0; r < NMAX; ++r) {
-                if (r == k) { col[r] = xp; icol[r] = ip; }
-                if (r == p) { col[r] = xk; icol[r] = ik; }
+                if (r == k) { col[r] = xp; if (INV) icol[r] = ip; }
+                if (r == p) { col[r] = xk; if (INV) icol[r] = ik; }
             }
             sg = -sg;
         }
-        // pivot-column entries (after the swap), broadcast from the owner of column k
-        S pivcol[NMAX];
+        // pivot value and its reciprocal from the owner of column k
+        S mine_k = 0;
         #pragma unroll
-        for (int r = 0; r < NMAX; ++r) pivcol[r] = __shfl_sync(0xffffffffu, col[r], team * NMAX + k);
-        S pk = 0;
-        #pragma unroll
-        for (int r = 0; r < NMAX; ++r) if (r == k) pk = pivcol[r];
-        if (singular) pk = (S)1;
-        ld += log(fabs((double)pk));
+        for (int r = 0; r < NMAX; ++r) if (r == k) mine_k = col[r];
+        S pk = __shfl_sync(0xffffffffu, mine_k, owner);
+        if (sing_now) pk = (S)1;
+        S inv = 0;
+        if (c == k) inv = (S)1 / pk;
+        inv = __shfl_sync(0xffffffffu, inv, owner);
+        int e;
+        mant *= frexp(fabs((double)pk), &e);
+        expo += e;
+        mant = frexp(mant, &e);
+        expo += e;
         if (pk < (S)0) sg = -sg;
-        const S inv = (S)1 / pk;
-        // scale row k of this lane's columns, then eliminate the other rows
-        S rk = 0, irk = 0;
+        // column-k entries of every row, broadcast from the owner
+        S f[NMAX];
         #pragma unroll
-        for (int r = 0; r < NMAX; ++r) if (r == k) { col[r] *= inv; icol[r] *= inv; rk = col[r]; irk = icol[r]; }
-        #pragma unroll
-        for (int r = 0; r < NMAX; ++r) {
-            if (r == k || r >= n) continue;
-            if (!want_inv && r < k) continue;
-            const S f = pivcol[r];
-            col[r] -= f * rk;
-            icol[r] -= f * irk;
+        for (int r = 0; r < NMAX; ++r) f[r] = __shfl_sync(0xffffffffu, col[r], owner);
+        if (INV) {
+            // Gauss-Jordan: scale row k, eliminate all other rows
+            S rk = 0, irk = 0;
+            #pragma unroll
+            for (int r = 0; r < NMAX; ++r) if (r == k) { col[r] *= inv; icol[r] *= inv; rk = col[r]; irk = icol[r]; }
+            #pragma unroll
+            for (int r = 0; r < NMAX; ++r) {
+                if (r == k || r >= n) continue;
+                col[r] -= f[r] * rk;
+                icol[r] -= f[r] * irk;
+            }
+        } else {
+            // LU: eliminate the rows below the pivot
+            S rk = 0;
+            #pragma unroll
+            for (int r = 0; r < NMAX; ++r) if (r == k) rk = col[r];
+            #pragma unroll
+            for (int r = 0; r < NMAX; ++r) {
+                if (r <= k || r >= n) continue;
+                col[r] -= (f[r] * inv) * rk;
+            }
         }
     }
     if (active && c == 0) {
-        logdet[mat] = singular ? -INFINITY : ld;
+        logdet[mat] = singular ? -INFINITY : log(mant) + (double)expo * 0.69314718055994530942;
         sign[mat] = singular ? 0.0 : sg;
     }
-    if (active && want_inv && c < n) {
+    if (INV && active) {
         float* out = Ainv + (int64_t)mat * n * n;
         #pragma unroll
         for (int r = 0; r < NMAX; ++r)
@@ -166,14 +190,19 @@ void launch_slogdet(const float* MO, const Dims& d, int B, double* logdet, doubl
     int n = d.n, want_inv = d.Tp > 1 ? 1 : 0;
     int nmat = B * d.K;
     if (n <= 32) {
-        auto go = [&](auto kern, int nmax) {
-            int teams = 32 / nmax;
-            int64_t warps = (nmat + teams - 1) / teams;
-            kern<<<(unsigned)((warps * 32 + 127) / 128), 128, 0, s>>>(MO, n, d.T, nmat, want_inv, logdet, sign, Ainv);
-        };
-        if (n <= 8) go(k_slogdet_reg<S, 8>, 8);
-        else if (n <= 16) go(k_slogdet_reg<S, 16>, 16);
-        else go(k_slogdet_reg<S, 32>, 32);
+        const int teams = 32 / n;
+        const int64_t warps = (nmat + teams - 1) / teams;
+        const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
+        auto go = [&](auto kern) { kern<<<blocks, 128, 0, s>>>(MO, n, d.T, nmat, logdet, sign, Ainv); };
+        if (want_inv) {
+            if (n <= 8) go(k_slogdet_reg<S, 8, true>);
+            else if (n <= 16) go(k_slogdet_reg<S, 16, true>);
+            else go(k_slogdet_reg<S, 32, true>);
+        } else {
+            if (n <= 8) go(k_slogdet_reg<S, 8, false>);
+            else if (n <= 16) go(k_slogdet_reg<S, 16, false>);
+            else go(k_slogdet_reg<S, 32, false>);
+        }
         count_launch();
         return;
     }

@@ -433,6 +433,7 @@ void launch_streams(const float* r, const float* R, const float* P, const ParamL
     if (tang) {
         size_t sm3 = 128 * (3 * 32 + 1) * sizeof(float), sm5 = 128 * (5 * 32 + 1) * sizeof(float);
         cudaFuncSetAttribute(k_ei_streams<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm5);
+        cudaFuncSetAttribute(k_pair_streams<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
         k_pair_streams<3><<<blocks(npair), 128, sm3, s>>>(r, P, L, d, B, WP);
         k_ei_streams<5><<<blocks(nei), 128, sm5, s>>>(r, R, P, L, d, B, HE);
     } else {

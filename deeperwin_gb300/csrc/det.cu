@@ -1,6 +1,7 @@
 // Determinants, their forward-mode derivatives, the multi-determinant combine, the
 // Jastrow add, the kinetic energy and the Coulomb potential.
 #include "net.cuh"
+#include <type_traits>
 
 namespace dw {
 
@@ -103,39 +104,36 @@ k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, double* __re
     double mant = 1.0, sg = 1.0;
     int expo = 0;
     bool singular = false;
-    // every lane runs all n steps (teams of one warp share the shuffles); a singular matrix
-    // only sets its flag and continues with a unit pivot
-    for (int k = 0; k < n; ++k) {
+    // All loops are unrolled over NMAX (== n for the exact-size instances, so no predicated-off
+    // FP64 work is issued). Every lane runs all steps (teams of one warp share the shuffles); a
+    // singular matrix only sets its flag and continues with a unit pivot.
+    #pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+        if (k >= n) break;
         const int owner = src_base + k;
-        S best = (S)-1; int p = k;
+        // pivot search in FP32 magnitudes (first maximum wins; only the owner's result is used)
+        float best = -1.f; int p = k;
         #pragma unroll
-        for (int r = 0; r < NMAX; ++r) {
-            const S v = col[r] < (S)0 ? -col[r] : col[r];
-            if (r >= k && r < n && v > best) { best = v; p = r; }
+        for (int r = k; r < NMAX; ++r) {
+            const float v = fabsf((float)col[r]);
+            if (r < n && v > best) { best = v; p = r; }
         }
         p = __shfl_sync(0xffffffffu, p, owner);
         best = __shfl_sync(0xffffffffu, best, owner);
-        const bool sing_now = !(best > (S)0);
-        singular = singular || sing_now;
+        bool sing_now = !(best > 0.f);
         if (p != k) {
-            S xk = 0, xp = 0, ik = 0, ip = 0;
+            S xk = col[k], xp = 0, ik = INV ? icol[k] : (S)0, ip = 0;
             #pragma unroll
-            for (int r = 0; r < NMAX; ++r) {
-                if (r == k) { xk = col[r]; if (INV) ik = icol[r]; }
-                if (r == p) { xp = col[r]; if (INV) ip = icol[r]; }
-            }
+            for (int r = k + 1; r < NMAX; ++r) if (r == p) { xp = col[r]; if (INV) ip = icol[r]; }
+            col[k] = xp;
+            if (INV) icol[k] = ip;
             #pragma unroll
-            for (int r = 0; r < NMAX; ++r) {
-                if (r == k) { col[r] = xp; if (INV) icol[r] = ip; }
-                if (r == p) { col[r] = xk; if (INV) icol[r] = ik; }
-            }
+            for (int r = k + 1; r < NMAX; ++r) if (r == p) { col[r] = xk; if (INV) icol[r] = ik; }
             sg = -sg;
         }
-        // pivot value and its reciprocal from the owner of column k
-        S mine_k = 0;
-        #pragma unroll
-        for (int r = 0; r < NMAX; ++r) if (r == k) mine_k = col[r];
-        S pk = __shfl_sync(0xffffffffu, mine_k, owner);
+        S pk = __shfl_sync(0xffffffffu, col[k], owner);
+        sing_now = sing_now || pk == (S)0;
+        singular = singular || sing_now;
         if (sing_now) pk = (S)1;
         S inv = 0;
         if (c == k) inv = (S)1 / pk;
@@ -146,30 +144,24 @@ k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, double* __re
         mant = frexp(mant, &e);
         expo += e;
         if (pk < (S)0) sg = -sg;
-        // column-k entries of every row, broadcast from the owner
-        S f[NMAX];
-        #pragma unroll
-        for (int r = 0; r < NMAX; ++r) f[r] = __shfl_sync(0xffffffffu, col[r], owner);
         if (INV) {
-            // Gauss-Jordan: scale row k, eliminate all other rows
-            S rk = 0, irk = 0;
-            #pragma unroll
-            for (int r = 0; r < NMAX; ++r) if (r == k) { col[r] *= inv; icol[r] *= inv; rk = col[r]; irk = icol[r]; }
+            // Gauss-Jordan: scale row k, eliminate all other rows with the broadcast column-k entries
+            col[k] *= inv;
+            icol[k] *= inv;
+            const S rk = col[k], irk = icol[k];
             #pragma unroll
             for (int r = 0; r < NMAX; ++r) {
-                if (r == k || r >= n) continue;
-                col[r] -= f[r] * rk;
-                icol[r] -= f[r] * irk;
+                if (r == k) continue;
+                const S f = __shfl_sync(0xffffffffu, col[r], owner);
+                if (r < n) { col[r] -= f * rk; icol[r] -= f * irk; }
             }
         } else {
-            // LU: eliminate the rows below the pivot
-            S rk = 0;
+            // LU: eliminate the rows below the pivot; the owner pre-scales its column by 1/pivot
+            const S rk = col[k];
             #pragma unroll
-            for (int r = 0; r < NMAX; ++r) if (r == k) rk = col[r];
-            #pragma unroll
-            for (int r = 0; r < NMAX; ++r) {
-                if (r <= k || r >= n) continue;
-                col[r] -= (f[r] * inv) * rk;
+            for (int r = k + 1; r < NMAX; ++r) {
+                const S f = __shfl_sync(0xffffffffu, col[r] * inv, owner);
+                if (r < n) col[r] -= f * rk;
             }
         }
     }
@@ -194,14 +186,24 @@ void launch_slogdet(const float* MO, const Dims& d, int B, double* logdet, doubl
         const int64_t warps = (nmat + teams - 1) / teams;
         const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
         auto go = [&](auto kern) { kern<<<blocks, 128, 0, s>>>(MO, n, d.T, nmat, logdet, sign, Ainv); };
-        if (want_inv) {
-            if (n <= 8) go(k_slogdet_reg<S, 8, true>);
-            else if (n <= 16) go(k_slogdet_reg<S, 16, true>);
-            else go(k_slogdet_reg<S, 32, true>);
-        } else {
-            if (n <= 8) go(k_slogdet_reg<S, 8, false>);
-            else if (n <= 16) go(k_slogdet_reg<S, 16, false>);
-            else go(k_slogdet_reg<S, 32, false>);
+        bool done = false;
+        if constexpr (std::is_same<S, double>::value) {
+            // exact-size instances of the FP64 form for the common electron counts
+            done = true;
+#define DW_SLOGDET_CASE(NN) case NN: if (want_inv) go(k_slogdet_reg<S, NN, true>); else go(k_slogdet_reg<S, NN, false>); break;
+            switch (n) {
+                DW_SLOGDET_CASE(2) DW_SLOGDET_CASE(3) DW_SLOGDET_CASE(4) DW_SLOGDET_CASE(5) DW_SLOGDET_CASE(6)
+                DW_SLOGDET_CASE(7) DW_SLOGDET_CASE(8) DW_SLOGDET_CASE(9) DW_SLOGDET_CASE(10) DW_SLOGDET_CASE(12)
+                DW_SLOGDET_CASE(14) DW_SLOGDET_CASE(16)
+                default: done = false;
+            }
+#undef DW_SLOGDET_CASE
+        }
+        if (!done) {
+            if (n <= 8) { if (want_inv) go(k_slogdet_reg<S, 8, true>); else go(k_slogdet_reg<S, 8, false>); }
+            else if (n <= 16) { if (want_inv) go(k_slogdet_reg<S, 16, true>); else go(k_slogdet_reg<S, 16, false>); }
+            else if (n <= 24) { if (want_inv) go(k_slogdet_reg<S, 24, true>); else go(k_slogdet_reg<S, 24, false>); }
+            else { if (want_inv) go(k_slogdet_reg<S, 32, true>); else go(k_slogdet_reg<S, 32, false>); }
         }
         count_launch();
         return;

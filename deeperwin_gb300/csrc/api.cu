@@ -354,6 +354,7 @@ static size_t plan_bytes(const DwArch* a, int B, bool tang) {
 
 template <class Act>
 static size_t ws_bytes_t(const DwArch* a, int n_walkers, int mode) {
+    if (mode == 3) return bwd_bytes(a, n_walkers, nullptr);
     if (mode == 2) {
         size_t b = plan_bytes<Act>(a, n_walkers, false);
         b += (size_t)n_walkers * a->n_el * 3 * sizeof(float) + 256;      // proposals
@@ -498,6 +499,19 @@ int dw_mcmc_steps(const DwArch* a, int precision, const float* params, const voi
         DW_CHECK_CUDA(cudaGetLastError());
         return (int)DW_OK;
     });
+}
+
+int dw_log_psi_sqr_backward(const DwArch* a, int precision, const float* params, const void* prepared, const float* r,
+                            int B, const float* R, const int32_t* Z, const float* coeff, float* grad, void* ws,
+                            size_t wsb, void* stream) {
+    reset_launch_count();
+    DW_CHECK(check_arch(a));
+    if (!params || !prepared || !r || !R || !Z || !coeff || !grad || B <= 0) return DW_ERR_ARG;
+    if (precision < DW_PRECISION_FP32 || precision > DW_PRECISION_BF16) return DW_ERR_ARG;
+    Prepared pre = carve_prepared(a, precision, const_cast<void*>(prepared));
+    const float* m4[4] = {pre.main[0], pre.main[1], pre.main[2], pre.main[3]};
+    const float* n4[4] = {pre.mean[0], pre.mean[1], pre.mean[2], pre.mean[3]};
+    return backward_all(a, params, m4, n4, pre.bf_cat, r, B, R, Z, coeff, grad, ws, wsb, (cudaStream_t)stream);
 }
 
 int dw_energy_stats(const float* E, int n, double* out, void* stream) {

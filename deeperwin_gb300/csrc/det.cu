@@ -178,8 +178,19 @@ k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, double* __re
 }
 
 template <class S>
+void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, int want_inv,
+                         cudaStream_t s);
+template <class S>
 void launch_slogdet(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, cudaStream_t s) {
-    int n = d.n, want_inv = d.Tp > 1 ? 1 : 0;
+    launch_slogdet_impl<S>(MO, d, B, logdet, sign, Ainv, d.Tp > 1 ? 1 : 0, s);
+}
+void launch_slogdet_inv(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, cudaStream_t s) {
+    launch_slogdet_impl<double>(MO, d, B, logdet, sign, Ainv, 1, s);
+}
+template <class S>
+void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, int want_inv,
+                         cudaStream_t s) {
+    int n = d.n;
     int nmat = B * d.K;
     if (n <= 32) {
         const int teams = 32 / n;

@@ -3,10 +3,11 @@
 // optional tanh for value-only rows). No TF32: the reference disables it
 // (NVIDIA_TF32_OVERRIDE=0, process_molecule.py:20-29).
 #include "net.cuh"
+#include <algorithm>
 
 namespace dw {
 
-template <int BM, int BN, int BK, int TM, int TN>
+template <int BM, int BN, int BK, int TM, int TN, bool TRANS_W = false, bool ACC = false>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 k_gemm_f32(const float* __restrict__ A, int lda, const float* __restrict__ W, int ldw, float* __restrict__ C, int ldc,
            int M, int N, int K, GemmEpi epi, int64_t sA, int64_t sC) {
@@ -35,7 +36,8 @@ k_gemm_f32(const float* __restrict__ A, int lda, const float* __restrict__ W, in
         for (int e = tid; e < BK * BN; e += NT) {
             int kk = e / BN, cc = e % BN;
             int gk = k0 + kk, gn = n0 + cc;
-            Ws[buf][kk][cc] = (gk < K && gn < N) ? __ldg(W + (int64_t)gk * ldw + gn) : 0.f;
+            Ws[buf][kk][cc] = (gk < K && gn < N) ? __ldg(TRANS_W ? W + (int64_t)gn * ldw + gk : W + (int64_t)gk * ldw + gn)
+                                                 : 0.f;
         }
     };
     int nk = (K + BK - 1) / BK;
@@ -72,7 +74,8 @@ k_gemm_f32(const float* __restrict__ A, int lda, const float* __restrict__ W, in
             if (epi.bias && t == 0) v += epi.bias[n];
             if (rb) v += rb[n];
             if (epi.act == 1) v = tanhf(v);
-            C[(int64_t)m * ldc + n] = v;
+            if (ACC) C[(int64_t)m * ldc + n] += v;
+            else C[(int64_t)m * ldc + n] = v;
         }
     }
 }
@@ -89,6 +92,88 @@ void gemm_f32(const float* A, int lda, const float* W, int ldw, float* C, int ld
         dim3 g((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
         k_gemm_f32<BM, BN, 8, 8, 4><<<g, (BM / 8) * (BN / 4), 0, s>>>(A, lda, W, ldw, C, ldc, M, N, K, epi, sA, sC);
     }
+    count_launch();
+}
+
+void gemm_f32_nt(const float* A, int lda, const float* W, int ldw, float* C, int ldc, int M, int N, int K,
+                 int accumulate, cudaStream_t s) {
+    if (M <= 0 || N <= 0) return;
+    GemmEpi epi;
+    constexpr int BM = 128, BN = 64;
+    dim3 g((N + BN - 1) / BN, (M + BM - 1) / BM, 1);
+    if (accumulate)
+        k_gemm_f32<BM, BN, 8, 8, 4, true, true><<<g, (BM / 8) * (BN / 4), 0, s>>>(A, lda, W, ldw, C, ldc, M, N, K, epi, 0, 0);
+    else
+        k_gemm_f32<BM, BN, 8, 8, 4, true, false><<<g, (BM / 8) * (BN / 4), 0, s>>>(A, lda, W, ldw, C, ldc, M, N, K, epi, 0, 0);
+    count_launch();
+}
+
+// Weight gradient: 64 x 64 output tiles, rows split into segments over grid.z; each block
+// stages 32-row slabs of A and G in shared memory and accumulates a 4 x 4 patch per thread.
+__global__ void __launch_bounds__(256)
+k_wgrad_f32(const float* __restrict__ A, int lda, const float* __restrict__ G, int ldg, int rows, int K, int N,
+            float* __restrict__ dW, int lddw, float* __restrict__ dB, const int8_t* __restrict__ sel, int want,
+            int rows_per_seg) {
+    __shared__ float As[32][64 + 1];
+    __shared__ float Gs[32][64 + 1];
+    const int k0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    const int r_begin = blockIdx.z * rows_per_seg, r_end = min(rows, r_begin + rows_per_seg);
+    const int tid = threadIdx.x, tk = tid / 16, tn = tid % 16;
+    float acc[4][4] = {{0.f}};
+    float bacc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int r0 = r_begin; r0 < r_end; r0 += 32) {
+        for (int e = tid; e < 32 * 64; e += 256) {
+            const int rr = e / 64, cc = e % 64, r = r0 + rr;
+            bool ok = r < r_end && (!sel || sel[r] == want);
+            As[rr][cc] = (ok && k0 + cc < K) ? A[(int64_t)r * lda + k0 + cc] : 0.f;
+            Gs[rr][cc] = (ok && n0 + cc < N) ? G[(int64_t)r * ldg + n0 + cc] : 0.f;
+        }
+        __syncthreads();
+        #pragma unroll 4
+        for (int rr = 0; rr < 32; ++rr) {
+            float a[4], g[4];
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) { a[u] = As[rr][tk + 16 * u]; g[u] = Gs[rr][tn + 16 * u]; }
+            #pragma unroll
+            for (int u = 0; u < 4; ++u)
+                #pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], g[v], acc[u][v]);
+            if (dB && blockIdx.y == 0 && tk == 0) {
+                #pragma unroll
+                for (int v = 0; v < 4; ++v) bacc[v] += g[v];
+            }
+        }
+        __syncthreads();
+    }
+    #pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int k = k0 + tk + 16 * u;
+        if (k >= K) continue;
+        #pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int n = n0 + tn + 16 * v;
+            if (n < N) atomicAdd(dW + (int64_t)k * lddw + n, acc[u][v]);
+        }
+    }
+    if (dB && blockIdx.y == 0 && tk == 0) {
+        #pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int n = n0 + tn + 16 * v;
+            if (n < N) atomicAdd(dB + n, bacc[v]);
+        }
+    }
+}
+
+void wgrad_f32(const float* A, int lda, const float* G, int ldg, int rows, int K, int N, float* dW, int lddw,
+               float* dB, const int8_t* sel, int want, cudaStream_t s) {
+    if (rows <= 0 || K <= 0 || N <= 0) return;
+    const int tiles = ((K + 63) / 64) * ((N + 63) / 64);
+    int segs = std::max(1, std::min((rows + 255) / 256, (4 * 152 + tiles - 1) / tiles));
+    int rps = (rows + segs - 1) / segs;
+    rps = (rps + 31) / 32 * 32;
+    segs = (rows + rps - 1) / rps;
+    dim3 g((N + 63) / 64, (K + 63) / 64, segs);
+    k_wgrad_f32<<<g, 256, 0, s>>>(A, lda, G, ldg, rows, K, N, dW, lddw, dB, sel, want, rps);
     count_launch();
 }
 

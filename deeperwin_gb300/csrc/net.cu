@@ -150,7 +150,7 @@ __device__ __forceinline__ void stream_layer(float (&h)[CH][32], int in_w, const
 template <int CH>
 __global__ void __launch_bounds__(128)
 k_pair_streams(const float* __restrict__ r, const float* __restrict__ P, ParamLayout L, Dims d, int B,
-               float* __restrict__ WP) {
+               float* __restrict__ WP, float* __restrict__ HP) {
     extern __shared__ float srow[];
     float* row = srow + threadIdx.x * (CH * 32 + 1);
     const int npair = d.n * (d.n + 1) / 2;
@@ -196,6 +196,12 @@ k_pair_streams(const float* __restrict__ r, const float* __restrict__ P, ParamLa
             const float* Ws = P + (same ? L.h_same_w[l] : L.h_diff_w[l]);
             const float* bs = P + (same ? L.h_same_b[l] : L.h_diff_b[l]);
             stream_layer<CH>(h, in_w, Ws, bs, l > 0, row);
+            if (HP && CH == 1) {      // keep h^(l+1) of this unordered pair for the backward pass
+                float* o = HP + ((int64_t)l * B * npair + gid) * 32;
+                #pragma unroll
+                for (int k = 0; k < 32; k += 4)
+                    *reinterpret_cast<float4*>(o + k) = make_float4(h[0][k], h[0][k + 1], h[0][k + 2], h[0][k + 3]);
+            }
         }
     }
 }
@@ -354,6 +360,86 @@ __global__ void k_conv(const float* __restrict__ r, const float* __restrict__ WP
     }
 }
 
+// Block per walker: the walker's h_map tangents (n x Tp x 32) and pair geometry are staged in
+// shared memory once, then every (electron, channel, column) output of conv_ee / conv_ei is
+// formed from shared memory. Same mathematics as k_conv.
+template <class Act>
+__global__ void __launch_bounds__(256)
+k_conv_walker(const float* __restrict__ r, const float* __restrict__ WPl, const float* __restrict__ HM,
+              const float* __restrict__ HEl, const float* __restrict__ himl, Dims d, int l, int B,
+              Act* __restrict__ X, int ldx) {
+    extern __shared__ float smc[];
+    const int b = blockIdx.x;
+    const int n = d.n, Tp = d.Tp, T = d.T;
+    const int hw = d.hw[l], E = d.E, eiw = d.eiw[l];
+    const int ncol = E + eiw;
+    const int pch = Tp > 1 ? 3 : 1, ech = Tp > 1 ? 5 : 1;
+    float* hm = smc;                                   // [n][Tp][32]
+    float* geo = hm + (size_t)n * Tp * 32;             // [n][n][4]: u_x, u_y, u_z, 1/d (0 on the diagonal)
+    const float* hmb = HM + (size_t)b * n * Tp * 32;
+    for (int e = threadIdx.x; e < n * Tp * 8; e += blockDim.x)
+        reinterpret_cast<float4*>(hm)[e] = __ldg(reinterpret_cast<const float4*>(hmb) + e);
+    const float* rb = r + (size_t)b * n * 3;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = e / n, j = e % n;
+        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i != j) {
+            const float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
+            const float inv = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
+            g = make_float4(dx * inv, dy * inv, dz * inv, inv);
+        }
+        reinterpret_cast<float4*>(geo)[e] = g;
+    }
+    __syncthreads();
+    const float* wpb = WPl + (size_t)b * n * n * pch * 32;
+    const float* heb = HEl + (size_t)b * n * d.N * ech * 32;
+    const int items = n * Tp * ncol;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const int col = it % ncol, t = (it / ncol) % Tp, i = it / (ncol * Tp);
+        float v = 0.f;
+        if (t < T) {
+            if (col < E) {
+                const int f = col;
+                const float* wrow = wpb + (size_t)i * n * pch * 32 + f;      // record (i, j) at j * pch * 32
+                for (int j = 0; j < n; ++j) v += __ldg(wrow + j * pch * 32) * hm[(j * Tp + t) * 32 + f];
+                if (t >= 1 && t <= 3 * n) {
+                    const int m = (t - 1) / 3, c = (t - 1) % 3;
+                    if (m == i) {
+                        for (int j = 0; j < n; ++j) {
+                            if (j == i) continue;
+                            v -= __ldg(wrow + j * pch * 32 + 32) * geo[(i * n + j) * 4 + c] * hm[(j * Tp) * 32 + f];
+                        }
+                    } else {
+                        v += __ldg(wrow + m * pch * 32 + 32) * geo[(i * n + m) * 4 + c] * hm[(m * Tp) * 32 + f];
+                    }
+                } else if (t == d.lap) {
+                    for (int j = 0; j < n; ++j) {
+                        if (j == i) continue;
+                        const float* gg = geo + (i * n + j) * 4;
+                        const float w1 = __ldg(wrow + j * pch * 32 + 32), w2 = __ldg(wrow + j * pch * 32 + 64);
+                        const float* hj = hm + (size_t)j * Tp * 32 + f;
+                        float cross = 0.f;
+                        #pragma unroll
+                        for (int c = 0; c < 3; ++c) cross += gg[c] * (hj[(1 + 3 * j + c) * 32] - hj[(1 + 3 * i + c) * 32]);
+                        v += 2.f * (w2 + 2.f * w1 * gg[3]) * hj[0] + 2.f * w1 * cross;
+                    }
+                }
+            } else {
+                const int f = col - E;
+                int ch = -1;
+                if (t == 0) ch = 0;
+                else if (t == d.lap) ch = 4;
+                else if (t >= 1 + 3 * i && t < 4 + 3 * i) ch = t - 3 * i;
+                if (ch >= 0) {
+                    const float* he = heb + (size_t)i * d.N * ech * 32;
+                    for (int I = 0; I < d.N; ++I) v += __ldg(he + (I * ech + ch) * 32 + f) * __ldg(himl + I * 32 + f);
+                }
+            }
+        }
+        ActIO<Act>::store(X, ((int64_t)b * n + i) * Tp + t, ldx, hw + col, v);
+    }
+}
+
 // ------------------------------------------------------------------ envelope x backflow -> Slater tangents
 // mo[b][k][t][i][o] = env[i,(k,o)] * bf[i,(k,o)] with tangents (envelope_orbitals.py:91-127).
 // env = sum_I w_I exp(-softplus(alpha_I) d_iI); grad/Laplacian w.r.t. r_i only.
@@ -426,7 +512,7 @@ void launch_features(const float* r, const float* R, const Dims& d, int B, Act* 
     k_features<Act><<<B * d.n, 256, 0, s>>>(r, R, d, B, X0); count_launch();
 }
 void launch_streams(const float* r, const float* R, const float* P, const ParamLayout& L, const Dims& d, int B,
-                    float* WP, float* HE, cudaStream_t s) {
+                    float* WP, float* HE, cudaStream_t s, float* HP) {
     const bool tang = d.Tp > 1;
     const int64_t npair = (int64_t)B * d.n * (d.n + 1) / 2, nei = (int64_t)B * d.n * d.N;
     auto blocks = [](int64_t n) { return (unsigned)((n + 127) / 128); };
@@ -434,11 +520,11 @@ void launch_streams(const float* r, const float* R, const float* P, const ParamL
         size_t sm3 = 128 * (3 * 32 + 1) * sizeof(float), sm5 = 128 * (5 * 32 + 1) * sizeof(float);
         cudaFuncSetAttribute(k_ei_streams<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm5);
         cudaFuncSetAttribute(k_pair_streams<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
-        k_pair_streams<3><<<blocks(npair), 128, sm3, s>>>(r, P, L, d, B, WP);
+        k_pair_streams<3><<<blocks(npair), 128, sm3, s>>>(r, P, L, d, B, WP, nullptr);
         k_ei_streams<5><<<blocks(nei), 128, sm5, s>>>(r, R, P, L, d, B, HE);
     } else {
         size_t sm1 = 128 * (32 + 1) * sizeof(float);
-        k_pair_streams<1><<<blocks(npair), 128, sm1, s>>>(r, P, L, d, B, WP);
+        k_pair_streams<1><<<blocks(npair), 128, sm1, s>>>(r, P, L, d, B, WP, HP);
         k_ei_streams<1><<<blocks(nei), 128, sm1, s>>>(r, R, P, L, d, B, HE);
     }
     count_launch(2);
@@ -455,7 +541,15 @@ void launch_tanh_fl(const float* Zb, int ldz, int ncols, int groups, const Dims&
 template <class Act>
 void launch_conv(const float* r, const float* WPl, const float* HM, const float* HEl, const float* himl, const Dims& d,
                  int l, int B, Act* X, int ldx, cudaStream_t s) {
-    k_conv<Act><<<B * d.n, 256, 0, s>>>(r, WPl, HM, HEl, himl, d, l, B, X, ldx); count_launch();
+    const size_t smem = ((size_t)d.n * d.Tp * 32 + (size_t)d.n * d.n * 4) * sizeof(float);
+    if (smem <= 200 * 1024) {
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_conv_walker<Act>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_conv_walker<Act><<<B, 256, smem, s>>>(r, WPl, HM, HEl, himl, d, l, B, X, ldx);
+    } else {
+        k_conv<Act><<<B * d.n, 256, 0, s>>>(r, WPl, HM, HEl, himl, d, l, B, X, ldx);
+    }
+    count_launch();
 }
 void launch_envelope(const float* r, const float* R, const float* P, const ParamLayout& L, const Dims& d, int B,
                      const float* BF, int ldbf, float* MO, cudaStream_t s) {

@@ -42,7 +42,7 @@ template <> struct ActIO<Split> {
 void launch_ion_maps(const float* P, const ParamLayout& L, const Dims& d, const int32_t* Z, float* him, cudaStream_t s);
 template <class Act> void launch_features(const float* r, const float* R, const Dims& d, int B, Act* X0, cudaStream_t s);
 void launch_streams(const float* r, const float* R, const float* P, const ParamLayout& L, const Dims& d, int B,
-                    float* WP, float* HE, cudaStream_t s);
+                    float* WP, float* HE, cudaStream_t s, float* HP = nullptr);
 template <class Act> void launch_spin_means(const Act* X, int ldx, int hw, const Dims& d, int B, Act* M, int mw, cudaStream_t s);
 template <class Act> void launch_tanh_fl(const float* Zb, int ldz, int ncols, int groups, const Dims& d, Act* Y, int ldy, cudaStream_t s);
 template <class Act> void launch_conv(const float* r, const float* WPl, const float* HM, const float* HEl, const float* himl,
@@ -62,6 +62,13 @@ struct GemmEpi {
 };
 void gemm_f32(const float* A, int lda, const float* W, int ldw, float* C, int ldc, int M, int N, int K,
               const GemmEpi& epi, int batch, int64_t sA, int64_t sC, cudaStream_t s);
+// C[M, N] (+)= A[M, K] @ W^T where W is [N, K] row-major (ldw); accumulate = 1 adds to C.
+void gemm_f32_nt(const float* A, int lda, const float* W, int ldw, float* C, int ldc, int M, int N, int K,
+                 int accumulate, cudaStream_t s);
+// dW[K, N] += sum_r A[r, k] G[r, n] over rows r (row selector sel[r] == want when sel != NULL),
+// dB[N] += sum_r G[r, n] when dB != NULL. Split over rows, atomically accumulated.
+void wgrad_f32(const float* A, int lda, const float* G, int ldg, int rows, int K, int N, float* dW, int lddw,
+               float* dB, const int8_t* sel, int want, cudaStream_t s);
 
 // det.cu
 template <class S>
@@ -72,5 +79,13 @@ void launch_combine(const double* logdet, const double* sign, const double* g, c
                     const float* r, const float* R, const int32_t* Z, const Dims& d, int B,
                     float* log_psi_sqr, float* phase, float* E_loc, float* grad_out, cudaStream_t s);
 void launch_coulomb(const float* r, int B, int n, const float* R, const int32_t* Z, int N, float* E, cudaStream_t s);
+// FP64 Gauss-Jordan log|det| and inverse of the value-channel Slater matrices (any Dims mode).
+void launch_slogdet_inv(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, cudaStream_t s);
+
+// backward.cu
+size_t bwd_bytes(const DwArch* a, int B, int* chunk);
+int backward_all(const DwArch* a, const float* P, const float* const main[4], const float* const mean[4],
+                 const float* bf_cat, const float* r, int B, const float* R, const int32_t* Z, const float* coeff,
+                 float* grad, void* ws, size_t wsb, cudaStream_t s);
 
 }  // namespace dw

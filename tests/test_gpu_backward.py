@@ -1,0 +1,92 @@
+"""GPU tests of the hand-written d log psi^2 / d theta backward (VMC gradient)."""
+import numpy as np
+import pytest
+import torch
+
+from deeperwin_gb300 import api, arch as A, params as P, vmc
+from oracle import dpe4 as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_grad(a, p, r, mol, coeff):
+    pt = {k: torch.tensor(v, dtype=torch.float64, requires_grad=True) for k, v in p.items()}
+    lp = O.log_psi_sqr(pt, a, r, mol.R, mol.Z)[1]
+    (lp * torch.tensor(coeff, dtype=torch.float64)).sum().backward()
+    g = {k: v.grad.numpy() for k, v in pt.items()}
+    lay, total = P.layout(a)
+    flat = np.zeros(total)
+    for k, (o, s) in lay.items():
+        flat[o:o + s] = g[k].reshape(-1)
+    return flat
+
+
+@pytest.mark.parametrize("case", ["lih", "h6", "c2h4"])
+def test_backward_matches_oracle_autograd(cuda, case):
+    mol, K, B = {"lih": (A.lih(), 4, 5), "h6": (A.h_chain(6), 4, 3), "c2h4": (A.c2h4_shaped(), 2, 2)}[case]
+    a = A.arch_for(mol, K)
+    p = P.init_params(a, 2, bias_std=0.1, envelope_jitter=0.2)
+    r = A.init_walkers(mol, B, seed=3)
+    coeff = np.random.default_rng(0).standard_normal(B)
+    params = api.Params.from_dict(a, p, "mixed")
+    g = vmc.log_psi_sqr_backward(params, torch.tensor(r, dtype=torch.float32), mol.R, mol.Z,
+                                 torch.tensor(coeff, dtype=torch.float32)).cpu().numpy().astype(np.float64)
+    ref = _oracle_grad(a, p, r, mol, coeff)
+    scale = np.abs(ref).max()
+    err = np.abs(g - ref)
+    lay, _ = P.layout(a)
+    worst = sorted(((float(err[o:o + s].max() / scale), k) for k, (o, s) in lay.items()), reverse=True)[:3]
+    assert err.max() <= 1e-4 * scale, worst
+    assert np.linalg.norm(g - ref) <= 1e-4 * np.linalg.norm(ref), worst
+
+
+def test_backward_matches_central_finite_differences(cuda):
+    """64 random parameters, central differences with h = 1e-3 on the FP64 oracle forward."""
+    mol = A.lih()
+    a = A.arch_for(mol, 4)
+    p = P.init_params(a, 5, bias_std=0.1, envelope_jitter=0.2)
+    r = A.init_walkers(mol, 4, seed=8)
+    coeff = np.array([0.7, -1.1, 0.4, 0.25])
+    params = api.Params.from_dict(a, p, "mixed")
+    g = vmc.log_psi_sqr_backward(params, torch.tensor(r, dtype=torch.float32), mol.R, mol.Z,
+                                 torch.tensor(coeff, dtype=torch.float32)).cpu().numpy().astype(np.float64)
+    lay, total = P.layout(a)
+    flat = P.pack(a, p).astype(np.float64)
+    valid = np.concatenate([np.arange(o, o + s) for o, s in lay.values()])
+    idx = np.random.default_rng(1).choice(valid, size=64, replace=False)
+    h = 1e-3
+
+    def f(x):
+        q = P.unpack(a, x)
+        return float((O.log_psi_sqr(O.tparams(q), a, r, mol.R, mol.Z)[1].numpy() * coeff).sum())
+    fd = []
+    for k in idx:
+        xp, xm = flat.copy(), flat.copy()
+        xp[k] += h
+        xm[k] -= h
+        fd.append((f(xp) - f(xm)) / (2 * h))
+    fd = np.array(fd)
+    scale = np.abs(fd).max()
+    assert np.abs(g[idx] - fd).max() <= 1e-4 * scale + 1e-6, np.abs(g[idx] - fd).max() / scale
+
+
+def test_autograd_function_and_value_and_grad(cuda):
+    mol = A.h_chain(4)
+    a = A.arch_for(mol, 4)
+    params = api.Params.from_dict(a, P.init_params(a, 1), "mixed")
+    r = torch.tensor(A.init_walkers(mol, 64, seed=2), dtype=torch.float32, device="cuda")
+    flat = params.flat.detach().clone().requires_grad_(True)
+    params.flat = flat.detach()
+    c = torch.randn(64, device="cuda")
+    lp = vmc.LogPsiSqr.apply(flat, params, r, mol.R, mol.Z)
+    (g,) = torch.autograd.grad((lp * c).sum(), flat)
+    g2 = vmc.log_psi_sqr_backward(params, r, mol.R, mol.Z, c)
+    torch.testing.assert_close(g, g2, rtol=1e-5, atol=1e-6)
+    vg = vmc.build_value_and_grad_func()
+    (loss, (state, aux)), grads = vg(params, vmc.init_clipping_state(), (a.n_up, a.n_dn), (r, mol.R, mol.Z))
+    E = aux["E_loc"].double()
+    assert float(loss) == pytest.approx(float(E.mean()), rel=1e-6)     # no clipping at width 1e12
+    coeff = (E - E.mean()) / E.numel()
+    g3 = vmc.log_psi_sqr_backward(params, r, mol.R, mol.Z, coeff.float())
+    torch.testing.assert_close(grads, g3, rtol=1e-4, atol=1e-6)
+    assert state[1] == pytest.approx(5.0 * float(E.std(unbiased=False)), rel=1e-5)

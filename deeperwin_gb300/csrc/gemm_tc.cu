@@ -131,7 +131,8 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
     auto sB = [&](int s, int part) { return smem + (size_t)s * stage_bytes + (size_t)NP * a_bytes + (size_t)part * b_bytes; };
     uint8_t* stage_out = smem + (size_t)S * stage_bytes;                   // [4 warps][NPO][4096]
     float* xchg = reinterpret_cast<float*>(stage_out + 4 * NPO * 4096);    // [2 bufs][2 arrays][4][64]
-    uint64_t* full = reinterpret_cast<uint64_t*>(xchg + 2 * 2 * 4 * 64);
+    float* flbuf = xchg + 2 * 2 * 4 * 64;                                  // [4 warps][4 arrays][4 groups][65]
+    uint64_t* full = reinterpret_cast<uint64_t*>(flbuf + 4 * 4 * 4 * 65);
     uint64_t* empty = full + S;
     uint64_t* tfull = empty + S;     // [2]
     uint64_t* tempty = tfull + 2;    // [2]
@@ -281,41 +282,83 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                 #pragma unroll
                 for (int j = 0; j < CW; ++j) v[j] += rbv[j];
                 if (a.fl) {
-                    // forward-Laplacian tanh over the Tp channel rows of each electron
-                    if (Tp <= 32) {
-                        const int src0 = lane & ~(Tp - 1);
+                    // Forward-Laplacian tanh over the Tp channel rows of each electron. Column sums
+                    // of z_t^2 over the gradient rows and tanh of the value row are formed per
+                    // column through a shared-memory transpose (the staging tile is free here:
+                    // the previous TMA store has finished reading it).
+                    if (lane == 0) bulk_wait_read0();
+                    __syncwarp();
+                    float* sq = reinterpret_cast<float*>(my_out);          // [32 rows][CW] swizzled by 16 B chunks
+                    float* fb = flbuf + (size_t)q * 4 * 4 * 65;            // [array][group][65]
+                    float* Z0 = fb;              // value-row z per group
+                    float* SS = fb + 4 * 65;     // sum of squares per group
+                    float* Y0 = fb + 8 * 65;     // tanh(z0)
+                    float* D1 = fb + 12 * 65;    // 1 - tanh^2
+                    #pragma unroll
+                    for (int j4 = 0; j4 < CW / 4; ++j4) {
+                        float4 x;
+                        x.x = is_grad ? v[4 * j4] * v[4 * j4] : 0.f;
+                        x.y = is_grad ? v[4 * j4 + 1] * v[4 * j4 + 1] : 0.f;
+                        x.z = is_grad ? v[4 * j4 + 2] * v[4 * j4 + 2] : 0.f;
+                        x.w = is_grad ? v[4 * j4 + 3] * v[4 * j4 + 3] : 0.f;
+                        *reinterpret_cast<float4*>(sq + lane * CW + ((j4 ^ (lane & 7)) << 2)) = x;
+                    }
+                    const int G = Tp < 32 ? 32 / Tp : 1;                    // electron groups in this warp
+                    const int grp = Tp < 32 ? lane / Tp : 0;
+                    if (is_val) {
                         #pragma unroll
-                        for (int j = 0; j < CW; ++j) {
-                            float sq = is_grad ? v[j] * v[j] : 0.f;
-                            #pragma unroll
-                            for (int o = 1; o < 32; o <<= 1)
-                                if (o < Tp) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-                            const float y0 = __shfl_sync(0xffffffffu, tanhf(v[j]), src0);
-                            const float d1 = 1.f - y0 * y0;
-                            const float g = d1 * v[j];
-                            v[j] = is_val ? y0 : (is_lap ? g - 2.f * y0 * d1 * sq : (is_grad ? g : 0.f));
+                        for (int j = 0; j < CW; ++j) Z0[grp * 65 + j] = v[j];
+                    }
+                    __syncwarp();
+                    const int rpg = Tp < 32 ? Tp : 32;                      // rows of a group inside this warp
+                    #pragma unroll
+                    for (int h = 0; h < CW / 32; ++h) {
+                        const int c = lane + 32 * h;
+                        for (int g = 0; g < G; ++g) {
+                            float acc = 0.f;
+                            for (int rr = g * rpg; rr < (g + 1) * rpg; ++rr)
+                                acc += sq[rr * CW + ((((c >> 2) ^ (rr & 7))) << 2) + (c & 3)];
+                            SS[g * 65 + c] = acc;
                         }
-                    } else {
-                        float* xs = xchg + (size_t)xbuf * 2 * 4 * 64;    // [2 arrays][4 quarters][64]
+                    }
+                    if (Tp > 32) {
+                        // a group spans several warps: exchange the partial sums and the value row
+                        float* xs = xchg + (size_t)xbuf * 2 * 4 * 64;
                         #pragma unroll
-                        for (int j = 0; j < CW; ++j) {
-                            float sq = is_grad ? v[j] * v[j] : 0.f;
-                            #pragma unroll
-                            for (int o = 1; o < 32; o <<= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-                            if (lane == 0) { xs[q * 64 + j] = sq; xs[4 * 64 + q * 64 + j] = v[j]; }
+                        for (int h = 0; h < CW / 32; ++h) {
+                            const int c = lane + 32 * h;
+                            xs[q * 64 + c] = SS[c];
+                            if ((q * 32) % Tp == 0) xs[4 * 64 + q * 64 + c] = Z0[c];   // this warp holds the value row
                         }
                         epi_bar();
                         const int qs = Tp / 32, g0 = (q / qs) * qs;
                         #pragma unroll
-                        for (int j = 0; j < CW; ++j) {
-                            float sq = 0.f;
-                            for (int k = 0; k < qs; ++k) sq += xs[(g0 + k) * 64 + j];
-                            const float y0 = tanhf(xs[4 * 64 + g0 * 64 + j]), d1 = 1.f - y0 * y0;
-                            const float g = d1 * v[j];
-                            v[j] = is_val ? y0 : (is_lap ? g - 2.f * y0 * d1 * sq : (is_grad ? g : 0.f));
+                        for (int h = 0; h < CW / 32; ++h) {
+                            const int c = lane + 32 * h;
+                            float acc = 0.f;
+                            for (int k = 0; k < qs; ++k) acc += xs[(g0 + k) * 64 + c];
+                            SS[c] = acc;
+                            Z0[c] = xs[4 * 64 + g0 * 64 + c];
                         }
                         xbuf ^= 1;   // the other exchange buffer is written only after the next barrier
                     }
+                    #pragma unroll
+                    for (int h = 0; h < CW / 32; ++h) {
+                        const int c = lane + 32 * h;
+                        for (int g = 0; g < G; ++g) {
+                            const float y0 = tanhf(Z0[g * 65 + c]);
+                            Y0[g * 65 + c] = y0;
+                            D1[g * 65 + c] = 1.f - y0 * y0;
+                        }
+                    }
+                    __syncwarp();
+                    #pragma unroll
+                    for (int j = 0; j < CW; ++j) {
+                        const float y0 = Y0[grp * 65 + j], d1 = D1[grp * 65 + j], ssum = SS[grp * 65 + j];
+                        const float g = d1 * v[j];
+                        v[j] = is_val ? y0 : (is_lap ? g - 2.f * y0 * d1 * ssum : (is_grad ? g : 0.f));
+                    }
+                    __syncwarp();
                 } else if (e.act == 1) {
                     #pragma unroll
                     for (int j = 0; j < CW; ++j) v[j] = tanhf(v[j]);
@@ -455,7 +498,7 @@ int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __
     a.M = M; a.N = N; a.K = K; a.BN = BN; a.epi = epi; a.fl = fl; a.n3 = n3;
     const int stage_bytes = NP * (BM * BK * 2 + BN * BK * 2);
     const int npo = OUT == 2 ? 2 : 1;
-    const int fixed = 1024 + 4 * npo * 4096 + 2 * 2 * 4 * 64 * 4 + 256;
+    const int fixed = 1024 + 4 * npo * 4096 + 2 * 2 * 4 * 64 * 4 + 4 * 4 * 4 * 65 * 4 + 256;
     a.stages = std::min(8, (220 * 1024 - fixed) / stage_bytes);
     if (a.stages < 2) return DW_ERR_ARCH;
     a.tmem_cols = 32;

@@ -81,7 +81,8 @@ def test_autograd_function_and_value_and_grad(cuda):
     lp = vmc.LogPsiSqr.apply(flat, params, r, mol.R, mol.Z)
     (g,) = torch.autograd.grad((lp * c).sum(), flat)
     g2 = vmc.log_psi_sqr_backward(params, r, mol.R, mol.Z, c)
-    torch.testing.assert_close(g, g2, rtol=1e-5, atol=1e-6)
+    # float atomics in the weight-gradient reductions make repeated calls differ in the last bits
+    torch.testing.assert_close(g, g2, rtol=1e-4, atol=1e-4 * float(g2.abs().max()))
     vg = vmc.build_value_and_grad_func()
     (loss, (state, aux)), grads = vg(params, vmc.init_clipping_state(), (a.n_up, a.n_dn), (r, mol.R, mol.Z))
     E = aux["E_loc"].double()

@@ -124,13 +124,14 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr int CW = OUT == 0 ? 32 : 64;             // columns per staged store box (128 bytes per row)
     constexpr int NPO = OUT == 2 ? 2 : 1;              // output parts
+    constexpr int SWB = OUT == 0 ? 4096 : 8192;        // staging bytes per warp (also holds 32 x CW fp32)
     const int S = a.stages, BN = a.BN;
     const uint32_t a_bytes = BM * BK * 2, b_bytes = (uint32_t)BN * BK * 2;
     const uint32_t stage_bytes = NP * (a_bytes + b_bytes);
     auto sA = [&](int s, int part) { return smem + (size_t)s * stage_bytes + (size_t)part * a_bytes; };
     auto sB = [&](int s, int part) { return smem + (size_t)s * stage_bytes + (size_t)NP * a_bytes + (size_t)part * b_bytes; };
-    uint8_t* stage_out = smem + (size_t)S * stage_bytes;                   // [4 warps][NPO][4096]
-    float* xchg = reinterpret_cast<float*>(stage_out + 4 * NPO * 4096);    // [2 bufs][2 arrays][4][64]
+    uint8_t* stage_out = smem + (size_t)S * stage_bytes;                   // [4 warps][SWB]
+    float* xchg = reinterpret_cast<float*>(stage_out + 4 * SWB);           // [2 bufs][2 arrays][4][64]
     float* flbuf = xchg + 2 * 2 * 4 * 64;                                  // [4 warps][4 arrays][4 groups][65]
     uint64_t* full = reinterpret_cast<uint64_t*>(flbuf + 4 * 4 * 4 * 65);
     uint64_t* empty = full + S;
@@ -226,7 +227,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
         const int q = warp & 3;                      // TMEM lane quarter
         const GemmEpi& e = a.epi;
         const int Tp = e.Tp;
-        uint8_t* my_out = stage_out + (size_t)q * NPO * 4096;
+        uint8_t* my_out = stage_out + (size_t)q * SWB;
         uint32_t it = 0;
         int xbuf = 0;
         for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++it) {
@@ -497,8 +498,8 @@ int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __
     TcArgs a;
     a.M = M; a.N = N; a.K = K; a.BN = BN; a.epi = epi; a.fl = fl; a.n3 = n3;
     const int stage_bytes = NP * (BM * BK * 2 + BN * BK * 2);
-    const int npo = OUT == 2 ? 2 : 1;
-    const int fixed = 1024 + 4 * npo * 4096 + 2 * 2 * 4 * 64 * 4 + 4 * 4 * 4 * 65 * 4 + 256;
+    const int swb = OUT == 0 ? 4096 : 8192;
+    const int fixed = 1024 + 4 * swb + 2 * 2 * 4 * 64 * 4 + 4 * 4 * 4 * 65 * 4 + 256;
     a.stages = std::min(8, (220 * 1024 - fixed) / stage_bytes);
     if (a.stages < 2) return DW_ERR_ARCH;
     a.tmem_cols = 32;

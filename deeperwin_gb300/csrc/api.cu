@@ -23,6 +23,7 @@ struct WRef {
 struct Prepared {
     float* main[4]; float* mean[4];
     float* bf_cat;                                   // [D, 2 KN] = [W_up | W_dn]
+    float* sp_alpha;                                 // [2][N][KN] softplus(alpha_up), softplus(alpha_dn)
     __nv_bfloat16* main_bf[2][4]; __nv_bfloat16* mean_bf[2][4]; __nv_bfloat16* map_bf[2][4];
     __nv_bfloat16* bf_bf[2]; __nv_bfloat16* jas0[2]; __nv_bfloat16* jas1[2];
     size_t bytes;
@@ -42,6 +43,7 @@ static Prepared carve_prepared(const DwArch* a, int precision, void* base) {
         p.mean[l] = c.take<float>((size_t)mean_width(d, l) * d.D);
     }
     p.bf_cat = c.take<float>((size_t)d.D * 2 * d.KN);
+    p.sp_alpha = c.take<float>((size_t)2 * d.N * d.KN);
     for (int part = 0; part < tc_parts(precision); ++part) {
         for (int l = 0; l < 4; ++l) {
             p.main_bf[part][l] = c.take<__nv_bfloat16>((size_t)d.kw[l] * d.D);
@@ -54,6 +56,13 @@ static Prepared carve_prepared(const DwArch* a, int precision, void* base) {
     }
     p.bytes = c.used;
     return p;
+}
+
+// softplus of the envelope exponents (parameters only, computed once per parameter update)
+__global__ void k_softplus(const float* __restrict__ a_up, const float* __restrict__ a_dn, int n, float* __restrict__ out) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 2 * n) return;
+    out[idx] = softplus_f(idx < n ? a_up[idx] : a_dn[idx - n]);
 }
 
 // Row gather for the prepared FP32 layer weights: mode 0 builds Wmain (rows h, conv_ee,
@@ -96,6 +105,8 @@ static int prepare(const DwArch* a, int precision, const float* P, void* prep, s
             count_launch();
         }
     }
+    k_softplus<<<(2 * d.N * d.KN + 255) / 256, 256, 0, s>>>(P + L.alpha_up, P + L.alpha_dn, d.N * d.KN, p.sp_alpha);
+    count_launch();
     for (int half = 0; half < 2; ++half) {
         DW_CHECK_CUDA(cudaMemcpy2DAsync(p.bf_cat + half * d.KN, sizeof(float) * 2 * d.KN,
                                         P + (half == 0 ? L.bf_up : L.bf_dn), sizeof(float) * d.KN,
@@ -307,7 +318,7 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         if (pt >= 2) wb.lo = pre.bf_bf[1];
         DW_TIMED("backflow_gemm", DW_CHECK(MM<Act>::mm(H, kXW, wb, p.BF, 2 * d.KN, rows, 2 * d.KN, d.D, e0, s)));
     }
-    DW_TIMED("envelope", launch_envelope(r, R, P, L, d, Bc, p.BF, 2 * d.KN, p.MO, s));
+    DW_TIMED("envelope", launch_envelope(r, R, P, L, pre.sp_alpha, d, Bc, p.BF, 2 * d.KN, p.MO, s));
     if (precision == DW_PRECISION_FP32) DW_TIMED("slogdet", launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
     else DW_TIMED("slogdet", launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
     if (tang) DW_TIMED("det_tangents", launch_det_tangents(p.MO, p.Ainv, p.sign, d, Bc, p.g, p.lapdet, s));
@@ -511,7 +522,8 @@ int dw_log_psi_sqr_backward(const DwArch* a, int precision, const float* params,
     Prepared pre = carve_prepared(a, precision, const_cast<void*>(prepared));
     const float* m4[4] = {pre.main[0], pre.main[1], pre.main[2], pre.main[3]};
     const float* n4[4] = {pre.mean[0], pre.mean[1], pre.mean[2], pre.mean[3]};
-    return backward_all(a, params, m4, n4, pre.bf_cat, r, B, R, Z, coeff, grad, ws, wsb, (cudaStream_t)stream);
+    return backward_all(a, params, m4, n4, pre.bf_cat, pre.sp_alpha, r, B, R, Z, coeff, grad, ws, wsb,
+                        (cudaStream_t)stream);
 }
 
 int dw_energy_stats(const float* E, int n, double* out, void* stream) {

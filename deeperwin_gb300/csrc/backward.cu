@@ -136,8 +136,8 @@ __global__ void k_bwd_dets(const double* __restrict__ logdet, const double* __re
 // Envelope x backflow adjoints per (walker, electron, column): dBF (in the spin's half of the
 // [W_up | W_dn] columns, zero in the other) and dENV = dmo * bf.
 __global__ void k_bwd_envelope(const float* __restrict__ r, const float* __restrict__ R, const float* __restrict__ P,
-                               ParamLayout L, Dims d, int B, const float* __restrict__ BF, const float* __restrict__ dMO,
-                               float* __restrict__ dBF, float* __restrict__ dENV) {
+                               ParamLayout L, const float* __restrict__ spA, Dims d, int B, const float* __restrict__ BF,
+                               const float* __restrict__ dMO, float* __restrict__ dBF, float* __restrict__ dENV) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)B * d.n * d.KN) return;
     const int col = idx % d.KN;
@@ -145,14 +145,14 @@ __global__ void k_bwd_envelope(const float* __restrict__ r, const float* __restr
     const int i = bi % d.n, b = bi / d.n;
     const int k = col / d.n, o = col % d.n;
     const bool up = i < d.nu;
-    const float* alpha = P + (up ? L.alpha_up : L.alpha_dn);
+    const float* spa = spA + (up ? 0 : d.N * d.KN);
     const float* wts = P + (up ? L.weights_up : L.weights_dn);
     const float* ri = r + bi * 3;
     float env = 0.f;
     for (int I = 0; I < d.N; ++I) {
         const float s0 = ri[0] - R[I * 3], s1 = ri[1] - R[I * 3 + 1], s2 = ri[2] - R[I * 3 + 2];
         const float dd = sqrtf(s0 * s0 + s1 * s1 + s2 * s2);
-        env += wts[I * d.KN + col] * expf(-softplus_f(alpha[I * d.KN + col]) * dd);
+        env += wts[I * d.KN + col] * expf(-spa[I * d.KN + col] * dd);
     }
     const float dmo = dMO[(((int64_t)b * d.K + k) * d.n + i) * d.n + o];
     const float bf = BF[bi * 2 * d.KN + (up ? 0 : d.KN) + col];
@@ -428,8 +428,8 @@ inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t
 void launch_slogdet_inv(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, cudaStream_t s);
 
 static int backward_chunk(const Bwd& w, int Bc, const float* P, const ParamLayout& L, const float* prepared_f32_main[4],
-                          const float* prepared_f32_mean[4], const float* bf_cat, const float* r, const float* R,
-                          const int32_t* Z, const float* coeff, float* grad, cudaStream_t s) {
+                          const float* prepared_f32_mean[4], const float* bf_cat, const float* spA, const float* r,
+                          const float* R, const int32_t* Z, const float* coeff, float* grad, cudaStream_t s) {
     const Dims& d = w.d;
     const int rows = Bc * d.n;
     const int npw = d.n * (d.n + 1) / 2;
@@ -454,7 +454,7 @@ static int backward_chunk(const Bwd& w, int Bc, const float* P, const ParamLayou
     }
     GemmEpi e0;
     gemm_f32(w.H4, d.D, bf_cat, 2 * d.KN, w.BF, 2 * d.KN, rows, 2 * d.KN, d.D, e0, 1, 0, 0, s);
-    launch_envelope(r, R, P, L, d, Bc, w.BF, 2 * d.KN, w.MO, s);
+    launch_envelope(r, R, P, L, spA, d, Bc, w.BF, 2 * d.KN, w.MO, s);
     launch_slogdet_inv(w.MO, d, Bc, w.logdet, w.sign, w.Ainv, s);
     GemmEpi j0; j0.bias = P + L.jas_b[0]; j0.act = 1;
     GemmEpi j1; j1.bias = P + L.jas_b[1]; j1.act = 1;
@@ -465,7 +465,7 @@ static int backward_chunk(const Bwd& w, int Bc, const float* P, const ParamLayou
     k_row_coeff<<<nblk(rows), 256, 0, s>>>(coeff, d.n, rows, w.crow);
     // determinants -> Slater matrices -> backflow / envelopes
     k_bwd_dets<<<Bc, 256, 0, s>>>(w.logdet, w.sign, w.Ainv, coeff, d.K, d.n, w.dMO);
-    k_bwd_envelope<<<nblk((int64_t)rows * d.KN), 256, 0, s>>>(r, R, P, L, d, Bc, w.BF, w.dMO, w.dBF, w.dENV);
+    k_bwd_envelope<<<nblk((int64_t)rows * d.KN), 256, 0, s>>>(r, R, P, L, spA, d, Bc, w.BF, w.dMO, w.dBF, w.dENV);
     k_bwd_env_params<<<dim3((d.KN + 31) / 32, d.N, 2), 256, 0, s>>>(r, R, P, L, d, Bc, w.dENV, grad);
     wgrad_f32(w.H4, d.D, w.dBF, 2 * d.KN, rows, d.D, d.KN, grad + L.bf_up, d.KN, nullptr, nullptr, 0, s);
     wgrad_f32(w.H4, d.D, w.dBF + d.KN, 2 * d.KN, rows, d.D, d.KN, grad + L.bf_dn, d.KN, nullptr, nullptr, 0, s);
@@ -544,8 +544,8 @@ size_t bwd_bytes(const DwArch* a, int B, int* chunk) {
 }
 
 int backward_all(const DwArch* a, const float* P, const float* const main[4], const float* const mean[4],
-                 const float* bf_cat, const float* r, int B, const float* R, const int32_t* Z, const float* coeff,
-                 float* grad, void* ws, size_t wsb, cudaStream_t s) {
+                 const float* bf_cat, const float* sp_alpha, const float* r, int B, const float* R, const int32_t* Z,
+                 const float* coeff, float* grad, void* ws, size_t wsb, cudaStream_t s) {
     Dims d = make_dims(a, false);
     if (d.n > 32) return DW_ERR_ARCH;
     ParamLayout L;
@@ -560,7 +560,8 @@ int backward_all(const DwArch* a, const float* P, const float* const main[4], co
         const int nb = std::min(bc, B - b0);
         Bwd wc = w;
         wc.Bc = nb; wc.rows = nb * d.n; wc.npair = nb * d.n * (d.n + 1) / 2; wc.nei = nb * d.n * d.N;
-        DW_CHECK(backward_chunk(wc, nb, P, L, m4, n4, bf_cat, r + (int64_t)b0 * d.n * 3, R, Z, coeff + b0, grad, s));
+        DW_CHECK(backward_chunk(wc, nb, P, L, m4, n4, bf_cat, sp_alpha, r + (int64_t)b0 * d.n * 3, R, Z, coeff + b0,
+                                grad, s));
     }
     return DW_OK;
 }

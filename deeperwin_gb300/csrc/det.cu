@@ -325,11 +325,16 @@ k_det_tangents_warp(const float* __restrict__ MO, const float* __restrict__ Ainv
         }
         __syncwarp();
         // lane j: C[j][j] and sum_a C[a][j] C[j][a]; the group leader adds the n lane partials
+        // lane partials in FP32 (n products of one row/column pair); the cross-lane and
+        // cross-channel trace sums below are accumulated in FP64
         double p0 = 0.0, p1 = 0.0;
         if (valid) {
             p0 = (double)Cg[j * (n + 1) + j];
-            if (t != T - 1)
-                for (int a = 0; a < n; ++a) p1 += (double)Cg[a * (n + 1) + j] * (double)Cg[j * (n + 1) + a];
+            if (t != T - 1) {
+                float q = 0.f;
+                for (int a = 0; a < n; ++a) q = fmaf(Cg[a * (n + 1) + j], Cg[j * (n + 1) + a], q);
+                p1 = (double)q;
+            }
         }
         __syncwarp();
         double* part = reinterpret_cast<double*>(Cg);     // reuse the C area as [n][2] doubles
@@ -429,14 +434,18 @@ __global__ void k_combine(const double* __restrict__ logdet, const double* __res
         if (phase) phase[b] = psi < 0 ? 3.14159265358979323846f : 0.f;
     }
     if (d.Tp == 1) return;
-    // tangents
+    // tangents; a_k = s_k e^{l_k - l_max} once per walker
+    __shared__ double a_sh[8][128];
+    double* ak = a_sh[threadIdx.x >> 5];
+    for (int k = lane; k < K; k += 32) ak[k] = sg[k] * exp(ld[k] - lmax);
+    __syncwarp();
     const double* gb = g + (int64_t)b * K * n3;
     const double* gs = gb + (int64_t)ks * n3;
     double grad_sq = 0.0, gpsi_sq = 0.0;
     // lane-parallel over coordinates
     for (int t = lane; t < n3; t += 32) {
         double gp = 0.0;
-        for (int k = 0; k < K; ++k) gp += sg[k] * exp(ld[k] - lmax) * (gb[(int64_t)k * n3 + t] - gs[t]);
+        for (int k = 0; k < K; ++k) gp += ak[k] * (gb[(int64_t)k * n3 + t] - gs[t]);
         double gf = sgn * gp / (u + eps) + gs[t];
         double gl = 2.0 * gf + jb[1 + t];
         grad_sq += gl * gl;
@@ -446,10 +455,9 @@ __global__ void k_combine(const double* __restrict__ logdet, const double* __res
     // Laplacian of psi~
     double lp = 0.0;
     for (int k = lane; k < K; k += 32) {
-        double a = sg[k] * exp(ld[k] - lmax);
         double dg2 = 0.0;
         for (int t = 0; t < n3; ++t) { double dd = gb[(int64_t)k * n3 + t] - gs[t]; dg2 += dd * dd; }
-        lp += a * ((lapdet[(int64_t)b * K + k] - lapdet[(int64_t)b * K + ks]) + dg2);
+        lp += ak[k] * ((lapdet[(int64_t)b * K + k] - lapdet[(int64_t)b * K + ks]) + dg2);
     }
     grad_sq = warp_sum(grad_sq); gpsi_sq = warp_sum(gpsi_sq); lp = warp_sum(lp);
     double lapf = sgn * lp / (u + eps) - gpsi_sq / ((u + eps) * (u + eps)) + lapdet[(int64_t)b * K + ks];

@@ -14,6 +14,7 @@
 // (value, 3 gradients w.r.t. r_i, Laplacian w.r.t. r_i).
 #include "common.cuh"
 #include "net.cuh"
+#include <type_traits>
 
 namespace dw {
 
@@ -248,6 +249,46 @@ k_ei_streams(const float* __restrict__ r, const float* __restrict__ R, const flo
 // ------------------------------------------------------------------ spin means of h_one
 // M[(b*Tp + t), 0:hw] = mean over up electrons, [hw:2hw] = mean over down electrons
 // (SymmetricFeatures, ferminet_embedding.py:60-72). Row width mw (>= 2hw, zero padded).
+// Split-BF16 variant, 8 columns per thread with 16-byte hi / lo loads (hw % 8 == 0).
+__global__ void k_spin_means_split8(const Split* __restrict__ X, int ldx, int hw, Dims d, Split* __restrict__ M, int mw) {
+    const int b = blockIdx.x;
+    const int m8 = mw / 8;
+    for (int idx = threadIdx.x; idx < d.Tp * m8; idx += blockDim.x) {
+        const int t = idx / m8, col = (idx % m8) * 8;
+        float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (col < 2 * hw) {
+            const int f = col % hw;
+            const int i0 = col < hw ? 0 : d.nu, i1 = col < hw ? d.nu : d.n;
+            for (int i = i0; i < i1; ++i) {
+                const int64_t row = (int64_t)(b * d.n + i) * d.Tp + t;
+                const uint4 h = *reinterpret_cast<const uint4*>(X + row * 2 * ldx + f);
+                const uint4 l = *reinterpret_cast<const uint4*>(X + row * 2 * ldx + ldx + f);
+                const uint32_t hh[4] = {h.x, h.y, h.z, h.w}, ll[4] = {l.x, l.y, l.z, l.w};
+                #pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    v[2 * k] += __uint_as_float(hh[k] << 16) + __uint_as_float(ll[k] << 16);
+                    v[2 * k + 1] += __uint_as_float(hh[k] & 0xffff0000u) + __uint_as_float(ll[k] & 0xffff0000u);
+                }
+            }
+            const float inv = 1.f / (float)(i1 - i0);
+            #pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] *= inv;
+        }
+        const int64_t orow = (int64_t)b * d.Tp + t;
+        uint32_t hh[4], ll[4];
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * k]), h1 = __float2bfloat16_rn(v[2 * k + 1]);
+            __nv_bfloat16 l0 = __float2bfloat16_rn(v[2 * k] - __bfloat162float(h0));
+            __nv_bfloat16 l1 = __float2bfloat16_rn(v[2 * k + 1] - __bfloat162float(h1));
+            hh[k] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+            ll[k] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+        }
+        *reinterpret_cast<uint4*>(M + orow * 2 * mw + col) = make_uint4(hh[0], hh[1], hh[2], hh[3]);
+        *reinterpret_cast<uint4*>(M + orow * 2 * mw + mw + col) = make_uint4(ll[0], ll[1], ll[2], ll[3]);
+    }
+}
+
 template <class Act>
 __global__ void k_spin_means(const Act* __restrict__ X, int ldx, int hw, Dims d, Act* __restrict__ M, int mw) {
     int b = blockIdx.x;
@@ -444,8 +485,8 @@ k_conv_walker(const float* __restrict__ r, const float* __restrict__ WPl, const 
 // mo[b][k][t][i][o] = env[i,(k,o)] * bf[i,(k,o)] with tangents (envelope_orbitals.py:91-127).
 // env = sum_I w_I exp(-softplus(alpha_I) d_iI); grad/Laplacian w.r.t. r_i only.
 __global__ void k_envelope(const float* __restrict__ r, const float* __restrict__ R, const float* __restrict__ P,
-                           ParamLayout L, Dims d, int B, const float* __restrict__ BF, int ldbf,
-                           float* __restrict__ MO) {
+                           ParamLayout L, const float* __restrict__ spA, Dims d, int B, const float* __restrict__ BF,
+                           int ldbf, float* __restrict__ MO) {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)B * d.n * d.KN) return;
     int col = idx % d.KN;
@@ -453,14 +494,14 @@ __global__ void k_envelope(const float* __restrict__ r, const float* __restrict_
     int i = bi % d.n, b = bi / d.n;
     int k = col / d.n, o = col % d.n;
     bool up = i < d.nu;
-    const float* alpha = P + (up ? L.alpha_up : L.alpha_dn);
+    const float* spa = spA + (up ? 0 : d.N * d.KN);          // softplus(alpha), prepared
     const float* wts = P + (up ? L.weights_up : L.weights_dn);
     const float* ri = r + bi * 3;
     float env = 0.f, g[3] = {0.f, 0.f, 0.f}, lapv = 0.f;
     for (int I = 0; I < d.N; ++I) {
         float s0 = ri[0] - R[I * 3], s1 = ri[1] - R[I * 3 + 1], s2 = ri[2] - R[I * 3 + 2];
         float dd = sqrtf(s0 * s0 + s1 * s1 + s2 * s2);
-        float a = softplus_f(alpha[I * d.KN + col]);
+        float a = __ldg(spa + I * d.KN + col);
         float e = wts[I * d.KN + col] * expf(-a * dd);
         env += e;
         if (d.Tp > 1) {
@@ -531,6 +572,9 @@ void launch_streams(const float* r, const float* R, const float* P, const ParamL
 }
 template <class Act>
 void launch_spin_means(const Act* X, int ldx, int hw, const Dims& d, int B, Act* M, int mw, cudaStream_t s) {
+    if constexpr (std::is_same<Act, Split>::value) {
+        if (hw % 8 == 0) { k_spin_means_split8<<<B, 256, 0, s>>>(X, ldx, hw, d, M, mw); count_launch(); return; }
+    }
     k_spin_means<Act><<<B, 256, 0, s>>>(X, ldx, hw, d, M, mw); count_launch();
 }
 template <class Act>
@@ -551,10 +595,10 @@ void launch_conv(const float* r, const float* WPl, const float* HM, const float*
     }
     count_launch();
 }
-void launch_envelope(const float* r, const float* R, const float* P, const ParamLayout& L, const Dims& d, int B,
-                     const float* BF, int ldbf, float* MO, cudaStream_t s) {
+void launch_envelope(const float* r, const float* R, const float* P, const ParamLayout& L, const float* sp_alpha,
+                     const Dims& d, int B, const float* BF, int ldbf, float* MO, cudaStream_t s) {
     int64_t n = (int64_t)B * d.n * d.KN;
-    k_envelope<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, R, P, L, d, B, BF, ldbf, MO); count_launch();
+    k_envelope<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, R, P, L, sp_alpha, d, B, BF, ldbf, MO); count_launch();
 }
 template <class Act>
 void launch_jastrow_out(const Act* J2, int ldj, const float* w2, const Dims& d, int B, double* jas, cudaStream_t s) {

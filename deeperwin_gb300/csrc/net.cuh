@@ -47,8 +47,8 @@ template <class Act> void launch_spin_means(const Act* X, int ldx, int hw, const
 template <class Act> void launch_tanh_fl(const float* Zb, int ldz, int ncols, int groups, const Dims& d, Act* Y, int ldy, cudaStream_t s);
 template <class Act> void launch_conv(const float* r, const float* WPl, const float* HM, const float* HEl, const float* himl,
                                       const Dims& d, int l, int B, Act* X, int ldx, cudaStream_t s);
-void launch_envelope(const float* r, const float* R, const float* P, const ParamLayout& L, const Dims& d, int B,
-                     const float* BF, int ldbf, float* MO, cudaStream_t s);
+void launch_envelope(const float* r, const float* R, const float* P, const ParamLayout& L, const float* sp_alpha,
+                     const Dims& d, int B, const float* BF, int ldbf, float* MO, cudaStream_t s);
 template <class Act> void launch_jastrow_out(const Act* J2, int ldj, const float* w2, const Dims& d, int B, double* jas, cudaStream_t s);
 
 // gemm_simt.cu: C[m, n] = sum_k A[m, k] W[k, n] with epilogue.
@@ -85,7 +85,7 @@ void launch_slogdet_inv(const float* MO, const Dims& d, int B, double* logdet, d
 // backward.cu
 size_t bwd_bytes(const DwArch* a, int B, int* chunk);
 int backward_all(const DwArch* a, const float* P, const float* const main[4], const float* const mean[4],
-                 const float* bf_cat, const float* r, int B, const float* R, const int32_t* Z, const float* coeff,
-                 float* grad, void* ws, size_t wsb, cudaStream_t s);
+                 const float* bf_cat, const float* sp_alpha, const float* r, int B, const float* R, const int32_t* Z,
+                 const float* coeff, float* grad, void* ws, size_t wsb, cudaStream_t s);
 
 }  // namespace dw

@@ -58,6 +58,9 @@ _SIGS = {
     "dw_log_psi_sqr_backward": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P,
                                                _P, _P, _P, _P, ctypes.c_size_t, _P]),
     "dw_last_launch_count": (ctypes.c_int64, []),
+    "dw_log_psi_sqr_noalloc": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P, _P,
+                                              _P, _P, _P]),
+    "dw_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "dw_debug_gemm_bf16": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_int, _P]),
     "dw_debug_tc_error_flag": (ctypes.c_int, []),

@@ -401,6 +401,21 @@ static int forward_all(const DwArch* a, int precision, const float* P, const voi
     return DW_OK;
 }
 
+// Value-only forward for the workspace-free entry point (noalloc.cu): bytes of scratch it needs
+// and the call itself on a caller-supplied scratch region.
+size_t value_forward_bytes(const DwArch* a, int precision, int B) {
+    size_t out = 0;
+    with_act(precision, false, [&](auto tag) { out = plan_bytes<act_of<decltype(tag)>>(a, B, false); return 0; });
+    return out;
+}
+int value_forward(const DwArch* a, int precision, const float* params, const void* prepared, const float* r, int B,
+                  const float* R, const int32_t* Z, float* lp, float* phase, void* ws, size_t wsb, cudaStream_t s) {
+    return with_act(precision, true, [&](auto tag) {
+        using Act = act_of<decltype(tag)>;
+        return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s);
+    });
+}
+
 }  // namespace dw
 
 using namespace dw;

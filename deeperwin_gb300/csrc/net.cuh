@@ -82,6 +82,11 @@ void launch_coulomb(const float* r, int B, int n, const float* R, const int32_t*
 // FP64 Gauss-Jordan log|det| and inverse of the value-channel Slater matrices (any Dims mode).
 void launch_slogdet_inv(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, cudaStream_t s);
 
+// api.cu: value-only forward on caller-provided scratch
+size_t value_forward_bytes(const DwArch* a, int precision, int B);
+int value_forward(const DwArch* a, int precision, const float* params, const void* prepared, const float* r, int B,
+                  const float* R, const int32_t* Z, float* lp, float* phase, void* ws, size_t wsb, cudaStream_t s);
+
 // backward.cu
 size_t bwd_bytes(const DwArch* a, int B, int* chunk);
 int backward_all(const DwArch* a, const float* P, const float* const main[4], const float* const mean[4],

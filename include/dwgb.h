@@ -162,6 +162,22 @@ int dw_log_psi_sqr_backward(const DwArch* arch, int precision, const float* para
                             const float* coeff, float* grad_params,
                             void* workspace, size_t workspace_bytes, void* stream);
 
+/* log psi^2 and phase like dw_log_psi_sqr, but with no workspace argument and no device
+ * allocation anywhere: scratch comes from a fixed static device array of
+ * dw_noalloc_scratch_bytes() bytes (64 MiB) that every GPU loading the library reserves until
+ * process exit. For callers that cannot allocate device memory at call time (a host framework
+ * owning all device memory through its own pool, or a fixed-budget embedding). Calls that need
+ * more scratch than the array (too many walkers for the architecture) return
+ * DW_ERR_WORKSPACE. The first call on a device resolves the array's device address with
+ * cudaGetSymbolAddress; make that first call before any stream capture. All calls share the
+ * array and its contents persist between calls, so calls that overlap on the GPU (different
+ * streams, or concurrent host threads) race; serialize them. No counterpart in the reference. */
+int dw_log_psi_sqr_noalloc(const DwArch* arch, int precision, const float* params, const void* prepared,
+                           const float* r, int n_walkers, const float* R, const int32_t* Z,
+                           float* log_psi_sqr, float* phase, void* stream);
+/* Size in bytes of the static scratch array used by dw_log_psi_sqr_noalloc. */
+size_t dw_noalloc_scratch_bytes(void);
+
 /* Number of kernel launches issued by the last call on this host thread (instrumentation). */
 int64_t dw_last_launch_count(void);
 

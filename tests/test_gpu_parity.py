@@ -168,3 +168,30 @@ def test_energy_stats(cuda):
     assert out[0] == pytest.approx(xn.mean(), rel=1e-12)
     assert out[1] == pytest.approx(xn.var(), rel=1e-12)
     assert out[2] == len(xn)
+
+
+def _big_case(name):
+    if name == "c2h4_tp64":
+        mol, K, B = A.c2h4_shaped(), 2, 2
+    else:   # 34 electrons: four O and two H -> Tp = 128, n > 32 fallbacks
+        R = np.array([[0.0, 0, 0], [2.6, 0, 0], [0, 2.6, 0], [2.6, 2.6, 0], [1.3, 1.3, 2.2], [1.3, 1.3, -2.2]])
+        mol = A.Molecule(R=R, Z=np.array([8, 8, 8, 8, 1, 1]), n_el=34, n_up=17, name="O4H2")
+        K, B = 1, 1
+    a = A.arch_for(mol, K)
+    p = P.init_params(a, 4, bias_std=0.1, envelope_jitter=0.2)
+    r = A.init_walkers(mol, B, seed=13)
+    E, lp, g, lap = O.local_energy(O.tparams(p), a, r, mol.R, mol.Z)
+    S = 0.25 * np.abs(lap.numpy()) + 0.125 * (g.numpy() ** 2).sum(-1) + np.abs(O.potential_energy(r, mol.R, mol.Z).numpy())
+    return mol, a, p, r, E.numpy(), lp.numpy(), S
+
+
+@pytest.mark.parametrize("name", ["c2h4_tp64", "o4h2_tp128"])
+def test_local_energy_many_channels(cuda, name):
+    """Electron counts whose channel groups span two (Tp = 64) or four (Tp = 128) epilogue warps."""
+    mol, a, p, r, E_ref, lp_ref, S = _big_case(name)
+    for prec, tol in (("fp32", 5e-5), ("mixed", 1e-4)):
+        params = api.Params.from_dict(a, p, prec)
+        E, lp, _ = api.local_energy(params, (a.n_up, a.n_dn), r, mol.R, mol.Z, return_grad=True)
+        E = E.cpu().numpy().astype(np.float64)
+        assert np.all(np.abs(E - E_ref) <= tol * S), (prec, E, E_ref, S)
+        np.testing.assert_allclose(lp.cpu().numpy(), lp_ref, rtol=1e-4, atol=1e-3)

@@ -52,6 +52,13 @@ _SIGS = {
     "dw_potential_energy": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int, _P, _P]),
     "dw_mcmc_steps": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P,
                                      _P, ctypes.POINTER(DwMcmcConfig), _P, ctypes.c_size_t, _P]),
+    "dw_log_psi_sqr_packed": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P, _P,
+                                             ctypes.c_int, _P, _P, _P, _P, ctypes.c_size_t, _P]),
+    "dw_local_energy_packed": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P, _P,
+                                              ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
+    "dw_mcmc_steps_packed": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P, _P,
+                                            ctypes.c_int, _P, _P, _P, _P, _P, _P, ctypes.POINTER(DwMcmcConfig), _P,
+                                            ctypes.c_size_t, _P]),
     "dw_energy_stats": (ctypes.c_int, [_P, ctypes.c_int, _P, _P]),
     "dw_clip_energies": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P, _P,
                                         _P]),

@@ -160,7 +160,7 @@ static Plan<Act> carve_plan(const Dims& d, int Bc, void* ws) {
     int mw = 0;
     for (int l = 0; l < 4; ++l) mw = std::max(mw, mean_width(d, l));
     int zw = std::max(std::max(d.D, d.J0), d.KN);
-    p.him = c.take<float>(4 * d.N * 32);
+    p.him = c.take<float>((size_t)kMaxSeg * 4 * d.N * 32);   // [segment][iteration][ion][32]
     p.X0 = c.take<Act>(np * rows * d.kw[0]);
     p.XA = c.take<Act>(np * rows * kXW);
     p.XB = c.take<Act>(np * rows * kXW);
@@ -250,9 +250,10 @@ template <class Act> static inline int64_t act_off(int64_t row, int ld) { return
 // The forward (value or tangent) of one chunk of walkers.
 template <class Act>
 static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, const ParamLayout& L,
-                     const Prepared& pre, const float* r, const float* R, const int32_t* Z,
+                     const Prepared& pre, const float* r, const float* R, const int32_t* Z, const int32_t* seg,
                      float* lp, float* phase, float* E_loc, float* grad, cudaStream_t s) {
-    const Dims& d = p.d;
+    Dims d = p.d;
+    d.seg = seg;          // walker -> geometry segment of this chunk (null: one geometry)
     const int rows = Bc * d.n * d.Tp;
     const bool tang = d.Tp > 1;
     const int pt = tc_parts(precision);
@@ -268,8 +269,8 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         if (pt >= 2) w.lo = bf[1];
         return w;
     };
-    DW_TIMED("features", launch_features<Act>(r, R, d, Bc, p.X0, s));
-    DW_TIMED("streams", launch_streams(r, R, P, L, d, Bc, p.WP, p.HE, s));
+    DW_TIMED("features", launch_features<Act>(r, R, Z, d, Bc, p.X0, s));
+    DW_TIMED("streams", launch_streams(r, R, Z, P, L, d, Bc, p.WP, p.HE, s));
     Act* xin = p.X0;
     int ldin = d.kw[0];
     int pc = tang ? 3 : 1, ec = tang ? 5 : 1;
@@ -318,7 +319,7 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         if (pt >= 2) wb.lo = pre.bf_bf[1];
         DW_TIMED("backflow_gemm", DW_CHECK(MM<Act>::mm(H, kXW, wb, p.BF, 2 * d.KN, rows, 2 * d.KN, d.D, e0, s)));
     }
-    DW_TIMED("envelope", launch_envelope(r, R, P, L, pre.sp_alpha, d, Bc, p.BF, 2 * d.KN, p.MO, s));
+    DW_TIMED("envelope", launch_envelope(r, R, Z, P, L, pre.sp_alpha, d, Bc, p.BF, 2 * d.KN, p.MO, s));
     if (precision == DW_PRECISION_FP32) DW_TIMED("slogdet", launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
     else DW_TIMED("slogdet", launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
     if (tang) DW_TIMED("det_tangents", launch_det_tangents(p.MO, p.Ainv, p.sign, d, Bc, p.g, p.lapdet, s));
@@ -370,7 +371,7 @@ static size_t ws_bytes_t(const DwArch* a, int n_walkers, int mode) {
         size_t b = plan_bytes<Act>(a, n_walkers, false);
         b += (size_t)n_walkers * a->n_el * 3 * sizeof(float) + 256;      // proposals
         b += (size_t)n_walkers * sizeof(float) + 256;                    // proposal log psi^2
-        b += (size_t)mh_partials_needed(n_walkers) * sizeof(int) + 256;
+        b += (size_t)mh_counts_needed(kMaxSeg) * sizeof(int) + 256;
         return b;
     }
     size_t b = plan_bytes<Act>(a, n_walkers, mode == 1);
@@ -381,8 +382,9 @@ static size_t ws_bytes_t(const DwArch* a, int n_walkers, int mode) {
 template <class Act>
 static int forward_all(const DwArch* a, int precision, const float* P, const void* prepared, const float* r, int B,
                        const float* R, const int32_t* Z, float* lp, float* phase, float* E, float* grad, bool tang,
-                       void* ws, size_t ws_bytes, cudaStream_t s) {
+                       void* ws, size_t ws_bytes, cudaStream_t s, const int32_t* seg = nullptr, int nseg = 1) {
     Dims d = make_dims(a, tang);
+    if (nseg < 1 || nseg > kMaxSeg || (nseg > 1 && !seg)) return DW_ERR_ARG;
     // the fused forward-Laplacian epilogue keeps one electron's channels inside a 128-row tile
     if (tang && !std::is_same<Act, float>::value && d.Tp > 128) return DW_ERR_ARCH;
     ParamLayout L;
@@ -391,10 +393,13 @@ static int forward_all(const DwArch* a, int precision, const float* P, const voi
     int bc = choose_chunk<Act>(d, B);
     Plan<Act> p = carve_plan<Act>(d, bc, ws);
     if (p.bytes > ws_bytes) return DW_ERR_WORKSPACE;
+    d.nseg = nseg;
+    p.d.nseg = nseg;      // the chunks index geometries through the plan's dims
     launch_ion_maps(P, L, d, Z, p.him, s);
     for (int b0 = 0; b0 < B; b0 += bc) {
         int nb = std::min(bc, B - b0);
-        DW_CHECK(run_chunk<Act>(p, nb, precision, P, L, pre, r + (int64_t)b0 * d.n * 3, R, Z, lp + b0,
+        DW_CHECK(run_chunk<Act>(p, nb, precision, P, L, pre, r + (int64_t)b0 * d.n * 3, R, Z, seg ? seg + b0 : nullptr,
+                                lp + b0,
                                 phase ? phase + b0 : nullptr, E ? E + b0 : nullptr,
                                 grad ? grad + (int64_t)b0 * 3 * d.n : nullptr, s));
     }
@@ -482,14 +487,16 @@ int dw_potential_energy(const float* r, int B, int n, const float* R, const int3
     return DW_OK;
 }
 
-int dw_mcmc_steps(const DwArch* a, int precision, const float* params, const void* prepared, float* r, int B,
-                  const float* R, const int32_t* Z, float* lp, int32_t* age, DwMcmcScalars* scalars,
-                  const DwMcmcConfig* cfg, void* ws, size_t wsb, void* stream) {
-    reset_launch_count();
-    DW_CHECK(check_arch(a));
-    if (!params || !prepared || !r || !R || !Z || !lp || !age || !scalars || !cfg || B <= 0) return DW_ERR_ARG;
-    if (cfg->n_steps < 0) return DW_ERR_ARG;
-    cudaStream_t s = (cudaStream_t)stream;
+}  // extern "C"
+
+namespace dw {
+
+// Metropolis-Hastings chains (mcmc.py:390-396 run_mcmc_steps): optional re-evaluation of log psi^2
+// at the current walkers, then n_steps x (forward at the proposals, accept / propose).
+static int mcmc_impl(const DwArch* a, int precision, const float* params, const void* prepared, float* r, int B,
+                     const float* R, const int32_t* Z, int nseg, const int32_t* seg, const int32_t* widx,
+                     const uint64_t* seeds, float* lp, int32_t* age, DwMcmcScalars* scalars, const DwMcmcConfig* cfg,
+                     void* ws, size_t wsb, cudaStream_t s) {
     return with_act(precision, true, [&](auto tag) {
         using Act = act_of<decltype(tag)>;
         if (wsb < ws_bytes_t<Act>(a, B, 2)) return (int)DW_ERR_WORKSPACE;
@@ -497,20 +504,22 @@ int dw_mcmc_steps(const DwArch* a, int precision, const float* params, const voi
         Carver c(static_cast<char*>(ws) + fwd, wsb - fwd);
         float* r_prop = c.take<float>((size_t)B * a->n_el * 3);
         float* lp_prop = c.take<float>((size_t)B);
-        int* partials = c.take<int>((size_t)mh_partials_needed(B));
+        int* counts = c.take<int>((size_t)mh_counts_needed(kMaxSeg));
         if (!c.ok()) return (int)DW_ERR_WORKSPACE;
         auto fwd_call = [&](const float* rr, float* out) {
             return forward_all<Act>(a, precision, params, prepared, rr, B, R, Z, out, nullptr, nullptr, nullptr, false,
-                                    ws, fwd, s);
+                                    ws, fwd, s, seg, nseg);
         };
         int64_t launches = 0;
         if (cfg->reevaluate) { DW_CHECK(fwd_call(r, lp)); launches += launch_count(); }   // mcmc.py:396
-        if (cfg->n_steps == 0) return (int)DW_OK;
+        if (cfg->n_steps == 0) { reset_launch_count(); count_launch((int)launches); return (int)DW_OK; }
+        DW_CHECK_CUDA(cudaMemsetAsync(counts, 0, (size_t)mh_counts_needed(nseg) * sizeof(int), s));
         MhArgs m;
         m.r = r; m.r_prop = r_prop; m.lp = lp; m.lp_prop = lp_prop; m.age = age; m.scalars = scalars;
-        m.partials = partials; m.B = B; m.n = a->n_el; m.max_age = cfg->max_age;
+        m.counts = counts; m.B = B; m.n = a->n_el; m.max_age = cfg->max_age;
         m.interval = cfg->stepsize_update_interval; m.target = cfg->target_acceptance_rate;
         m.min_step = cfg->min_stepsize; m.max_step = cfg->max_stepsize; m.seed = cfg->seed;
+        m.seg = seg; m.widx = widx; m.seeds = seeds; m.nseg = nseg;
         reset_launch_count();
         DW_TIMED("mh", launch_mh(m, 0, s));
         launches += launch_count();
@@ -524,6 +533,73 @@ int dw_mcmc_steps(const DwArch* a, int precision, const float* params, const voi
         count_launch((int)launches);
         DW_CHECK_CUDA(cudaGetLastError());
         return (int)DW_OK;
+    });
+}
+
+}  // namespace dw
+
+extern "C" {
+
+int dw_mcmc_steps(const DwArch* a, int precision, const float* params, const void* prepared, float* r, int B,
+                  const float* R, const int32_t* Z, float* lp, int32_t* age, DwMcmcScalars* scalars,
+                  const DwMcmcConfig* cfg, void* ws, size_t wsb, void* stream) {
+    reset_launch_count();
+    DW_CHECK(check_arch(a));
+    if (!params || !prepared || !r || !R || !Z || !lp || !age || !scalars || !cfg || B <= 0) return DW_ERR_ARG;
+    if (cfg->n_steps < 0) return DW_ERR_ARG;
+    return mcmc_impl(a, precision, params, prepared, r, B, R, Z, 1, nullptr, nullptr, nullptr, lp, age, scalars, cfg,
+                     ws, wsb, (cudaStream_t)stream);
+}
+
+int dw_mcmc_steps_packed(const DwArch* a, int precision, const float* params, const void* prepared, float* r, int B,
+                         const float* R, const int32_t* Z, int nseg, const int32_t* seg, const int32_t* walker_index,
+                         const uint64_t* seeds, float* lp, int32_t* age, DwMcmcScalars* scalars,
+                         const DwMcmcConfig* cfg, void* ws, size_t wsb, void* stream) {
+    reset_launch_count();
+    DW_CHECK(check_arch(a));
+    if (!params || !prepared || !r || !R || !Z || !seg || !walker_index || !seeds || !lp || !age || !scalars || !cfg ||
+        B <= 0)
+        return DW_ERR_ARG;
+    if (cfg->n_steps < 0 || nseg < 1 || nseg > kMaxSeg) return DW_ERR_ARG;
+    return mcmc_impl(a, precision, params, prepared, r, B, R, Z, nseg, seg, walker_index, seeds, lp, age, scalars, cfg,
+                     ws, wsb, (cudaStream_t)stream);
+}
+
+int dw_log_psi_sqr_packed(const DwArch* a, int precision, const float* params, const void* prepared, const float* r,
+                          int B, const float* R, const int32_t* Z, int nseg, const int32_t* seg, float* lp,
+                          float* phase, void* ws, size_t wsb, void* stream) {
+    reset_launch_count();
+    DW_CHECK(check_arch(a));
+    if (!params || !prepared || !r || !R || !Z || !seg || !lp || B <= 0 || nseg < 1 || nseg > kMaxSeg)
+        return DW_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    return with_act(precision, true, [&](auto tag) {
+        using Act = act_of<decltype(tag)>;
+        return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s,
+                                seg, nseg);
+    });
+}
+
+int dw_local_energy_packed(const DwArch* a, int precision, const float* params, const void* prepared, const float* r,
+                           int B, const float* R, const int32_t* Z, int nseg, const int32_t* seg, float* E, float* lp,
+                           float* grad, void* ws, size_t wsb, void* stream) {
+    reset_launch_count();
+    DW_CHECK(check_arch(a));
+    if (!params || !prepared || !r || !R || !Z || !seg || !E || B <= 0 || nseg < 1 || nseg > kMaxSeg)
+        return DW_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    return with_act(precision, true, [&](auto tag) {
+        using Act = act_of<decltype(tag)>;
+        size_t pb = plan_bytes<Act>(a, B, true);
+        float* lpo = lp;
+        size_t fwd_bytes = wsb;
+        if (!lpo) {
+            if (pb + (size_t)B * sizeof(float) > wsb) return (int)DW_ERR_WORKSPACE;
+            lpo = reinterpret_cast<float*>(static_cast<char*>(ws) + pb);
+            fwd_bytes = pb;
+        }
+        return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, fwd_bytes, s,
+                                seg, nseg);
     });
 }
 

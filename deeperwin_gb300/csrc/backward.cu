@@ -436,8 +436,8 @@ static int backward_chunk(const Bwd& w, int Bc, const float* P, const ParamLayou
     const int64_t npair = (int64_t)Bc * npw, nei = (int64_t)Bc * d.n * d.N;
     // ---------------- forward with stored activations (value only, FP32)
     launch_ion_maps(P, L, d, Z, w.him, s);
-    launch_features<float>(r, R, d, Bc, w.X[0], s);
-    launch_streams(r, R, P, L, d, Bc, w.WP, w.HE, s, w.HP);
+    launch_features<float>(r, R, Z, d, Bc, w.X[0], s);
+    launch_streams(r, R, Z, P, L, d, Bc, w.WP, w.HE, s, w.HP);
     for (int l = 0; l < 4; ++l) {
         const int hw = d.hw[l], mw = mean_w(d, l);
         launch_spin_means<float>(w.X[l], d.kw[l], hw, d, Bc, w.Mc[l], mw, s);
@@ -454,7 +454,7 @@ static int backward_chunk(const Bwd& w, int Bc, const float* P, const ParamLayou
     }
     GemmEpi e0;
     gemm_f32(w.H4, d.D, bf_cat, 2 * d.KN, w.BF, 2 * d.KN, rows, 2 * d.KN, d.D, e0, 1, 0, 0, s);
-    launch_envelope(r, R, P, L, spA, d, Bc, w.BF, 2 * d.KN, w.MO, s);
+    launch_envelope(r, R, Z, P, L, spA, d, Bc, w.BF, 2 * d.KN, w.MO, s);
     launch_slogdet_inv(w.MO, d, Bc, w.logdet, w.sign, w.Ainv, s);
     GemmEpi j0; j0.bias = P + L.jas_b[0]; j0.act = 1;
     GemmEpi j1; j1.bias = P + L.jas_b[1]; j1.act = 1;

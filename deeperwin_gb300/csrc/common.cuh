@@ -61,7 +61,18 @@ struct Dims {
     int T;         // channels: 1 (value) or 3n + 2 (value, 3n gradients, Laplacian)
     int Tp;        // padded channel count (power of two >= T)
     int lap;       // index of the Laplacian channel (T-1) or -1
+    // Packed launches: walker b of this launch belongs to geometry segment seg[b] (R, Z and the
+    // ion maps are per segment; ions with Z = 0 are padding and contribute nothing).
+    // seg == nullptr: one geometry for all walkers.
+    const int32_t* seg;
+    int nseg;
 };
+
+constexpr int kMaxSeg = 256;     // geometries per packed launch
+// Out-of-range segment indices are clamped so that a bad index cannot read outside the
+// geometry arrays; the host wrappers validate seg before the launch.
+__host__ __device__ __forceinline__ int clamp_seg(int s, int nseg) { return s < 0 ? 0 : (s >= nseg ? nseg - 1 : s); }
+__host__ __device__ __forceinline__ int seg_of(const Dims& d, int64_t b) { return d.seg ? clamp_seg(d.seg[b], d.nseg) : 0; }
 
 inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
 inline int next_pow2(int x) { int p = 1; while (p < x) p <<= 1; return p; }

@@ -382,12 +382,13 @@ __device__ double coulomb_walker(const float* rb, int n, const float* R, const i
     }
     for (int p = lane; p < n * N; p += 32) {
         int i = p / N, I = p % N;
+        if (Z[I] <= 0) continue;                                  // padding ion
         double dx = rb[i * 3] - R[I * 3], dy = rb[i * 3 + 1] - R[I * 3 + 1], dz = rb[i * 3 + 2] - R[I * 3 + 2];
         e -= (double)Z[I] / sqrt(dx * dx + dy * dy + dz * dz);
     }
     for (int p = lane; p < N * N; p += 32) {
         int I = p / N, J = p % N;
-        if (J <= I) continue;
+        if (J <= I || Z[I] <= 0 || Z[J] <= 0) continue;
         double dx = R[J * 3] - R[I * 3], dy = R[J * 3 + 1] - R[I * 3 + 1], dz = R[J * 3 + 2] - R[I * 3 + 2];
         e += (double)Z[I] * Z[J] / sqrt(dx * dx + dy * dy + dz * dz);
     }
@@ -463,7 +464,8 @@ __global__ void k_combine(const double* __restrict__ logdet, const double* __res
     double lapf = sgn * lp / (u + eps) - gpsi_sq / ((u + eps) * (u + eps)) + lapdet[(int64_t)b * K + ks];
     double lap = 2.0 * lapf + jb[d.lap];
     double ekin = -0.5 * (0.5 * lap + 0.25 * grad_sq);
-    double epot = coulomb_walker(r + (int64_t)b * d.n * 3, d.n, R, Z, d.N, lane);
+    const int gs_ = seg_of(d, b);
+    double epot = coulomb_walker(r + (int64_t)b * d.n * 3, d.n, R + (size_t)gs_ * d.N * 3, Z + (size_t)gs_ * d.N, d.N, lane);
     if (lane == 0) E_loc[b] = (float)(ekin + epot);
 }
 

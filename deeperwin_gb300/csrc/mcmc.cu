@@ -28,25 +28,28 @@ __device__ __forceinline__ float next_stepsize(float s, double acc_rate_prev, in
 }
 
 // phase 0: propose only (r_prop = r + s N); phase 1: accept proposal, then propose the next;
-// phase 2: accept only. One warp per walker.
+// phase 2: accept only. One warp per walker; each walker follows the scalars of its chain.
 __global__ void k_mh(MhArgs a, int phase) {
-    __shared__ int blk_acc[32];
+    __shared__ int blk_seg[32], blk_acc[32];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
     const int w = blockIdx.x * wpb + wid;
     const int n3 = 3 * a.n;
-    DwMcmcScalars* S = a.scalars;
-    const double acc_rate = S->acc_rate;
-    const float step = S->stepsize;
-    const int step_nr = S->step_nr;
-    int accepted = 0;
+    int accepted = 0, sg = -1;
     if (w < a.B) {
+        sg = a.seg ? clamp_seg(a.seg[w], a.nseg) : 0;
+        const DwMcmcScalars* S = a.scalars + sg;
+        const double acc_rate = S->acc_rate;
+        const float step = S->stepsize;
+        const int step_nr = S->step_nr;
+        const uint64_t key = a.seeds ? a.seeds[sg] : a.seed;
+        const uint32_t wk = a.widx ? (uint32_t)a.widx[w] : (uint32_t)w;
         float* rw = a.r + (int64_t)w * n3;
         float* pw = a.r_prop + (int64_t)w * n3;
         float s_prop = step;
         int nr_prop = step_nr;
         if (phase >= 1) {
             float lp = a.lp[w], lpn = a.lp_prop[w];
-            float U = uniform1(a.seed, (uint32_t)w, (uint32_t)step_nr);
+            float U = uniform1(key, wk, (uint32_t)step_nr);
             bool acc = expf(lpn - lp) > U;          // mcmc.py:359-362
             int age = a.age[w];
             acc = acc || (age >= a.max_age);        // mcmc.py:363
@@ -63,7 +66,7 @@ __global__ void k_mh(MhArgs a, int phase) {
         if (phase <= 1) {
             for (int g = lane; g * 4 < n3; g += 32) {
                 float z[4];
-                normals4(a.seed, (uint32_t)w, (uint32_t)nr_prop, (uint32_t)g, z);
+                normals4(key, wk, (uint32_t)nr_prop, (uint32_t)g, z);
                 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
                     int q = g * 4 + c;
@@ -73,25 +76,36 @@ __global__ void k_mh(MhArgs a, int phase) {
         }
     }
     if (phase == 0) return;
-    // FP64 all-walker mean acceptance: block partials, the last block reduces in fixed order.
-    if (lane == 0) blk_acc[wid] = accepted;
+    // Integer accept / walker counts per chain (runs of equal chain within the block merged),
+    // then the last block turns them into FP64 acceptance rates and the next step sizes.
+    if (lane == 0) { blk_seg[wid] = sg; blk_acc[wid] = accepted; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        int sacc = 0;
-        for (int k = 0; k < wpb; ++k) sacc += blk_acc[k];
-        a.partials[blockIdx.x] = sacc;
+        int k = 0;
+        while (k < wpb) {
+            const int cs = blk_seg[k];
+            int acc = 0, cnt = 0;
+            for (; k < wpb && blk_seg[k] == cs; ++k) { acc += blk_acc[k]; ++cnt; }
+            if (cs >= 0) { atomicAdd(a.counts + 2 * cs, acc); atomicAdd(a.counts + 2 * cs + 1, cnt); }
+        }
         __threadfence();
-        unsigned t = atomicAdd(&S->ticket, 1u);
+        unsigned t = atomicAdd(&a.scalars[0].ticket, 1u);
         if (t == gridDim.x - 1) {
             __threadfence();
-            long long tot = 0;
-            for (unsigned k = 0; k < gridDim.x; ++k) tot += ((volatile int*)a.partials)[k];
-            double mean = (double)tot / (double)a.B;
-            S->last_acc = mean;
-            S->acc_rate = 0.9 * acc_rate + 0.1 * mean;      // mcmc.py:371
-            S->stepsize = next_stepsize(step, acc_rate, step_nr + 1, a);
-            S->step_nr = step_nr + 1;
-            S->ticket = 0u;
+            for (int c = 0; c < a.nseg; ++c) {
+                volatile int* cc = a.counts + 2 * c;
+                const int acc = cc[0], cnt = cc[1];
+                cc[0] = 0; cc[1] = 0;
+                if (cnt == 0) continue;              // chain not in this launch
+                DwMcmcScalars* S = a.scalars + c;
+                const double prev = S->acc_rate;
+                const double mean = (double)acc / (double)cnt;
+                S->last_acc = mean;
+                S->acc_rate = 0.9 * prev + 0.1 * mean;      // mcmc.py:371
+                S->stepsize = next_stepsize(S->stepsize, prev, S->step_nr + 1, a);
+                S->step_nr = S->step_nr + 1;
+            }
+            a.scalars[0].ticket = 0u;
             __threadfence();
         }
     }
@@ -103,7 +117,7 @@ void launch_mh(const MhArgs& a, int phase, cudaStream_t s) {
     k_mh<<<blocks, wpb * 32, 0, s>>>(a, phase);
     count_launch();
 }
-int mh_partials_needed(int B) { return (B + 7) / 8; }
+int mh_counts_needed(int nseg) { return 2 * nseg; }
 
 // ------------------------------------------------------------------ FP64 statistics
 struct Welford { double n, mean, m2; };

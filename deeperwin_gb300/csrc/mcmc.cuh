@@ -9,16 +9,22 @@ struct MhArgs {
     float* lp;             // [B] current log psi^2
     const float* lp_prop;  // [B] log psi^2 of the proposals
     int32_t* age;          // [B]
-    DwMcmcScalars* scalars;
-    int* partials;         // [blocks] block accept counts
+    DwMcmcScalars* scalars;  // [nseg] chain scalars (step size, acceptance, step counter) per segment
+    int* counts;           // [2 * nseg] accepted / walker counts of the running step (zero between steps)
     int B, n;
     int max_age, interval;
     float target, min_step, max_step;
     uint64_t seed;
+    // Packed chains: walker b belongs to chain seg[b], draws its random numbers as walker
+    // widx[b] of that chain, keyed by seeds[seg[b]]. All null: one chain, walker b, key `seed`.
+    const int32_t* seg;
+    const int32_t* widx;
+    const uint64_t* seeds;
+    int nseg;
 };
 
 void launch_mh(const MhArgs& a, int phase, cudaStream_t s);
-int mh_partials_needed(int B);
+int mh_counts_needed(int nseg);
 void launch_stats(const float* E, int n, int clip, double c, double w, double cb, float* Ec, double* out, cudaStream_t s);
 
 }  // namespace dw

@@ -129,6 +129,8 @@ Dims make_dims(const DwArch* a, bool tangents) {
     } else {
         d.T = 1; d.Tp = 1; d.lap = -1;
     }
+    d.seg = nullptr;
+    d.nseg = 1;
     return d;
 }
 

@@ -23,11 +23,14 @@ namespace dw {
 // input_features.py:184-191)
 __global__ void k_ion_maps(const float* __restrict__ P, ParamLayout L, Dims d, const int32_t* __restrict__ Z,
                            float* __restrict__ him) {
-    for (int idx = threadIdx.x; idx < 4 * d.N * 32; idx += blockDim.x) {
-        int l = idx / (d.N * 32), rem = idx % (d.N * 32), I = rem / 32, f = rem % 32;
+    // him[seg][l][I][f]; padding ions (Z = 0) map to 0 so they drop out of conv_ei
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < d.nseg * 4 * d.N * 32; idx += gridDim.x * blockDim.x) {
+        const int sg = idx / (4 * d.N * 32), li = idx % (4 * d.N * 32);
+        int l = li / (d.N * 32), rem = li % (d.N * 32), I = rem / 32, f = rem % 32;
         float v = 0.f;
-        if (f < d.eiw[l]) {
-            int z = Z[I] - d.zmin;
+        const int zI = Z[sg * d.N + I];
+        if (f < d.eiw[l] && zI > 0) {
+            int z = zI - d.zmin;
             z = z < 0 ? 0 : (z > d.zmax - d.zmin ? d.zmax - d.zmin : z);
             const float* emb = P + L.ion_embed + (int64_t)z * d.EI;
             const float* W = P + L.h_ion_map_w[l];
@@ -43,10 +46,13 @@ __global__ void k_ion_maps(const float* __restrict__ P, ParamLayout L, Dims d, c
 // X0[(b,i,t), 4I + q] = [d_iI, (r_i - R_I)_{x,y,z}] with tangents (input_features.py:51-68, :237-239).
 // Also zero-fills the padding columns of the layer-0 input.
 template <class Act>
-__global__ void k_features(const float* __restrict__ r, const float* __restrict__ R, Dims d, int B,
-                           Act* __restrict__ X0) {
+__global__ void k_features(const float* __restrict__ r, const float* __restrict__ Rall, const int32_t* __restrict__ Zall,
+                           Dims d, int B, Act* __restrict__ X0) {
     int bi = blockIdx.x;          // b * n + i
     int i = bi % d.n;
+    const int sg = seg_of(d, bi / d.n);
+    const float* R = Rall + (size_t)sg * d.N * 3;
+    const int32_t* Z = Zall + (size_t)sg * d.N;
     const float* ri = r + (int64_t)bi * 3;
     int width = d.kw[0];
     int nf = 4 * d.N;
@@ -55,7 +61,7 @@ __global__ void k_features(const float* __restrict__ r, const float* __restrict_
         int t = idx / width, col = idx % width;
         if (col >= nf && col < nf + d.E + 4) continue;   // conv columns written by k_conv
         float v = 0.f;
-        if (col < nf) {
+        if (col < nf && Z[col >> 2] > 0) {
             int I = col >> 2, q = col & 3;
             float sx = ri[0] - R[I * 3 + 0], sy = ri[1] - R[I * 3 + 1], sz = ri[2] - R[I * 3 + 2];
             float dd = sqrtf(sx * sx + sy * sy + sz * sz);
@@ -209,8 +215,8 @@ k_pair_streams(const float* __restrict__ r, const float* __restrict__ P, ParamLa
 
 template <int CH>
 __global__ void __launch_bounds__(128)
-k_ei_streams(const float* __restrict__ r, const float* __restrict__ R, const float* __restrict__ P, ParamLayout L,
-             Dims d, int B, float* __restrict__ HE) {
+k_ei_streams(const float* __restrict__ r, const float* __restrict__ R, const int32_t* __restrict__ Z,
+             const float* __restrict__ P, ParamLayout L, Dims d, int B, float* __restrict__ HE) {
     extern __shared__ float srow[];
     float* row = srow + threadIdx.x * (CH * 32 + 1);
     const int nei = d.n * d.N;
@@ -219,6 +225,16 @@ k_ei_streams(const float* __restrict__ r, const float* __restrict__ R, const flo
     const int b = (int)(gid / nei), p = (int)(gid % nei);
     const int i = p / d.N, I = p % d.N;
     const float* ri = r + ((int64_t)b * d.n + i) * 3;
+    const int sg = seg_of(d, b);
+    R += (size_t)sg * d.N * 3;
+    const int64_t plane = (int64_t)B * nei;
+    if (Z[sg * d.N + I] <= 0) {       // padding ion: zero stream (its ion map is zero as well)
+        for (int l = 0; l < 4; ++l) {
+            float4* o = reinterpret_cast<float4*>(HE + ((int64_t)l * plane + (int64_t)b * nei + p) * CH * 32);
+            for (int k = 0; k < CH * 8; ++k) o[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        return;
+    }
     const float s[3] = {ri[0] - R[I * 3], ri[1] - R[I * 3 + 1], ri[2] - R[I * 3 + 2]};
     const float dd = sqrtf(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
     float h[CH][32];
@@ -233,7 +249,6 @@ k_ei_streams(const float* __restrict__ r, const float* __restrict__ R, const flo
         for (int c = 0; c < 3; ++c) { h[1 + c][0] = s[c] / dd; h[1 + c][1 + c] = 1.f; }
         h[4][0] = 2.f / dd;
     }
-    const int64_t plane = (int64_t)B * nei;
     for (int l = 0; l < 4; ++l) {
         float* o = HE + ((int64_t)l * plane + (int64_t)b * nei + p) * CH * 32;
         #pragma unroll
@@ -393,11 +408,154 @@ __global__ void k_conv(const float* __restrict__ r, const float* __restrict__ WP
                 else if (t >= 1 + 3 * i && t < 4 + 3 * i) ch = t - 3 * i;
                 if (ch >= 0) {
                     const float* he = HEl + ((int64_t)b * d.n * d.N + (int64_t)i * d.N) * ech * 32;
-                    for (int I = 0; I < d.N; ++I) v += he[(I * ech + ch) * 32 + f] * himl[I * 32 + f];
+                    const float* hs = himl + (size_t)seg_of(d, b) * 4 * d.N * 32;
+                    for (int I = 0; I < d.N; ++I) v += he[(I * ech + ch) * 32 + f] * hs[I * 32 + f];
                 }
             }
         }
         ActIO<Act>::store(X, (int64_t)bi * d.Tp + t, ldx, hw + col, v);
+    }
+}
+
+// Register-tiled tangent convolution. Block = (walker, tile of TI = 4 electrons i) with
+// NW = Tp / TT warps; lane = feature f, warp w owns channels [w TT, w TT + TT). The main loop
+// loads w_ij (4 rows) and h_j (TT channels) once per j and issues 4 TT FMAs. The results are
+// staged in shared memory, where the product-rule terms are added with per-(i, j) items spread
+// over the warps: single terms w'_im u_im h_m for the channels of the other electrons m, the
+// j-sums of the electron's own gradient channels and of the Laplacian. Columns are then written
+// eight at a time (16-byte stores). conv_ei is non-zero on 5 channels per electron only. Same
+// mathematics as k_conv.
+template <class Act, int TT>
+__global__ void __launch_bounds__(512)
+k_conv_tile(const float* __restrict__ r, const float* __restrict__ WPl, const float* __restrict__ HM,
+            const float* __restrict__ HEl, const float* __restrict__ himl, Dims d, int l, int B, Act* __restrict__ X,
+            int ldx) {
+    constexpr int TI = 4;
+    extern __shared__ __align__(16) float smc[];
+    const int n = d.n, Tp = d.Tp, T = d.T;
+    const int NW = Tp / TT;
+    float* out = smc;                                   // [TI][Tp][32] conv_ee
+    float* red = out + TI * Tp * 32;                    // [NW][TI][4][32] own-gradient / Laplacian partials
+    float* eiv = red + NW * TI * 4 * 32;                // [TI][5][32] conv_ei channels
+    const int f = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int ntile = (n + TI - 1) / TI;
+    const int b = blockIdx.x / ntile, i0 = (blockIdx.x % ntile) * TI;
+    const int ni = min(TI, n - i0);
+    const int hw = d.hw[l], E = d.E, eiw = d.eiw[l];
+    const int t0 = w * TT;
+    const float* rb = r + (size_t)b * n * 3;
+    const float* wpb = WPl + (size_t)b * n * n * 96 + f;           // records [i * n + j][3][32]
+    const float* hmb = HM + (size_t)b * n * Tp * 32 + f;           // [j][Tp][32]
+    {
+        float acc[TI][TT];
+        #pragma unroll
+        for (int ii = 0; ii < TI; ++ii)
+            #pragma unroll
+            for (int k = 0; k < TT; ++k) acc[ii][k] = 0.f;
+        const int i_last = i0 + ni - 1;
+        for (int j = 0; j < n; ++j) {
+            const float* hj = hmb + (size_t)j * Tp * 32;
+            float h[TT];
+            #pragma unroll
+            for (int k = 0; k < TT; ++k) h[k] = (t0 + k < T) ? __ldg(hj + (t0 + k) * 32) : 0.f;
+            #pragma unroll
+            for (int ii = 0; ii < TI; ++ii) {
+                const int i = min(i0 + ii, i_last);           // rows past the tile repeat the last one
+                const float w0 = __ldg(wpb + ((size_t)i * n + j) * 96);
+                #pragma unroll
+                for (int k = 0; k < TT; ++k) acc[ii][k] = fmaf(w0, h[k], acc[ii][k]);
+            }
+        }
+        #pragma unroll
+        for (int ii = 0; ii < TI; ++ii)
+            #pragma unroll
+            for (int k = 0; k < TT; ++k) out[(ii * Tp + t0 + k) * 32 + f] = acc[ii][k];
+    }
+    // product-rule partials of the own-gradient channels and the Laplacian, j split over warps
+    for (int ii = 0; ii < ni; ++ii) {
+        const int i = i0 + ii;
+        const float rx = rb[i * 3], ry = rb[i * 3 + 1], rz = rb[i * 3 + 2];
+        float o0 = 0.f, o1 = 0.f, o2 = 0.f, ol = 0.f;
+        for (int j = w; j < n; j += NW) {
+            if (j == i) continue;
+            const float* wr = wpb + ((size_t)i * n + j) * 96;
+            const float* hj = hmb + (size_t)j * Tp * 32;
+            const float w1 = __ldg(wr + 32), w2 = __ldg(wr + 64), h0 = __ldg(hj);
+            const float dx = rb[j * 3] - rx, dy = rb[j * 3 + 1] - ry, dz = rb[j * 3 + 2] - rz;
+            const float inv = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
+            const float ux = dx * inv, uy = dy * inv, uz = dz * inv;
+            o0 += w1 * ux * h0; o1 += w1 * uy * h0; o2 += w1 * uz * h0;
+            const float cross = ux * (__ldg(hj + (1 + 3 * j) * 32) - __ldg(hj + (1 + 3 * i) * 32)) +
+                                uy * (__ldg(hj + (2 + 3 * j) * 32) - __ldg(hj + (2 + 3 * i) * 32)) +
+                                uz * (__ldg(hj + (3 + 3 * j) * 32) - __ldg(hj + (3 + 3 * i) * 32));
+            ol += 2.f * (w2 + 2.f * w1 * inv) * h0 + 2.f * w1 * cross;
+        }
+        float* rr = red + ((w * TI + ii) * 4) * 32 + f;
+        rr[0] = o0; rr[32] = o1; rr[64] = o2; rr[96] = ol;
+    }
+    // conv_ei on its 5 non-zero channels: items (ii, ch) over the warps
+    const float* hs = himl + (size_t)seg_of(d, b) * 4 * d.N * 32 + f;
+    for (int it = w; it < ni * 5; it += NW) {
+        const int ii = it / 5, ch = it % 5;
+        const float* he = HEl + ((size_t)b * n * d.N + (size_t)(i0 + ii) * d.N) * 5 * 32 + ch * 32 + f;
+        float v = 0.f;
+        if (f < eiw)
+            for (int I = 0; I < d.N; ++I) v += __ldg(he + I * 5 * 32) * __ldg(hs + I * 32);
+        eiv[(ii * 5 + ch) * 32 + f] = v;
+    }
+    __syncthreads();
+    // single product-rule terms: channel 1 + 3m + c of electron i gains w'_im u_im,c h_m,0 (m != i)
+    for (int it = w; it < ni * n; it += NW) {
+        const int ii = it / n, m = it % n, i = i0 + ii;
+        float* o = out + (ii * Tp) * 32 + f;
+        if (m == i) {
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, sl = 0.f;
+            for (int q = 0; q < NW; ++q) {
+                const float* rr = red + ((q * TI + ii) * 4) * 32 + f;
+                s0 += rr[0]; s1 += rr[32]; s2 += rr[64]; sl += rr[96];
+            }
+            o[(1 + 3 * i) * 32] -= s0; o[(2 + 3 * i) * 32] -= s1; o[(3 + 3 * i) * 32] -= s2;
+            o[d.lap * 32] += sl;
+        } else {
+            const float dx = rb[m * 3] - rb[i * 3], dy = rb[m * 3 + 1] - rb[i * 3 + 1], dz = rb[m * 3 + 2] - rb[i * 3 + 2];
+            const float inv = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
+            const float g = __ldg(wpb + ((size_t)i * n + m) * 96 + 32) * __ldg(hmb + (size_t)m * Tp * 32) * inv;
+            o[(1 + 3 * m) * 32] += g * dx; o[(2 + 3 * m) * 32] += g * dy; o[(3 + 3 * m) * 32] += g * dz;
+        }
+    }
+    __syncthreads();
+    // stores: row (ii, t), units of 8 columns: 4 units of conv_ee, then conv_ei
+    const int ei_units = (eiw + 7) / 8;
+    const int units = 4 + ei_units;
+    const bool rowvec = (hw % 8) == 0 && (ldx % 8) == 0;      // 16-byte aligned column groups
+    for (int it = threadIdx.x; it < ni * Tp * units; it += blockDim.x) {
+        const int u = it % units, rt = it / units, t = rt % Tp, ii = rt / Tp, i = i0 + ii;
+        const int64_t row = ((int64_t)b * n + i) * Tp + t;
+        float v[8];
+        int col;
+        if (u < 4) {
+            const float* src = out + (ii * Tp + t) * 32 + 8 * u;
+            #pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = t < T ? src[k] : 0.f;
+            col = hw + 8 * u;
+        } else {
+            int ch = -1;
+            if (t == 0) ch = 0;
+            else if (t == d.lap) ch = 4;
+            else if (t >= 1 + 3 * i && t < 4 + 3 * i) ch = t - 3 * i;
+            const float* src = eiv + (ii * 5 + (ch < 0 ? 0 : ch)) * 32 + 8 * (u - 4);
+            #pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = ch >= 0 ? src[k] : 0.f;
+            col = hw + E + 8 * (u - 4);
+        }
+        if (rowvec && (u < 4 || eiw - 8 * (u - 4) >= 8)) {
+            ActIO<Act>::store8(X, row, ldx, col, v);
+        } else {
+            const int lim = u < 4 ? 8 : min(8, eiw - 8 * (u - 4));
+            #pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < lim) ActIO<Act>::store(X, row, ldx, col + k, v[k]);
+        }
     }
 }
 
@@ -473,7 +631,8 @@ k_conv_walker(const float* __restrict__ r, const float* __restrict__ WPl, const 
                 else if (t >= 1 + 3 * i && t < 4 + 3 * i) ch = t - 3 * i;
                 if (ch >= 0) {
                     const float* he = heb + (size_t)i * d.N * ech * 32;
-                    for (int I = 0; I < d.N; ++I) v += __ldg(he + (I * ech + ch) * 32 + f) * __ldg(himl + I * 32 + f);
+                    const float* hs = himl + (size_t)seg_of(d, b) * 4 * d.N * 32;
+                    for (int I = 0; I < d.N; ++I) v += __ldg(he + (I * ech + ch) * 32 + f) * __ldg(hs + I * 32 + f);
                 }
             }
         }
@@ -484,9 +643,9 @@ k_conv_walker(const float* __restrict__ r, const float* __restrict__ WPl, const 
 // ------------------------------------------------------------------ envelope x backflow -> Slater tangents
 // mo[b][k][t][i][o] = env[i,(k,o)] * bf[i,(k,o)] with tangents (envelope_orbitals.py:91-127).
 // env = sum_I w_I exp(-softplus(alpha_I) d_iI); grad/Laplacian w.r.t. r_i only.
-__global__ void k_envelope(const float* __restrict__ r, const float* __restrict__ R, const float* __restrict__ P,
-                           ParamLayout L, const float* __restrict__ spA, Dims d, int B, const float* __restrict__ BF,
-                           int ldbf, float* __restrict__ MO) {
+__global__ void k_envelope(const float* __restrict__ r, const float* __restrict__ Rall, const int32_t* __restrict__ Zall,
+                           const float* __restrict__ P, ParamLayout L, const float* __restrict__ spA, Dims d, int B,
+                           const float* __restrict__ BF, int ldbf, float* __restrict__ MO) {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)B * d.n * d.KN) return;
     int col = idx % d.KN;
@@ -497,8 +656,12 @@ __global__ void k_envelope(const float* __restrict__ r, const float* __restrict_
     const float* spa = spA + (up ? 0 : d.N * d.KN);          // softplus(alpha), prepared
     const float* wts = P + (up ? L.weights_up : L.weights_dn);
     const float* ri = r + bi * 3;
+    const int sg = seg_of(d, b);
+    const float* R = Rall + (size_t)sg * d.N * 3;
+    const int32_t* Z = Zall + (size_t)sg * d.N;
     float env = 0.f, g[3] = {0.f, 0.f, 0.f}, lapv = 0.f;
     for (int I = 0; I < d.N; ++I) {
+        if (Z[I] <= 0) continue;                                  // padding ion
         float s0 = ri[0] - R[I * 3], s1 = ri[1] - R[I * 3 + 1], s2 = ri[2] - R[I * 3 + 2];
         float dd = sqrtf(s0 * s0 + s1 * s1 + s2 * s2);
         float a = __ldg(spa + I * d.KN + col);
@@ -546,14 +709,15 @@ __global__ void k_jastrow_out(const Act* __restrict__ J2, int ldj, const float* 
 
 // ------------------------------------------------------------------ launch wrappers
 void launch_ion_maps(const float* P, const ParamLayout& L, const Dims& d, const int32_t* Z, float* him, cudaStream_t s) {
-    k_ion_maps<<<1, 256, 0, s>>>(P, L, d, Z, him); count_launch();
+    const int n = d.nseg * 4 * d.N * 32;
+    k_ion_maps<<<(n + 255) / 256, 256, 0, s>>>(P, L, d, Z, him); count_launch();
 }
 template <class Act>
-void launch_features(const float* r, const float* R, const Dims& d, int B, Act* X0, cudaStream_t s) {
-    k_features<Act><<<B * d.n, 256, 0, s>>>(r, R, d, B, X0); count_launch();
+void launch_features(const float* r, const float* R, const int32_t* Z, const Dims& d, int B, Act* X0, cudaStream_t s) {
+    k_features<Act><<<B * d.n, 256, 0, s>>>(r, R, Z, d, B, X0); count_launch();
 }
-void launch_streams(const float* r, const float* R, const float* P, const ParamLayout& L, const Dims& d, int B,
-                    float* WP, float* HE, cudaStream_t s, float* HP) {
+void launch_streams(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,
+                    const Dims& d, int B, float* WP, float* HE, cudaStream_t s, float* HP) {
     const bool tang = d.Tp > 1;
     const int64_t npair = (int64_t)B * d.n * (d.n + 1) / 2, nei = (int64_t)B * d.n * d.N;
     auto blocks = [](int64_t n) { return (unsigned)((n + 127) / 128); };
@@ -562,11 +726,11 @@ void launch_streams(const float* r, const float* R, const float* P, const ParamL
         cudaFuncSetAttribute(k_ei_streams<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm5);
         cudaFuncSetAttribute(k_pair_streams<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
         k_pair_streams<3><<<blocks(npair), 128, sm3, s>>>(r, P, L, d, B, WP, nullptr);
-        k_ei_streams<5><<<blocks(nei), 128, sm5, s>>>(r, R, P, L, d, B, HE);
+        k_ei_streams<5><<<blocks(nei), 128, sm5, s>>>(r, R, Z, P, L, d, B, HE);
     } else {
         size_t sm1 = 128 * (32 + 1) * sizeof(float);
         k_pair_streams<1><<<blocks(npair), 128, sm1, s>>>(r, P, L, d, B, WP, HP);
-        k_ei_streams<1><<<blocks(nei), 128, sm1, s>>>(r, R, P, L, d, B, HE);
+        k_ei_streams<1><<<blocks(nei), 128, sm1, s>>>(r, R, Z, P, L, d, B, HE);
     }
     count_launch(2);
 }
@@ -585,6 +749,24 @@ void launch_tanh_fl(const float* Zb, int ldz, int ncols, int groups, const Dims&
 template <class Act>
 void launch_conv(const float* r, const float* WPl, const float* HM, const float* HEl, const float* himl, const Dims& d,
                  int l, int B, Act* X, int ldx, cudaStream_t s) {
+    if (d.Tp >= 8 && d.Tp <= 128 && d.E == 32) {
+        const unsigned grid = (unsigned)B * ((d.n + 3) / 4);
+        const int TT = d.Tp >= 64 ? 8 : d.Tp / 8;
+        const int NW = d.Tp / TT;
+        const size_t smem = ((size_t)4 * d.Tp * 32 + (size_t)NW * 4 * 4 * 32 + 4 * 5 * 32) * sizeof(float);
+        auto go = [&](auto kern) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kern<<<grid, NW * 32, smem, s>>>(r, WPl, HM, HEl, himl, d, l, B, X, ldx);
+        };
+        switch (TT) {
+            case 1: go(k_conv_tile<Act, 1>); break;
+            case 2: go(k_conv_tile<Act, 2>); break;
+            case 4: go(k_conv_tile<Act, 4>); break;
+            default: go(k_conv_tile<Act, 8>); break;
+        }
+        count_launch();
+        return;
+    }
     const size_t smem = ((size_t)d.n * d.Tp * 32 + (size_t)d.n * d.n * 4) * sizeof(float);
     if (smem <= 200 * 1024) {
         if (smem > 48 * 1024)
@@ -595,10 +777,10 @@ void launch_conv(const float* r, const float* WPl, const float* HM, const float*
     }
     count_launch();
 }
-void launch_envelope(const float* r, const float* R, const float* P, const ParamLayout& L, const float* sp_alpha,
-                     const Dims& d, int B, const float* BF, int ldbf, float* MO, cudaStream_t s) {
+void launch_envelope(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,
+                     const float* sp_alpha, const Dims& d, int B, const float* BF, int ldbf, float* MO, cudaStream_t s) {
     int64_t n = (int64_t)B * d.n * d.KN;
-    k_envelope<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, R, P, L, sp_alpha, d, B, BF, ldbf, MO); count_launch();
+    k_envelope<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, R, Z, P, L, sp_alpha, d, B, BF, ldbf, MO); count_launch();
 }
 template <class Act>
 void launch_jastrow_out(const Act* J2, int ldj, const float* w2, const Dims& d, int B, double* jas, cudaStream_t s) {
@@ -607,7 +789,8 @@ void launch_jastrow_out(const Act* J2, int ldj, const float* w2, const Dims& d, 
 }
 
 #define DW_INST(Act)                                                                                          \
-    template void launch_features<Act>(const float*, const float*, const Dims&, int, Act*, cudaStream_t);     \
+    template void launch_features<Act>(const float*, const float*, const int32_t*, const Dims&, int, Act*,    \
+                                       cudaStream_t);                                                         \
     template void launch_spin_means<Act>(const Act*, int, int, const Dims&, int, Act*, int, cudaStream_t);    \
     template void launch_tanh_fl<Act>(const float*, int, int, int, const Dims&, Act*, int, cudaStream_t);     \
     template void launch_conv<Act>(const float*, const float*, const float*, const float*, const float*,      \

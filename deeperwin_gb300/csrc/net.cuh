@@ -1,5 +1,6 @@
 // Declarations of the network, determinant, MCMC and GEMM launchers.
 #pragma once
+#include <type_traits>
 #include "common.cuh"
 
 namespace dw {
@@ -21,6 +22,22 @@ template <class Act> struct ActIO {
     __device__ static __forceinline__ void store(Act* b, int64_t row, int ld, int col, float x) {
         b[row * ld + col] = from_f<Act>(x);
     }
+    // eight consecutive columns; col % 8 == 0 and the row start 16-byte aligned
+    __device__ static __forceinline__ void store8(Act* b, int64_t row, int ld, int col, const float (&x)[8]) {
+        if constexpr (std::is_same<Act, float>::value) {
+            float4* o = reinterpret_cast<float4*>(b + row * ld + col);
+            o[0] = make_float4(x[0], x[1], x[2], x[3]);
+            o[1] = make_float4(x[4], x[5], x[6], x[7]);
+        } else {
+            uint32_t p[4];
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                __nv_bfloat162 h = __floats2bfloat162_rn(x[2 * k], x[2 * k + 1]);
+                p[k] = *reinterpret_cast<uint32_t*>(&h);
+            }
+            *reinterpret_cast<uint4*>(b + row * ld + col) = make_uint4(p[0], p[1], p[2], p[3]);
+        }
+    }
     __device__ static __forceinline__ float load(const Act* b, int64_t row, int ld, int col) {
         return to_f(b[row * ld + col]);
     }
@@ -33,6 +50,18 @@ template <> struct ActIO<Split> {
         b[row * 2 * ld + col].v = hi;
         b[row * 2 * ld + ld + col].v = lo;
     }
+    __device__ static __forceinline__ void store8(Split* b, int64_t row, int ld, int col, const float (&x)[8]) {
+        uint32_t ph[4], pl[4];
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            __nv_bfloat162 h = __floats2bfloat162_rn(x[2 * k], x[2 * k + 1]);
+            __nv_bfloat162 l = __floats2bfloat162_rn(x[2 * k] - __low2float(h), x[2 * k + 1] - __high2float(h));
+            ph[k] = *reinterpret_cast<uint32_t*>(&h);
+            pl[k] = *reinterpret_cast<uint32_t*>(&l);
+        }
+        *reinterpret_cast<uint4*>(b + row * 2 * ld + col) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+        *reinterpret_cast<uint4*>(b + row * 2 * ld + ld + col) = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+    }
     __device__ static __forceinline__ float load(const Split* b, int64_t row, int ld, int col) {
         return __bfloat162float(b[row * 2 * ld + col].v) + __bfloat162float(b[row * 2 * ld + ld + col].v);
     }
@@ -40,15 +69,16 @@ template <> struct ActIO<Split> {
 
 // net.cu
 void launch_ion_maps(const float* P, const ParamLayout& L, const Dims& d, const int32_t* Z, float* him, cudaStream_t s);
-template <class Act> void launch_features(const float* r, const float* R, const Dims& d, int B, Act* X0, cudaStream_t s);
-void launch_streams(const float* r, const float* R, const float* P, const ParamLayout& L, const Dims& d, int B,
-                    float* WP, float* HE, cudaStream_t s, float* HP = nullptr);
+template <class Act> void launch_features(const float* r, const float* R, const int32_t* Z, const Dims& d, int B, Act* X0,
+                                          cudaStream_t s);
+void launch_streams(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,
+                    const Dims& d, int B, float* WP, float* HE, cudaStream_t s, float* HP = nullptr);
 template <class Act> void launch_spin_means(const Act* X, int ldx, int hw, const Dims& d, int B, Act* M, int mw, cudaStream_t s);
 template <class Act> void launch_tanh_fl(const float* Zb, int ldz, int ncols, int groups, const Dims& d, Act* Y, int ldy, cudaStream_t s);
 template <class Act> void launch_conv(const float* r, const float* WPl, const float* HM, const float* HEl, const float* himl,
                                       const Dims& d, int l, int B, Act* X, int ldx, cudaStream_t s);
-void launch_envelope(const float* r, const float* R, const float* P, const ParamLayout& L, const float* sp_alpha,
-                     const Dims& d, int B, const float* BF, int ldbf, float* MO, cudaStream_t s);
+void launch_envelope(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,
+                     const float* sp_alpha, const Dims& d, int B, const float* BF, int ldbf, float* MO, cudaStream_t s);
 template <class Act> void launch_jastrow_out(const Act* J2, int ldj, const float* w2, const Dims& d, int B, double* jas, cudaStream_t s);
 
 // gemm_simt.cu: C[m, n] = sum_k A[m, k] W[k, n] with epilogue.

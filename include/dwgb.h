@@ -144,6 +144,36 @@ int dw_mcmc_steps(const DwArch* arch, int precision, const float* params, const 
                   float* log_psi_sqr, int32_t* age, DwMcmcScalars* scalars_dev,
                   const DwMcmcConfig* cfg, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- Packed launches (continuous-batching serving) -------------------------------------
+ * One launch over the walkers of nseg geometries (requests) that share n_el and n_up and one
+ * weight set. Geometry g occupies R[g * n_ions .. ][3] and Z[g * n_ions ..]; a geometry with
+ * fewer nuclei than arch->n_ions is padded with Z = 0 ions, which contribute exactly nothing
+ * (input features, ion maps, envelopes, Coulomb). seg[b] in [0, nseg) names walker b's
+ * geometry (device int32 array). 1 <= nseg <= 256. Every walker's result equals the result of
+ * the same walker evaluated in a launch of its geometry alone. No counterpart in the reference,
+ * which evaluates one geometry per call (get_log_psi_squared / get_local_energy with a single
+ * fixed R, Z: model/wavefunction.py:152-171, hamiltonian.py:272-291). */
+int dw_log_psi_sqr_packed(const DwArch* arch, int precision, const float* params, const void* prepared,
+                          const float* r, int n_walkers, const float* R, const int32_t* Z, int nseg,
+                          const int32_t* seg, float* log_psi_sqr, float* phase,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
+int dw_local_energy_packed(const DwArch* arch, int precision, const float* params, const void* prepared,
+                           const float* r, int n_walkers, const float* R, const int32_t* Z, int nseg,
+                           const int32_t* seg, float* E_loc, float* log_psi_sqr, float* grad_log_psi_sqr,
+                           void* workspace, size_t workspace_bytes, void* stream);
+
+/* Packed Metropolis-Hastings: walker b runs in chain seg[b], which has its own scalars
+ * scalars_dev[seg[b]] (step size, acceptance, step counter) and Philox key seeds[seg[b]]
+ * (device uint64 array; cfg->seed is ignored), and draws its random numbers as walker
+ * walker_index[b] of that chain. A chain therefore follows the same trajectory whatever it
+ * is packed with. The other cfg fields apply to all chains. */
+int dw_mcmc_steps_packed(const DwArch* arch, int precision, const float* params, const void* prepared,
+                         float* r, int n_walkers, const float* R, const int32_t* Z, int nseg,
+                         const int32_t* seg, const int32_t* walker_index, const uint64_t* seeds,
+                         float* log_psi_sqr, int32_t* age, DwMcmcScalars* scalars_dev,
+                         const DwMcmcConfig* cfg, void* workspace, size_t workspace_bytes, void* stream);
+
 /* FP64 cross-walker statistics of a float32 vector: out[0]=mean, out[1]=variance
  * (population), out[2]=count of finite entries. NaNs are skipped (nanmean, loss_function.py:94-95). */
 int dw_energy_stats(const float* E, int n, double* out_dev, void* stream);

@@ -137,11 +137,24 @@ def run_ours(args, rank, world, dev):
     L = _lib.lib()
     launches = [0]
 
+    from deeperwin_gb300 import vmc
+    clip_state = [vmc.init_clipping_state()]
+
     def step(prm):
         mh.run_mcmc_steps(None, state, prm, a.n_up, a.n_dn, None, n_steps=n_mh, reevaluate=True)
         launches[0] += api.last_launch_count()
         E = api.local_energy(prm, spin, state.r, state.R, state.Z)
         launches[0] += api.last_launch_count()
+        if w.backward:
+            # clipped VMC gradient (loss_function.py:75-156): tanh clipping with the previous
+            # step's (center, width), coefficients (E_clip - mean) / B, hand-written backward
+            Ec, cs = vmc._clip(E, clip_state[0][0], clip_state[0][1], 5.0)
+            launches[0] += 1
+            coeff = ((Ec.double() - cs[0]) / B).float()
+            vmc.log_psi_sqr_backward(prm, state.r, state.R, state.Z, coeff)
+            launches[0] += api.last_launch_count()
+            c = cs[2:4].cpu()
+            clip_state[0] = (float(c[0]), max(float(c[1]), 1e-12))
         return E
 
     def barrier():
@@ -254,7 +267,8 @@ def run_ours(args, rank, world, dev):
             "data": "synthetic: random-init weights (seed 0), Gaussian walkers around nuclei",
             "config": {"workload": w.name, "molecule": mol.name, "n_el": a.n_el, "n_up": a.n_up,
                        "n_ions": a.n_ions, "n_dets": a.n_dets, "walkers_per_gpu": B, "mh_steps_per_iter": n_mh,
-                       "step": "reevaluate + %d MH forwards + forward-Laplacian E_L" % n_mh,
+                       "step": "reevaluate + %d MH forwards + forward-Laplacian E_L" % n_mh
+                               + (" + clipped VMC gradient (hand-written backward)" if w.backward else ""),
                        "precision": w.precision, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set (activations, several GB per step) exceeds L2; no flush needed"},
             "e2e": e2e, "gpu_launches": int(n_launch), "clocks": clocks, "roofline": roof,

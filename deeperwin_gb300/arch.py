@@ -194,13 +194,14 @@ class Workload:
     n_mh_steps: int
     precision: str           # "fp32" (plain) or "mixed"
     step_size: float = 0.1
+    backward: bool = False   # the step also forms the clipped VMC gradient (hand-written backward)
 
 
 WORKLOADS = {
     "lih": Workload("lih_4e_k8_b2048_fp32", lih, 8, 2048, 10, "fp32"),
     "h10": Workload("h10_10e_k16_b8192_mixed", h_chain, 16, 8192, 10, "mixed"),
-    "c2h4": Workload("c2h4_16e_k32_b4096_mixed", c2h4_shaped, 32, 4096, 10, "mixed"),
-    "scale40": Workload("scale_40e_k64_b16384_mixed", scale_molecule, 64, 16384, 10, "mixed"),
+    "c2h4": Workload("c2h4_16e_k32_b4096_mixed_grad", c2h4_shaped, 32, 4096, 10, "mixed", backward=True),
+    "scale40": Workload("scale_40e_k64_b16384_mixed_grad", scale_molecule, 64, 16384, 10, "mixed", backward=True),
 }
 
 

@@ -547,7 +547,6 @@ int backward_all(const DwArch* a, const float* P, const float* const main[4], co
                  const float* bf_cat, const float* sp_alpha, const float* r, int B, const float* R, const int32_t* Z,
                  const float* coeff, float* grad, void* ws, size_t wsb, cudaStream_t s) {
     Dims d = make_dims(a, false);
-    if (d.n > 32) return DW_ERR_ARCH;
     ParamLayout L;
     make_layout(a, &L);
     int bc = 0;

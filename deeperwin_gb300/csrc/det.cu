@@ -177,6 +177,90 @@ k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, double* __re
     }
 }
 
+// Value-only log|det| with rows in lanes: a team of n lanes per matrix (32 / n matrices per
+// warp), lane r owning row r of A. Per pivot k: a segmented shuffle argmax over the team picks
+// the first row of maximal |a_rk| at or below the diagonal (as LAPACK getrf; magnitudes are
+// compared through their IEEE bit patterns, which order non-negative values), the two rows are
+// exchanged by shuffles, the pivot row is broadcast one entry at a time and every lane below
+// the pivot eliminates its own row: (n - k - 1) FMAs per lane, the minimum for LU. After each
+// step the rows shift one column to the left, so the pivot column is always register a[0] and
+// every register index is static (the pivot loop itself is not unrolled). The pivot product is
+// kept as a mantissa and a binary exponent (frexp), with one log per matrix.
+template <class S> __device__ __forceinline__ int mag_key(S v);
+template <> __device__ __forceinline__ int mag_key<double>(double v) { return __double2hiint(v) & 0x7fffffff; }
+template <> __device__ __forceinline__ int mag_key<float>(float v) { return __float_as_int(v) & 0x7fffffff; }
+
+template <class S, int NMAX>
+__global__ void __launch_bounds__(128)
+k_slogdet_rows(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
+               double* __restrict__ sign) {
+    const int lane = threadIdx.x & 31;
+    const int teams = 32 / n;
+    const int team = lane / n, r = lane % n;
+    const bool lane_on = team < teams;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int mat = gw * teams + (lane_on ? team : 0);
+    const bool active = lane_on && mat < nmat;
+    const int base = (lane_on ? team : 0) * n;
+    S a[NMAX];
+    const float* A = MO + (int64_t)(active ? mat : 0) * T * n * n + (int64_t)r * n;
+    #pragma unroll
+    for (int c = 0; c < NMAX; ++c) a[c] = (active && c < n) ? (S)__ldg(A + c) : (S)0;
+    double mant = 1.0, sg = 1.0;
+    int expo = 0;
+    bool singular = false;
+    #pragma unroll 1
+    for (int k = 0; k < n; ++k) {
+        const int rem = n - k;                       // live columns a[0 .. rem)
+        // team argmax of |a_r0| over rows r >= k (ties: lowest row)
+        int key = (lane_on && r >= k) ? mag_key<S>(a[0]) : -1, row = r;
+        #pragma unroll
+        for (int off = 1; off < NMAX; off <<= 1) {
+            const int ok = __shfl_down_sync(0xffffffffu, key, off);
+            const int orow = __shfl_down_sync(0xffffffffu, row, off);
+            if (r + off < n && (ok > key || (ok == key && orow < row))) { key = ok; row = orow; }
+        }
+        const int p = __shfl_sync(0xffffffffu, row, base);
+        const int kmax = __shfl_sync(0xffffffffu, key, base);
+        bool sing_now = kmax <= 0;
+        // row exchange; the shuffles run warp-wide whenever any team of the warp swaps
+        const bool swap = p != k;
+        if (__any_sync(0xffffffffu, swap)) {
+            const int src = base + (swap ? (r == k ? p : (r == p ? k : r)) : r);
+            #pragma unroll
+            for (int c = 0; c < NMAX; ++c) {
+                if (c >= rem) break;
+                a[c] = __shfl_sync(0xffffffffu, a[c], src);
+            }
+        }
+        if (swap) sg = -sg;
+        S pk = __shfl_sync(0xffffffffu, a[0], base + k);
+        sing_now = sing_now || pk == (S)0;
+        singular = singular || sing_now;
+        if (sing_now) pk = (S)1;
+        int e;
+        mant *= frexp(fabs((double)pk), &e);
+        expo += e;
+        mant = frexp(mant, &e);
+        expo += e;
+        if (pk < (S)0) sg = -sg;
+        const bool below = r > k;
+        const S l = below ? a[0] / pk : (S)0;
+        #pragma unroll
+        for (int c = 1; c < NMAX; ++c) {
+            if (c >= rem) break;
+            const S pc = __shfl_sync(0xffffffffu, a[c], base + k);
+            if (below) a[c] -= l * pc;
+        }
+        #pragma unroll
+        for (int c = 0; c + 1 < NMAX; ++c) a[c] = a[c + 1];
+    }
+    if (active && r == 0) {
+        logdet[mat] = singular ? -INFINITY : log(mant) + (double)expo * 0.69314718055994530942;
+        sign[mat] = singular ? 0.0 : sg;
+    }
+}
+
 template <class S>
 void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, int want_inv,
                          cudaStream_t s);
@@ -196,6 +280,15 @@ void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, 
         const int teams = 32 / n;
         const int64_t warps = (nmat + teams - 1) / teams;
         const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
+        if (!want_inv && n > 16) {
+            // rows in lanes beyond 16 electrons (the column form's unrolled register arrays
+            // no longer stay in registers there)
+            auto rows = [&](auto kern) { kern<<<blocks, 128, 0, s>>>(MO, n, d.T, nmat, logdet, sign); };
+            if (n <= 24) rows(k_slogdet_rows<S, 24>);
+            else rows(k_slogdet_rows<S, 32>);
+            count_launch();
+            return;
+        }
         auto go = [&](auto kern) { kern<<<blocks, 128, 0, s>>>(MO, n, d.T, nmat, logdet, sign, Ainv); };
         bool done = false;
         if constexpr (std::is_same<S, double>::value) {

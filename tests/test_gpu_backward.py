@@ -9,21 +9,39 @@ from oracle import dpe4 as O
 pytestmark = pytest.mark.gpu
 
 
-def _oracle_grad(a, p, r, mol, coeff):
-    pt = {k: torch.tensor(v, dtype=torch.float64, requires_grad=True) for k, v in p.items()}
+def _oracle_grad(a, p, r, mol, coeff, dtype=torch.float64):
+    """d/dtheta sum_b coeff_b log psi^2_b from the oracle by autograd (FP64, or the same
+    mathematics in FP32 to measure what FP32 arithmetic alone costs)."""
+    old = O.T
+    O.T = dtype
+    try:
+        return _oracle_grad_t(a, p, r, mol, coeff, dtype)
+    finally:
+        O.T = old
+
+
+def _oracle_grad_t(a, p, r, mol, coeff, dtype):
+    pt = {k: torch.tensor(v, dtype=dtype, requires_grad=True) for k, v in p.items()}
     lp = O.log_psi_sqr(pt, a, r, mol.R, mol.Z)[1]
-    (lp * torch.tensor(coeff, dtype=torch.float64)).sum().backward()
+    (lp * torch.tensor(coeff, dtype=dtype)).sum().backward()
     g = {k: v.grad.numpy() for k, v in pt.items()}
     lay, total = P.layout(a)
     flat = np.zeros(total)
     for k, (o, s) in lay.items():
-        flat[o:o + s] = g[k].reshape(-1)
+        flat[o:o + s] = g[k].reshape(-1).astype(np.float64)
     return flat
 
 
-@pytest.mark.parametrize("case", ["lih", "h6", "c2h4"])
+def _o4h2():
+    """34 electrons (n > 32: the shared-memory LU / inverse of the larger molecules)."""
+    R = np.array([[0.0, 0, 0], [2.6, 0, 0], [0, 2.6, 0], [2.6, 2.6, 0], [1.3, 1.3, 2.2], [1.3, 1.3, -2.2]])
+    return A.Molecule(R=R, Z=np.array([8, 8, 8, 8, 1, 1]), n_el=34, n_up=17, name="O4H2")
+
+
+@pytest.mark.parametrize("case", ["lih", "h6", "c2h4", "o4h2"])
 def test_backward_matches_oracle_autograd(cuda, case):
-    mol, K, B = {"lih": (A.lih(), 4, 5), "h6": (A.h_chain(6), 4, 3), "c2h4": (A.c2h4_shaped(), 2, 2)}[case]
+    mol, K, B = {"lih": (A.lih(), 4, 5), "h6": (A.h_chain(6), 4, 3), "c2h4": (A.c2h4_shaped(), 2, 2),
+                 "o4h2": (_o4h2(), 2, 2)}[case]
     a = A.arch_for(mol, K)
     p = P.init_params(a, 2, bias_std=0.1, envelope_jitter=0.2)
     r = A.init_walkers(mol, B, seed=3)
@@ -34,10 +52,20 @@ def test_backward_matches_oracle_autograd(cuda, case):
     ref = _oracle_grad(a, p, r, mol, coeff)
     scale = np.abs(ref).max()
     err = np.abs(g - ref)
+    # The kernels recompute the forward in FP32, so the error floor is that of FP32 arithmetic
+    # on these Slater matrices (condition numbers 1e3 at 16 electrons, 2-6e4 at 34, where it
+    # reaches 1e-4 to 8e-4 of the gradient scale depending on the host's FP32 op order): the
+    # same oracle run in FP32 measures it. The bound is 1e-4 of the gradient scale or 5x that
+    # floor (the kernels measured 2.7x at 34 electrons).
+    floor = np.abs(_oracle_grad(a, p, r, mol, coeff, torch.float32) - ref)
+    tol = max(1e-4 * scale, 5.0 * floor.max())
+    tol_norm = max(1e-4 * np.linalg.norm(ref), 5.0 * np.linalg.norm(floor))
     lay, _ = P.layout(a)
     worst = sorted(((float(err[o:o + s].max() / scale), k) for k, (o, s) in lay.items()), reverse=True)[:3]
-    assert err.max() <= 1e-4 * scale, worst
-    assert np.linalg.norm(g - ref) <= 1e-4 * np.linalg.norm(ref), worst
+    assert err.max() <= tol, (worst, tol / scale)
+    assert np.linalg.norm(g - ref) <= tol_norm, (worst, tol_norm)
+    if case != "o4h2":
+        assert err.max() <= 1e-4 * scale, worst
 
 
 def test_backward_matches_central_finite_differences(cuda):

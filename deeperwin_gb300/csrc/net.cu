@@ -213,6 +213,204 @@ k_pair_streams(const float* __restrict__ r, const float* __restrict__ P, ParamLa
     }
 }
 
+// ------------------------------------------------------------------ value-mode stream MLPs
+// Value-only 2-el and el-ion streams as block-level MLP chains: a block takes RB = 64 rows
+// (unordered electron pairs of one spin type, or electron-ion entries) and keeps their
+// activations in shared memory, feature-major, through all layers; each layer is a
+// [64 x in] x [in x 32] product with 4 x 4 register tiles per thread (a 16-byte shared load of
+// 4 rows and one of 4 weights per k feeds 16 FMAs), the layer's weights staged in shared
+// memory. Same mathematics as k_pair_streams<1> / k_ei_streams<1>.
+constexpr int kRB = 64;
+struct MlpSmem {
+    float H[2][32][kRB + 4];     // activations [buffer][feature][row]
+    float W[32 * 32];
+    float bias[32];
+};
+
+__device__ __forceinline__ void mlp_load_w(MlpSmem& sm, const float* __restrict__ W, const float* __restrict__ b,
+                                           int in_w) {
+    for (int e = threadIdx.x; e < in_w * 32; e += blockDim.x) sm.W[e] = __ldg(W + e);
+    if (threadIdx.x < 32) sm.bias[threadIdx.x] = __ldg(b + threadIdx.x);
+}
+
+// z[rr][ff] = bias[f] + sum_k H[k][row] W[k][f], rows 4 rg + rr, features 4 fg + ff
+__device__ __forceinline__ void mlp_tile(const MlpSmem& sm, int cur, int in_w, int rg, int fg, float (&z)[4][4]) {
+    const float4 b4 = *reinterpret_cast<const float4*>(&sm.bias[4 * fg]);
+    #pragma unroll
+    for (int rr = 0; rr < 4; ++rr) { z[rr][0] = b4.x; z[rr][1] = b4.y; z[rr][2] = b4.z; z[rr][3] = b4.w; }
+    #pragma unroll 8
+    for (int k = 0; k < in_w; ++k) {
+        const float4 h4 = *reinterpret_cast<const float4*>(&sm.H[cur][k][4 * rg]);
+        const float4 w4 = *reinterpret_cast<const float4*>(&sm.W[k * 32 + 4 * fg]);
+        const float hv[4] = {h4.x, h4.y, h4.z, h4.w};
+        #pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+            z[rr][0] = fmaf(hv[rr], w4.x, z[rr][0]); z[rr][1] = fmaf(hv[rr], w4.y, z[rr][1]);
+            z[rr][2] = fmaf(hv[rr], w4.z, z[rr][2]); z[rr][3] = fmaf(hv[rr], w4.w, z[rr][3]);
+        }
+    }
+}
+
+// Blocks [0, blocks_same) take same-spin pairs (up-up then down-down, i <= j), the rest the
+// up-down pairs. WP[l][b][i n + j][32] gets both orders; HP (optional) the stream levels 1..3
+// at the unordered-pair index used by the backward pass.
+__global__ void __launch_bounds__(128)
+k_pair_mlp(const float* __restrict__ r, const float* __restrict__ P, ParamLayout L, Dims d, int B, int blocks_same,
+           float* __restrict__ WP, float* __restrict__ HP) {
+    __shared__ __align__(16) MlpSmem sm;
+    __shared__ int rw[kRB], ri[kRB], rj[kRB];
+    const int tid = threadIdx.x;
+    const int n = d.n, nu = d.nu, nd = d.nd;
+    const bool same = (int)blockIdx.x < blocks_same;
+    const int cu = nu * (nu + 1) / 2;
+    const int npt = same ? cu + nd * (nd + 1) / 2 : nu * nd;
+    const int64_t g0 = (int64_t)(same ? blockIdx.x : blockIdx.x - blocks_same) * kRB;
+    const int64_t total = (int64_t)B * npt;
+    for (int q = tid; q < kRB; q += blockDim.x) {
+        const int64_t g = g0 + q;
+        int b = -1, i = 0, j = 0;
+        if (g < total) {
+            b = (int)(g / npt);
+            int p = (int)(g % npt);
+            if (same) {
+                int m = nu, base = 0;
+                if (p >= cu) { p -= cu; m = nd; base = nu; }
+                int a = 0;
+                while (p >= m - a) { p -= m - a; ++a; }
+                i = base + a; j = base + a + p;
+            } else {
+                i = p / nd; j = nu + p % nd;
+            }
+        }
+        rw[q] = b; ri[q] = i; rj[q] = j;
+        float dd = 0.f;
+        if (b >= 0 && i != j) {
+            const float* rb = r + (int64_t)b * n * 3;
+            const float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
+            dd = sqrtf(dx * dx + dy * dy + dz * dz);
+        }
+        sm.H[0][0][q] = dd;             // input feature [dist] (utils.py:297-300: 0 on the diagonal)
+    }
+    const int rg = tid >> 3, fg = tid & 7;
+    const int64_t plane = (int64_t)B * n * n;
+    const int64_t npair_u = (int64_t)n * (n + 1) / 2;
+    const float rs = 0.70710678118654752f;
+    int cur = 0;
+    for (int l = 0; l < 4; ++l) {
+        const int in_w = d.eew[l];
+        __syncthreads();
+        mlp_load_w(sm, P + (same ? L.w_same_w[l] : L.w_diff_w[l]), P + (same ? L.w_same_b[l] : L.w_diff_b[l]), in_w);
+        __syncthreads();
+        float z[4][4];
+        mlp_tile(sm, cur, in_w, rg, fg, z);
+        #pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+            const int q = 4 * rg + rr, b = rw[q];
+            if (b < 0) continue;
+            const int i = ri[q], j = rj[q];
+            const float4 v = make_float4(tanhf(z[rr][0]), tanhf(z[rr][1]), tanhf(z[rr][2]), tanhf(z[rr][3]));
+            const int64_t wb = (int64_t)l * plane + (int64_t)b * n * n;
+            *reinterpret_cast<float4*>(WP + (wb + i * n + j) * 32 + 4 * fg) = v;
+            if (i != j) *reinterpret_cast<float4*>(WP + (wb + j * n + i) * 32 + 4 * fg) = v;
+        }
+        if (l == 3) break;
+        __syncthreads();
+        mlp_load_w(sm, P + (same ? L.h_same_w[l] : L.h_diff_w[l]), P + (same ? L.h_same_b[l] : L.h_diff_b[l]), in_w);
+        __syncthreads();
+        mlp_tile(sm, cur, in_w, rg, fg, z);
+        #pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+            const int q = 4 * rg + rr;
+            float hn[4];
+            #pragma unroll
+            for (int ff = 0; ff < 4; ++ff) {
+                const int f = 4 * fg + ff;
+                const float y = tanhf(z[rr][ff]);
+                hn[ff] = l > 0 ? (sm.H[cur][f][q] + y) * rs : y;        // residual (mlp.py:13-17)
+                sm.H[cur ^ 1][f][q] = hn[ff];
+            }
+            const int b = rw[q];
+            if (HP && b >= 0) {     // keep h^(l+1) of this unordered pair for the backward pass
+                const int i = ri[q], j = rj[q];
+                const int64_t pu = (int64_t)i * n - (int64_t)i * (i - 1) / 2 + (j - i);
+                *reinterpret_cast<float4*>(HP + (((int64_t)l * B + b) * npair_u + pu) * 32 + 4 * fg) =
+                    make_float4(hn[0], hn[1], hn[2], hn[3]);
+            }
+        }
+        cur ^= 1;
+    }
+}
+
+// Value-only el-ion stream: rows (walker, electron, ion); HE[l][row][32] for levels 0..3
+// (level 0 the input [d, dx, dy, dz]); padding ions (Z = 0) give zero rows.
+__global__ void __launch_bounds__(128)
+k_ei_mlp(const float* __restrict__ r, const float* __restrict__ Rall, const int32_t* __restrict__ Zall,
+         const float* __restrict__ P, ParamLayout L, Dims d, int B, float* __restrict__ HE) {
+    __shared__ __align__(16) MlpSmem sm;
+    __shared__ int rok[kRB];
+    const int tid = threadIdx.x;
+    const int nei = d.n * d.N;
+    const int64_t total = (int64_t)B * nei;
+    const int64_t g0 = (int64_t)blockIdx.x * kRB;
+    for (int q = tid; q < kRB; q += blockDim.x) {
+        const int64_t g = g0 + q;
+        float f4[4] = {0.f, 0.f, 0.f, 0.f};
+        int ok = 0;
+        if (g < total) {
+            const int b = (int)(g / nei), p = (int)(g % nei), i = p / d.N, I = p % d.N;
+            const int sg = seg_of(d, b);
+            if (Zall[(size_t)sg * d.N + I] > 0) {
+                const float* R = Rall + (size_t)sg * d.N * 3;
+                const float* rr = r + ((int64_t)b * d.n + i) * 3;
+                f4[1] = rr[0] - R[I * 3]; f4[2] = rr[1] - R[I * 3 + 1]; f4[3] = rr[2] - R[I * 3 + 2];
+                f4[0] = sqrtf(f4[1] * f4[1] + f4[2] * f4[2] + f4[3] * f4[3]);   // [d, dx, dy, dz]
+                ok = 1;
+            } else {
+                ok = 2;                  // padding ion: zero rows at every level
+            }
+        }
+        rok[q] = ok;
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) sm.H[0][k][q] = f4[k];
+    }
+    __syncthreads();
+    const int rg = tid >> 3, fg = tid & 7;
+    // level 0: the input features, zero padded to 32
+    for (int e = tid; e < kRB * 8; e += blockDim.x) {
+        const int q = e / 8, f0 = (e % 8) * 4;
+        if (!rok[q]) continue;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (f0 == 0) v = make_float4(sm.H[0][0][q], sm.H[0][1][q], sm.H[0][2][q], sm.H[0][3][q]);
+        *reinterpret_cast<float4*>(HE + (g0 + q) * 32 + f0) = v;
+    }
+    const float rs = 0.70710678118654752f;
+    int cur = 0;
+    for (int l = 0; l < 3; ++l) {
+        const int in_w = d.eiw[l];
+        __syncthreads();
+        mlp_load_w(sm, P + L.h_ei_w[l], P + L.h_ei_b[l], in_w);
+        __syncthreads();
+        float z[4][4];
+        mlp_tile(sm, cur, in_w, rg, fg, z);
+        #pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+            const int q = 4 * rg + rr;
+            float hn[4];
+            #pragma unroll
+            for (int ff = 0; ff < 4; ++ff) {
+                const int f = 4 * fg + ff;
+                const float y = tanhf(z[rr][ff]);
+                hn[ff] = rok[q] == 2 ? 0.f : (l > 0 ? (sm.H[cur][f][q] + y) * rs : y);
+                sm.H[cur ^ 1][f][q] = hn[ff];
+            }
+            if (rok[q])
+                *reinterpret_cast<float4*>(HE + ((int64_t)(l + 1) * total + g0 + q) * 32 + 4 * fg) =
+                    make_float4(hn[0], hn[1], hn[2], hn[3]);
+        }
+        cur ^= 1;
+    }
+}
+
 template <int CH>
 __global__ void __launch_bounds__(128)
 k_ei_streams(const float* __restrict__ r, const float* __restrict__ R, const int32_t* __restrict__ Z,
@@ -728,9 +926,11 @@ void launch_streams(const float* r, const float* R, const int32_t* Z, const floa
         k_pair_streams<3><<<blocks(npair), 128, sm3, s>>>(r, P, L, d, B, WP, nullptr);
         k_ei_streams<5><<<blocks(nei), 128, sm5, s>>>(r, R, Z, P, L, d, B, HE);
     } else {
-        size_t sm1 = 128 * (32 + 1) * sizeof(float);
-        k_pair_streams<1><<<blocks(npair), 128, sm1, s>>>(r, P, L, d, B, WP, HP);
-        k_ei_streams<1><<<blocks(nei), 128, sm1, s>>>(r, R, Z, P, L, d, B, HE);
+        const int64_t same_rows = (int64_t)B * (d.nu * (d.nu + 1) / 2 + d.nd * (d.nd + 1) / 2);
+        const int64_t diff_rows = (int64_t)B * d.nu * d.nd;
+        const int bs = (int)((same_rows + kRB - 1) / kRB), bd = (int)((diff_rows + kRB - 1) / kRB);
+        k_pair_mlp<<<bs + bd, 128, 0, s>>>(r, P, L, d, B, bs, WP, HP);
+        k_ei_mlp<<<(unsigned)((nei + kRB - 1) / kRB), 128, 0, s>>>(r, R, Z, P, L, d, B, HE);
     }
     count_launch(2);
 }

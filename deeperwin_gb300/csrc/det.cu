@@ -186,6 +186,19 @@ k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, double* __re
 // step the rows shift one column to the left, so the pivot column is always register a[0] and
 // every register index is static (the pivot loop itself is not unrolled). The pivot product is
 // kept as a mantissa and a binary exponent (frexp), with one log per matrix.
+// 1/d by Newton-Raphson iteration x <- x + x (1 - d x), seeded with the approximate FP32
+// reciprocal (about 2^-22 relative); each step squares the relative error, so two steps reach
+// FP64 precision. Divisions stay exact outside the FP32 exponent range.
+__device__ __forceinline__ double recip_nr(double d) {
+    const double ad = fabs(d);
+    if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
+    double x = (double)__fdividef(1.0f, (float)d);
+    x = fma(x, fma(-d, x, 1.0), x);
+    x = fma(x, fma(-d, x, 1.0), x);
+    return x;
+}
+__device__ __forceinline__ float recip_nr(float d) { return 1.0f / d; }
+
 template <class S> __device__ __forceinline__ int mag_key(S v);
 template <> __device__ __forceinline__ int mag_key<double>(double v) { return __double2hiint(v) & 0x7fffffff; }
 template <> __device__ __forceinline__ int mag_key<float>(float v) { return __float_as_int(v) & 0x7fffffff; }
@@ -245,7 +258,7 @@ k_slogdet_rows(const float* __restrict__ MO, int n, int T, int nmat, double* __r
         expo += e;
         if (pk < (S)0) sg = -sg;
         const bool below = r > k;
-        const S l = below ? a[0] / pk : (S)0;
+        const S l = below ? a[0] * recip_nr(pk) : (S)0;
         #pragma unroll
         for (int c = 1; c < NMAX; ++c) {
             if (c >= rem) break;
@@ -280,11 +293,14 @@ void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, 
         const int teams = 32 / n;
         const int64_t warps = (nmat + teams - 1) / teams;
         const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
-        if (!want_inv && n > 16) {
-            // rows in lanes beyond 16 electrons (the column form's unrolled register arrays
-            // no longer stay in registers there)
+        if (!want_inv) {
             auto rows = [&](auto kern) { kern<<<blocks, 128, 0, s>>>(MO, n, d.T, nmat, logdet, sign); };
-            if (n <= 24) rows(k_slogdet_rows<S, 24>);
+            if (n <= 4) rows(k_slogdet_rows<S, 4>);
+            else if (n <= 8) rows(k_slogdet_rows<S, 8>);
+            else if (n <= 10) rows(k_slogdet_rows<S, 10>);
+            else if (n <= 12) rows(k_slogdet_rows<S, 12>);
+            else if (n <= 16) rows(k_slogdet_rows<S, 16>);
+            else if (n <= 24) rows(k_slogdet_rows<S, 24>);
             else rows(k_slogdet_rows<S, 32>);
             count_launch();
             return;

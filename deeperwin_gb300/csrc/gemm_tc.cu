@@ -104,6 +104,12 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 // 16-byte chunk j of row r in a 128-byte-swizzled staging tile (1024-byte aligned).
 __device__ __forceinline__ uint32_t swz(int r, int j) { return (uint32_t)(r * 128 + ((j ^ (r & 7)) << 4)); }
 
+// Forward-Laplacian scratch per epilogue warp: five per-column arrays for up to four electron
+// groups (value-row z, sum of squared gradient rows, and the row coefficients d1 = 1 - tanh^2,
+// y0 = tanh(z0), cl = -2 y0 d1 sum), pitch kFlP floats (16-byte aligned), then a zero row.
+constexpr int kFlP = 68;
+constexpr int kFlWarp = 5 * 4 * kFlP + 64;
+
 struct TcArgs {
     int M, N, K, BN;
     GemmEpi epi;
@@ -132,8 +138,8 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
     auto sB = [&](int s, int part) { return smem + (size_t)s * stage_bytes + (size_t)NP * a_bytes + (size_t)part * b_bytes; };
     uint8_t* stage_out = smem + (size_t)S * stage_bytes;                   // [4 warps][SWB]
     float* xchg = reinterpret_cast<float*>(stage_out + 4 * SWB);           // [2 bufs][2 arrays][4][64]
-    float* flbuf = xchg + 2 * 2 * 4 * 64;                                  // [4 warps][4 arrays][4 groups][65]
-    uint64_t* full = reinterpret_cast<uint64_t*>(flbuf + 4 * 4 * 4 * 65);
+    float* flbuf = xchg + 2 * 2 * 4 * 64;                                  // [4 warps][kFlWarp]
+    uint64_t* full = reinterpret_cast<uint64_t*>(flbuf + 4 * kFlWarp);
     uint64_t* empty = full + S;
     uint64_t* tfull = empty + S;     // [2]
     uint64_t* tempty = tfull + 2;    // [2]
@@ -283,33 +289,33 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                 #pragma unroll
                 for (int j = 0; j < CW; ++j) v[j] += rbv[j];
                 if (a.fl) {
-                    // Forward-Laplacian tanh over the Tp channel rows of each electron. Column sums
-                    // of z_t^2 over the gradient rows and tanh of the value row are formed per
-                    // column through a shared-memory transpose (the staging tile is free here:
-                    // the previous TMA store has finished reading it).
+                    // Forward-Laplacian tanh over the Tp channel rows of each electron:
+                    // y_0 = tanh(z_0), y_t = d1 z_t (gradients), y_lap = d1 z_lap - 2 y0 d1 sum_t z_t^2,
+                    // d1 = 1 - y0^2. The column sums and the value row are formed per column through
+                    // shared memory (the staging tile is free here: the previous TMA store has finished
+                    // reading it); each row then takes y = alpha v + beta with per-column coefficient
+                    // rows chosen once by its row type.
                     if (lane == 0) bulk_wait_read0();
                     __syncwarp();
                     float* sq = reinterpret_cast<float*>(my_out);          // [32 rows][CW] swizzled by 16 B chunks
-                    float* fb = flbuf + (size_t)q * 4 * 4 * 65;            // [array][group][65]
-                    float* Z0 = fb;              // value-row z per group
-                    float* SS = fb + 4 * 65;     // sum of squares per group
-                    float* Y0 = fb + 8 * 65;     // tanh(z0)
-                    float* D1 = fb + 12 * 65;    // 1 - tanh^2
-                    #pragma unroll
-                    for (int j4 = 0; j4 < CW / 4; ++j4) {
-                        float4 x;
-                        x.x = is_grad ? v[4 * j4] * v[4 * j4] : 0.f;
-                        x.y = is_grad ? v[4 * j4 + 1] * v[4 * j4 + 1] : 0.f;
-                        x.z = is_grad ? v[4 * j4 + 2] * v[4 * j4 + 2] : 0.f;
-                        x.w = is_grad ? v[4 * j4 + 3] * v[4 * j4 + 3] : 0.f;
-                        *reinterpret_cast<float4*>(sq + lane * CW + ((j4 ^ (lane & 7)) << 2)) = x;
-                    }
+                    float* fb = flbuf + (size_t)q * kFlWarp;
+                    float* Z0 = fb;                                       // [group][kFlP]
+                    float* SS = fb + 4 * kFlP;
+                    float* D1 = fb + 8 * kFlP;
+                    float* Y0 = fb + 12 * kFlP;
+                    float* CL = fb + 16 * kFlP;
+                    float* ZR = fb + 20 * kFlP;                           // zero row
                     const int G = Tp < 32 ? 32 / Tp : 1;                    // electron groups in this warp
                     const int grp = Tp < 32 ? lane / Tp : 0;
-                    if (is_val) {
-                        #pragma unroll
-                        for (int j = 0; j < CW; ++j) Z0[grp * 65 + j] = v[j];
+                    #pragma unroll
+                    for (int j4 = 0; j4 < CW / 4; ++j4) {
+                        const float4 x4 = make_float4(v[4 * j4], v[4 * j4 + 1], v[4 * j4 + 2], v[4 * j4 + 3]);
+                        const float4 s4 = is_grad ? make_float4(x4.x * x4.x, x4.y * x4.y, x4.z * x4.z, x4.w * x4.w)
+                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+                        *reinterpret_cast<float4*>(sq + lane * CW + ((j4 ^ (lane & 7)) << 2)) = s4;
+                        if (is_val) *reinterpret_cast<float4*>(Z0 + grp * kFlP + 4 * j4) = x4;
                     }
+                    if (lane < CW / 4) reinterpret_cast<float4*>(ZR)[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
                     __syncwarp();
                     const int rpg = Tp < 32 ? Tp : 32;                      // rows of a group inside this warp
                     #pragma unroll
@@ -317,9 +323,10 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                         const int c = lane + 32 * h;
                         for (int g = 0; g < G; ++g) {
                             float acc = 0.f;
+                            #pragma unroll 8
                             for (int rr = g * rpg; rr < (g + 1) * rpg; ++rr)
                                 acc += sq[rr * CW + ((((c >> 2) ^ (rr & 7))) << 2) + (c & 3)];
-                            SS[g * 65 + c] = acc;
+                            SS[g * kFlP + c] = acc;
                         }
                     }
                     if (Tp > 32) {
@@ -347,17 +354,26 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                     for (int h = 0; h < CW / 32; ++h) {
                         const int c = lane + 32 * h;
                         for (int g = 0; g < G; ++g) {
-                            const float y0 = tanhf(Z0[g * 65 + c]);
-                            Y0[g * 65 + c] = y0;
-                            D1[g * 65 + c] = 1.f - y0 * y0;
+                            const float y0 = tanhf(Z0[g * kFlP + c]);
+                            const float d1 = 1.f - y0 * y0;
+                            Y0[g * kFlP + c] = y0;
+                            D1[g * kFlP + c] = d1;
+                            CL[g * kFlP + c] = -2.f * y0 * d1 * SS[g * kFlP + c];
                         }
                     }
                     __syncwarp();
+                    // row type -> coefficient rows: value (0, y0), gradient (d1, 0), Laplacian
+                    // (d1, cl), padding channels (0, 0)
+                    const float* al = (is_grad || is_lap) ? D1 + grp * kFlP : ZR;
+                    const float* be = is_val ? Y0 + grp * kFlP : (is_lap ? CL + grp * kFlP : ZR);
                     #pragma unroll
-                    for (int j = 0; j < CW; ++j) {
-                        const float y0 = Y0[grp * 65 + j], d1 = D1[grp * 65 + j], ssum = SS[grp * 65 + j];
-                        const float g = d1 * v[j];
-                        v[j] = is_val ? y0 : (is_lap ? g - 2.f * y0 * d1 * ssum : (is_grad ? g : 0.f));
+                    for (int j4 = 0; j4 < CW / 4; ++j4) {
+                        const float4 a4 = *reinterpret_cast<const float4*>(al + 4 * j4);
+                        const float4 b4 = *reinterpret_cast<const float4*>(be + 4 * j4);
+                        v[4 * j4] = fmaf(a4.x, v[4 * j4], b4.x);
+                        v[4 * j4 + 1] = fmaf(a4.y, v[4 * j4 + 1], b4.y);
+                        v[4 * j4 + 2] = fmaf(a4.z, v[4 * j4 + 2], b4.z);
+                        v[4 * j4 + 3] = fmaf(a4.w, v[4 * j4 + 3], b4.w);
                     }
                     __syncwarp();
                 } else if (e.act == 1) {
@@ -378,13 +394,12 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                         uint32_t hw_[4], lw_[4];
                         #pragma unroll
                         for (int k = 0; k < 4; ++k) {
-                            float x0 = v[8 * j + 2 * k], x1 = v[8 * j + 2 * k + 1];
-                            __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
-                            hw_[k] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                            const float x0 = v[8 * j + 2 * k], x1 = v[8 * j + 2 * k + 1];
+                            const __nv_bfloat162 hh = __floats2bfloat162_rn(x0, x1);
+                            hw_[k] = *reinterpret_cast<const uint32_t*>(&hh);
                             if (OUT == 2) {
-                                __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
-                                __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
-                                lw_[k] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                                const __nv_bfloat162 ll = __floats2bfloat162_rn(x0 - __low2float(hh), x1 - __high2float(hh));
+                                lw_[k] = *reinterpret_cast<const uint32_t*>(&ll);
                             } else {
                                 lw_[k] = 0u;
                             }
@@ -499,7 +514,7 @@ int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __
     a.M = M; a.N = N; a.K = K; a.BN = BN; a.epi = epi; a.fl = fl; a.n3 = n3;
     const int stage_bytes = NP * (BM * BK * 2 + BN * BK * 2);
     const int swb = OUT == 0 ? 4096 : 8192;
-    const int fixed = 1024 + 4 * swb + 2 * 2 * 4 * 64 * 4 + 4 * 4 * 4 * 65 * 4 + 256;
+    const int fixed = 1024 + 4 * swb + 2 * 2 * 4 * 64 * 4 + 4 * kFlWarp * 4 + 256;
     a.stages = std::min(8, (220 * 1024 - fixed) / stage_bytes);
     if (a.stages < 2) return DW_ERR_ARCH;
     a.tmem_cols = 32;

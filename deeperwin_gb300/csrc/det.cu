@@ -274,6 +274,107 @@ k_slogdet_rows(const float* __restrict__ MO, int n, int T, int nmat, double* __r
     }
 }
 
+// Value-only FP64 log|det| with one matrix per thread. On this part FP64 arithmetic issues at
+// a small fraction of the FP32 rate, so the LU is bound by the number of FP64 instructions;
+// giving each thread a whole matrix issues exactly the (n-k-1)^2 trailing-update FMAs and
+// (n-k-1) multiplier products of pivot k, plus one reciprocal and one mantissa product per
+// pivot -- with no lanes idling above the pivot and no per-lane copies of the per-pivot
+// work (about a quarter of the FP64 instructions of the rows-in-lanes form).
+// The matrices live in shared memory, element (i, j) of thread t at
+// sm[(i * NMAX + j) * LD + t] with LD = TPB + 1: accesses of one element by all threads are
+// consecutive words, and the odd stride keeps the cooperative staging of the row-major input
+// free of bank conflicts. Partial pivoting takes the first row of maximal |a_ik| at or below
+// the diagonal (as LAPACK getrf), comparing the full 64-bit magnitude patterns; rows are
+// exchanged physically, so ties are resolved in the current row order exactly as getrf does.
+// The pivot product is kept as a mantissa in [0.5, 1) and a binary exponent, normalised with
+// integer operations, and one log is taken per matrix.
+__device__ __forceinline__ double mant_mul_norm(double mant, double a, int& expo) {
+    double m = mant * a;                                  // a = |pivot| > 0, mant in [0.5, 1)
+    const int hi = __double2hiint(m), lo = __double2loint(m);
+    const int eb = (hi >> 20) & 0x7ff;
+    if (eb == 0 || eb == 0x7ff) {                         // subnormal / overflow: library frexp
+        int e;
+        m = frexp(m, &e);
+        expo += e;
+        return m;
+    }
+    expo += eb - 1022;
+    return __hiloint2double((hi & 0x800fffff) | 0x3fe00000, lo);
+}
+
+template <int NMAX, int TPB>
+__global__ void __launch_bounds__(TPB)
+k_slogdet_thread(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
+                 double* __restrict__ sign) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int LD = TPB + 1;
+    double* sm = reinterpret_cast<double*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int mat0 = blockIdx.x * TPB;
+    const int nm = min(TPB, nmat - mat0);
+    const int nn = n * n;
+    // cooperative staging: matrix m of the block is n*n contiguous floats at MO + (mat0+m) T n^2
+    for (int q = tid; q < nm * nn; q += TPB) {
+        const int m = q / nn, e = q - m * nn;
+        const int i = e / n, j = e - i * n;
+        sm[(i * NMAX + j) * LD + m] = (double)__ldg(MO + (int64_t)(mat0 + m) * T * nn + e);
+    }
+    __syncthreads();
+    if (tid >= nm) return;
+    double* a = sm + tid;
+    auto at = [&](int i, int j) -> double& { return a[(i * NMAX + j) * LD]; };
+    double mant = 1.0, sg = 1.0;
+    int expo = 0;
+    bool singular = false;
+    #pragma unroll 1
+    for (int k = 0; k < n; ++k) {
+        // pivot search on 64-bit magnitude patterns (non-negative doubles order as integers)
+        long long best = __double_as_longlong(at(k, k)) & 0x7fffffffffffffffll;
+        int p = k;
+        #pragma unroll 1
+        for (int i = k + 1; i < n; ++i) {
+            const long long v = __double_as_longlong(at(i, k)) & 0x7fffffffffffffffll;
+            if (v > best) { best = v; p = i; }
+        }
+        if (best == 0) { singular = true; break; }
+        if (p != k) {
+            #pragma unroll 1
+            for (int j = k; j < n; ++j) { const double t = at(k, j); at(k, j) = at(p, j); at(p, j) = t; }
+            sg = -sg;
+        }
+        const double pk = at(k, k);
+        if (pk < 0.0) sg = -sg;
+        mant = mant_mul_norm(mant, fabs(pk), expo);
+        const double rp = recip_nr(pk);
+        const int rem = n - k - 1;                       // trailing columns k+1 .. n-1
+        double u[NMAX - 1];
+        #pragma unroll
+        for (int c = 0; c < NMAX - 1; ++c) {
+            if (c >= rem) break;
+            u[c] = at(k, k + 1 + c);
+        }
+        #pragma unroll 1
+        for (int i = k + 1; i < n; ++i) {
+            double* row = &at(i, k);
+            const double l = row[0] * rp;
+            #pragma unroll
+            for (int c = 0; c < NMAX - 1; ++c) {
+                if (c >= rem) break;
+                row[(c + 1) * LD] = fma(-l, u[c], row[(c + 1) * LD]);
+            }
+        }
+    }
+    logdet[mat0 + tid] = singular ? -INFINITY : log(mant) + (double)expo * 0.69314718055994530942;
+    sign[mat0 + tid] = singular ? 0.0 : sg;
+}
+
+template <int NMAX, int TPB>
+static void launch_slogdet_thread(const float* MO, int n, int T, int nmat, double* logdet, double* sign, cudaStream_t s) {
+    const size_t smem = (size_t)NMAX * NMAX * (TPB + 1) * sizeof(double);
+    cudaFuncSetAttribute(k_slogdet_thread<NMAX, TPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_slogdet_thread<NMAX, TPB><<<(unsigned)((nmat + TPB - 1) / TPB), TPB, smem, s>>>(MO, n, T, nmat, logdet, sign);
+}
+
 template <class S>
 void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, int want_inv,
                          cudaStream_t s);
@@ -293,6 +394,15 @@ void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, 
         const int teams = 32 / n;
         const int64_t warps = (nmat + teams - 1) / teams;
         const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
+        if (!want_inv && std::is_same<S, double>::value && n <= 16) {
+            if (n <= 4) launch_slogdet_thread<4, 64>(MO, n, d.T, nmat, logdet, sign, s);
+            else if (n <= 8) launch_slogdet_thread<8, 64>(MO, n, d.T, nmat, logdet, sign, s);
+            else if (n <= 10) launch_slogdet_thread<10, 64>(MO, n, d.T, nmat, logdet, sign, s);
+            else if (n <= 12) launch_slogdet_thread<12, 64>(MO, n, d.T, nmat, logdet, sign, s);
+            else launch_slogdet_thread<16, 32>(MO, n, d.T, nmat, logdet, sign, s);
+            count_launch();
+            return;
+        }
         if (!want_inv) {
             auto rows = [&](auto kern) { kern<<<blocks, 128, 0, s>>>(MO, n, d.T, nmat, logdet, sign); };
             if (n <= 4) rows(k_slogdet_rows<S, 4>);

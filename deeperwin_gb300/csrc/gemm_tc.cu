@@ -104,11 +104,11 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 // 16-byte chunk j of row r in a 128-byte-swizzled staging tile (1024-byte aligned).
 __device__ __forceinline__ uint32_t swz(int r, int j) { return (uint32_t)(r * 128 + ((j ^ (r & 7)) << 4)); }
 
-// Forward-Laplacian scratch per epilogue warp: five per-column arrays for up to four electron
-// groups (value-row z, sum of squared gradient rows, and the row coefficients d1 = 1 - tanh^2,
-// y0 = tanh(z0), cl = -2 y0 d1 sum), pitch kFlP floats (16-byte aligned), then a zero row.
+// Forward-Laplacian scratch per epilogue warp: four per-column arrays for up to four electron
+// groups (value-row z and the coefficient rows d1 = 1 - tanh^2, y0 = tanh(z0),
+// cl = -2 y0 d1 sum_t z_t^2), pitch kFlP floats (16-byte aligned), then a zero row.
 constexpr int kFlP = 68;
-constexpr int kFlWarp = 5 * 4 * kFlP + 64;
+constexpr int kFlWarp = 4 * 4 * kFlP + 64;
 
 struct TcArgs {
     int M, N, K, BN;
@@ -129,7 +129,6 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr int CW = OUT == 0 ? 32 : 64;             // columns per staged store box (128 bytes per row)
-    constexpr int NPO = OUT == 2 ? 2 : 1;              // output parts
     constexpr int SWB = OUT == 0 ? 4096 : 8192;        // staging bytes per warp (also holds 32 x CW fp32)
     const int S = a.stages, BN = a.BN;
     const uint32_t a_bytes = BM * BK * 2, b_bytes = (uint32_t)BN * BK * 2;
@@ -239,22 +238,16 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
         for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++it) {
             const int m0 = (tile / a.n_tiles_n) * BM, n0 = (tile % a.n_tiles_n) * BN;
             const uint32_t acc = it & 1;
-            const bool ready = mbar_wait(&tfull[acc], (it >> 1) & 1);
-            if (!ready && lane == 0) s_epi_err = 1;
-            epi_bar();                               // all four epilogue warps agree before leaving
-            if (*(volatile int*)&s_epi_err) { if (lane == 0) atomicExch(&s_err, 1); break; }
-            tc_fence_after();
             const int row = q * 32 + lane;           // row within the tile
             const int m = m0 + row;
             const int t = m % Tp;
             const float* rb = (e.rowbias && m < a.M) ? e.rowbias + ((int64_t)(m / e.rows_per_walker) * Tp + t) * e.ldrb
                                                      : nullptr;
             const bool is_val = t == 0, is_grad = t >= 1 && t <= a.n3, is_lap = a.fl && t == a.n3 + 1;
-            for (int c0 = 0; c0 < BN; c0 += CW) {
-                float v[CW];
-                float rbv[CW];
-                // vectorized bias / row-bias loads for this chunk, issued before the TMEM reads
-                // (rows of one walker share their row-bias rows, so neighbouring warps hit in L1)
+            // bias / row-bias of one CW-column chunk (vectorized; rows of one walker share their
+            // row-bias rows, so neighbouring warps hit in L1)
+            float rbv[CW];
+            auto load_bias = [&](int c0) {
                 const bool full_chunk = n0 + c0 + CW <= a.N;
                 #pragma unroll
                 for (int j = 0; j < CW; j += 4) {
@@ -282,6 +275,20 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                     }
                     rbv[j] = x.x; rbv[j + 1] = x.y; rbv[j + 2] = x.z; rbv[j + 3] = x.w;
                 }
+            };
+            if (rb) {
+                // pull this row's row-bias segment into L1 while the accumulator is finished
+                for (int j = 0; j < BN && n0 + j < a.N; j += 32)
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(rb + n0 + j));
+            }
+            const bool ready = mbar_wait(&tfull[acc], (it >> 1) & 1);
+            if (!ready && lane == 0) s_epi_err = 1;
+            epi_bar();                               // all four epilogue warps agree before leaving
+            if (*(volatile int*)&s_epi_err) { if (lane == 0) atomicExch(&s_err, 1); break; }
+            tc_fence_after();
+            for (int c0 = 0; c0 < BN; c0 += CW) {
+                float v[CW];
+                load_bias(c0);                        // issued before the TMEM reads of this chunk
                 const uint32_t base = tmem + acc * (uint32_t)BN + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
                 #pragma unroll
                 for (int j = 0; j < CW; j += 16) tmem_ld16(base + j, v + j);
@@ -291,21 +298,21 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                 if (a.fl) {
                     // Forward-Laplacian tanh over the Tp channel rows of each electron:
                     // y_0 = tanh(z_0), y_t = d1 z_t (gradients), y_lap = d1 z_lap - 2 y0 d1 sum_t z_t^2,
-                    // d1 = 1 - y0^2. The column sums and the value row are formed per column through
-                    // shared memory (the staging tile is free here: the previous TMA store has finished
-                    // reading it); each row then takes y = alpha v + beta with per-column coefficient
-                    // rows chosen once by its row type.
+                    // d1 = 1 - y0^2. Gradient rows stage their squares in the swizzled staging tile (free
+                    // here: the previous TMA store has finished reading it) and the value row its value
+                    // in Z0. Lanes add float4 column chunks over 8-row blocks, the blocks of one electron
+                    // are combined in-lane, by shuffles or (Tp > 32) across warps, and the lane holding a
+                    // group's column sums writes that group's coefficient rows for its four columns.
+                    // Each row then takes y = alpha v + beta with coefficient rows chosen by its type.
                     if (lane == 0) bulk_wait_read0();
                     __syncwarp();
                     float* sq = reinterpret_cast<float*>(my_out);          // [32 rows][CW] swizzled by 16 B chunks
                     float* fb = flbuf + (size_t)q * kFlWarp;
                     float* Z0 = fb;                                       // [group][kFlP]
-                    float* SS = fb + 4 * kFlP;
-                    float* D1 = fb + 8 * kFlP;
-                    float* Y0 = fb + 12 * kFlP;
-                    float* CL = fb + 16 * kFlP;
-                    float* ZR = fb + 20 * kFlP;                           // zero row
-                    const int G = Tp < 32 ? 32 / Tp : 1;                    // electron groups in this warp
+                    float* D1 = fb + 4 * kFlP;
+                    float* Y0 = fb + 8 * kFlP;
+                    float* CL = fb + 12 * kFlP;
+                    float* ZR = fb + 16 * kFlP;                           // zero row
                     const int grp = Tp < 32 ? lane / Tp : 0;
                     #pragma unroll
                     for (int j4 = 0; j4 < CW / 4; ++j4) {
@@ -317,48 +324,76 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                     }
                     if (lane < CW / 4) reinterpret_cast<float4*>(ZR)[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
                     __syncwarp();
-                    const int rpg = Tp < 32 ? Tp : 32;                      // rows of a group inside this warp
+                    // lane (rb, jc): column chunk jc (columns 4 jc .. 4 jc + 3), rows [rb RPL, (rb + 1) RPL)
+                    constexpr int NCH = CW / 4, RPL = NCH, NS = RPL / 8;
+                    const int jc = lane % NCH, rbk = lane / NCH;
+                    float4 ps[NS];
                     #pragma unroll
-                    for (int h = 0; h < CW / 32; ++h) {
-                        const int c = lane + 32 * h;
-                        for (int g = 0; g < G; ++g) {
-                            float acc = 0.f;
-                            #pragma unroll 8
-                            for (int rr = g * rpg; rr < (g + 1) * rpg; ++rr)
-                                acc += sq[rr * CW + ((((c >> 2) ^ (rr & 7))) << 2) + (c & 3)];
-                            SS[g * kFlP + c] = acc;
-                        }
-                    }
-                    if (Tp > 32) {
-                        // a group spans several warps: exchange the partial sums and the value row
-                        float* xs = xchg + (size_t)xbuf * 2 * 4 * 64;
+                    for (int s8 = 0; s8 < NS; ++s8) {
+                        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
                         #pragma unroll
-                        for (int h = 0; h < CW / 32; ++h) {
-                            const int c = lane + 32 * h;
-                            xs[q * 64 + c] = SS[c];
-                            if ((q * 32) % Tp == 0) xs[4 * 64 + q * 64 + c] = Z0[c];   // this warp holds the value row
+                        for (int i = 0; i < 8; ++i) {
+                            const int r = rbk * RPL + 8 * s8 + i;            // r & 7 == i
+                            const float4 y = *reinterpret_cast<const float4*>(sq + r * CW + ((jc ^ i) << 2));
+                            x.x += y.x; x.y += y.y; x.z += y.z; x.w += y.w;
                         }
-                        epi_bar();
-                        const int qs = Tp / 32, g0 = (q / qs) * qs;
-                        #pragma unroll
-                        for (int h = 0; h < CW / 32; ++h) {
-                            const int c = lane + 32 * h;
-                            float acc = 0.f;
-                            for (int k = 0; k < qs; ++k) acc += xs[(g0 + k) * 64 + c];
-                            SS[c] = acc;
-                            Z0[c] = xs[4 * 64 + g0 * 64 + c];
-                        }
-                        xbuf ^= 1;   // the other exchange buffer is written only after the next barrier
+                        ps[s8] = x;
                     }
-                    #pragma unroll
-                    for (int h = 0; h < CW / 32; ++h) {
-                        const int c = lane + 32 * h;
-                        for (int g = 0; g < G; ++g) {
-                            const float y0 = tanhf(Z0[g * kFlP + c]);
-                            const float d1 = 1.f - y0 * y0;
-                            Y0[g * kFlP + c] = y0;
-                            D1[g * kFlP + c] = d1;
-                            CL[g * kFlP + c] = -2.f * y0 * d1 * SS[g * kFlP + c];
+                    auto coeffs = [&](int g, float4 ss, float4 z0) {
+                        const float y[4] = {tanhf(z0.x), tanhf(z0.y), tanhf(z0.z), tanhf(z0.w)};
+                        const float sv[4] = {ss.x, ss.y, ss.z, ss.w};
+                        float d1[4], cl[4];
+                        #pragma unroll
+                        for (int k = 0; k < 4; ++k) { d1[k] = 1.f - y[k] * y[k]; cl[k] = -2.f * y[k] * d1[k] * sv[k]; }
+                        *reinterpret_cast<float4*>(Y0 + g * kFlP + 4 * jc) = make_float4(y[0], y[1], y[2], y[3]);
+                        *reinterpret_cast<float4*>(D1 + g * kFlP + 4 * jc) = make_float4(d1[0], d1[1], d1[2], d1[3]);
+                        *reinterpret_cast<float4*>(CL + g * kFlP + 4 * jc) = make_float4(cl[0], cl[1], cl[2], cl[3]);
+                    };
+                    const int gsz = Tp < 32 ? Tp : 32;                      // rows of a group in this warp
+                    const int bpg = gsz / 8;                                // 8-row blocks per group
+                    if (bpg >= NS) {
+                        // all blocks of this lane lie in one group; add the lanes of the same group
+                        float4 g4 = ps[0];
+                        #pragma unroll
+                        for (int s8 = 1; s8 < NS; ++s8) { g4.x += ps[s8].x; g4.y += ps[s8].y; g4.z += ps[s8].z; g4.w += ps[s8].w; }
+                        for (int o = NCH; o < NCH * (bpg / NS); o <<= 1) {
+                            g4.x += __shfl_xor_sync(0xffffffffu, g4.x, o);
+                            g4.y += __shfl_xor_sync(0xffffffffu, g4.y, o);
+                            g4.z += __shfl_xor_sync(0xffffffffu, g4.z, o);
+                            g4.w += __shfl_xor_sync(0xffffffffu, g4.w, o);
+                        }
+                        const int g = (rbk * NS) / bpg;
+                        const bool holder = (rbk * NS) % bpg == 0;
+                        if (Tp <= 32) {
+                            if (holder) coeffs(g, g4, *reinterpret_cast<const float4*>(Z0 + g * kFlP + 4 * jc));
+                        } else {
+                            // a group spans several warps: exchange the partial sums and the value row
+                            float* xs = xchg + (size_t)xbuf * 2 * 4 * 64;
+                            const bool has_val = (q * 32) % Tp == 0;        // this warp holds the value row
+                            if (holder) {
+                                *reinterpret_cast<float4*>(xs + q * 64 + 4 * jc) = g4;
+                                if (has_val)
+                                    *reinterpret_cast<float4*>(xs + 4 * 64 + q * 64 + 4 * jc) =
+                                        *reinterpret_cast<const float4*>(Z0 + 4 * jc);
+                            }
+                            epi_bar();
+                            const int qs = Tp / 32, g0 = (q / qs) * qs;
+                            if (holder) {
+                                float4 tot = make_float4(0.f, 0.f, 0.f, 0.f);
+                                for (int k = 0; k < qs; ++k) {
+                                    const float4 pk = *reinterpret_cast<const float4*>(xs + (g0 + k) * 64 + 4 * jc);
+                                    tot.x += pk.x; tot.y += pk.y; tot.z += pk.z; tot.w += pk.w;
+                                }
+                                coeffs(0, tot, *reinterpret_cast<const float4*>(xs + 4 * 64 + g0 * 64 + 4 * jc));
+                            }
+                            xbuf ^= 1;   // the other exchange buffer is written only after the next barrier
+                        }
+                    } else {
+                        // one 8-row block per group (Tp = 8 with 16 rows per lane)
+                        #pragma unroll
+                        for (int s8 = 0; s8 < NS; ++s8) {
+                            const int g = rbk * NS + s8;
+                            coeffs(g, ps[s8], *reinterpret_cast<const float4*>(Z0 + g * kFlP + 4 * jc));
                         }
                     }
                     __syncwarp();

@@ -106,17 +106,19 @@ def peaks():
 
 
 def profile_traffic(name: str):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    """(DRAM bytes, algorithmic bytes) of the launch captured in the committed ncu summary."""
     f = ROOT / "profiles" / name
     if not f.exists():
-        return None
+        return None, None
+    vals = {}
     for line in f.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch_full_workload:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+        for key in ("traffic_bytes_per_launch_full_workload:", "algorithmic_bytes_captured_launch:"):
+            if line.startswith(key):
+                try:
+                    vals[key] = float(line.split(":", 1)[1].split()[0])
+                except ValueError:
+                    pass
+    return vals.get("traffic_bytes_per_launch_full_workload:"), vals.get("algorithmic_bytes_captured_launch:")
 
 
 def run_ours(args, rank, world, dev):
@@ -246,11 +248,20 @@ def run_ours(args, rank, world, dev):
             tfs = kt["flops"] / kt["launches"] / t_launch / 1e12
             intensity = kt["flops"] / kt["bytes"]
             ridge = pk["bf16_tflops"] * 1e12 / (pk["hbm_gbs"] * 1e9)
-            traffic = profile_traffic("layer_gemm_h10.txt")
+            # ncu traffic of one captured layer-1 launch, scaled to the average launch by the ratio of
+            # algorithmic bytes (DRAM traffic grows in proportion to the rows and K of a launch)
+            cap_traffic, cap_alg = profile_traffic("layer_gemm_h10.txt") if w.name.startswith("h10") else (None, None)
+            traffic = (round(cap_traffic / cap_alg * kt["bytes"] / kt["launches"])
+                       if cap_traffic and cap_alg else None)
             if intensity < ridge:
-                roof = {"kernel": "layer_gemm (tcgen05 split-BF16, forward-Laplacian h_el layers)", "bound": "hbm",
+                kname = {"mixed": "layer_gemm (tcgen05 split-BF16, forward-Laplacian h_el layers)",
+                         "bf16": "layer_gemm (tcgen05 BF16, forward-Laplacian h_el layers)",
+                         "fp32": "layer_gemm (FP32 CUDA-core GEMM + forward-Laplacian tanh, h_el layers)"}[w.precision]
+                roof = {"kernel": kname, "bound": "hbm",
                         "achieved": round(gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                         "frac": round(gbs / pk["hbm_gbs"], 4), "traffic": traffic,
+                        "traffic_source": ("ncu dram read+write of the h_el layer-1 launch (profiles/layer_gemm_h10.txt), "
+                                           "scaled to the average launch by algorithmic bytes") if traffic else None,
                         "algorithmic_bytes_per_launch": kt["bytes"] / kt["launches"],
                         "avg_launch_ms": t_launch * 1e3, "tflops": round(tfs, 2),
                         "peak_source": pk_kind}

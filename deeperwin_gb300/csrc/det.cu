@@ -6,6 +6,40 @@
 namespace dw {
 
 // ------------------------------------------------------------------ slogdet (+ inverse)
+// Shared FP64 helpers of the LU kernels.
+// 1/d by Newton-Raphson iteration x <- x + x (1 - d x), seeded with the approximate FP32
+// reciprocal (about 2^-22 relative); each step squares the relative error, so two steps reach
+// FP64 precision. Divisions stay exact outside the FP32 exponent range.
+__device__ __forceinline__ double recip_nr(double d) {
+    const double ad = fabs(d);
+    if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
+    double x = (double)__fdividef(1.0f, (float)d);
+    x = fma(x, fma(-d, x, 1.0), x);
+    x = fma(x, fma(-d, x, 1.0), x);
+    return x;
+}
+__device__ __forceinline__ float recip_nr(float d) { return 1.0f / d; }
+
+template <class S> __device__ __forceinline__ int mag_key(S v);
+template <> __device__ __forceinline__ int mag_key<double>(double v) { return __double2hiint(v) & 0x7fffffff; }
+template <> __device__ __forceinline__ int mag_key<float>(float v) { return __float_as_int(v) & 0x7fffffff; }
+
+// Multiplies the pivot-product mantissa by |pivot| and renormalises it to [0.5, 1) with
+// integer operations on the exponent field (the library frexp only for subnormal / overflow).
+__device__ __forceinline__ double mant_mul_norm(double mant, double a, int& expo) {
+    double m = mant * a;                                  // a = |pivot| > 0, mant in [0.5, 1)
+    const int hi = __double2hiint(m), lo = __double2loint(m);
+    const int eb = (hi >> 20) & 0x7ff;
+    if (eb == 0 || eb == 0x7ff) {                         // subnormal / overflow: library frexp
+        int e;
+        m = frexp(m, &e);
+        expo += e;
+        return m;
+    }
+    expo += eb - 1022;
+    return __hiloint2double((hi & 0x800fffff) | 0x3fe00000, lo);
+}
+
 // One warp per (walker, determinant). Gauss-Jordan elimination with partial pivoting
 // (first maximal |pivot| wins, as LAPACK getrf) on [A | I] in scalar type S; in value-only
 // mode an LU elimination on A alone. Mirrors jnp.linalg.slogdet in
@@ -111,16 +145,19 @@ k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, double* __re
     for (int k = 0; k < NMAX; ++k) {
         if (k >= n) break;
         const int owner = src_base + k;
-        // pivot search in FP32 magnitudes (first maximum wins; only the owner's result is used)
-        float best = -1.f; int p = k;
+        // pivot search on magnitude bit patterns (non-negative IEEE values order as integers; no
+        // FP64 instructions), first maximum wins; only the owner's result is used
+        long long best = -1; int p = k;
         #pragma unroll
         for (int r = k; r < NMAX; ++r) {
-            const float v = fabsf((float)col[r]);
+            const long long v = std::is_same<S, double>::value
+                                    ? (__double_as_longlong((double)col[r]) & 0x7fffffffffffffffll)
+                                    : (long long)(__float_as_int((float)col[r]) & 0x7fffffff);
             if (r < n && v > best) { best = v; p = r; }
         }
         p = __shfl_sync(0xffffffffu, p, owner);
         best = __shfl_sync(0xffffffffu, best, owner);
-        bool sing_now = !(best > 0.f);
+        bool sing_now = !(best > 0);
         if (p != k) {
             S xk = col[k], xp = 0, ik = INV ? icol[k] : (S)0, ip = 0;
             #pragma unroll
@@ -136,13 +173,9 @@ k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, double* __re
         singular = singular || sing_now;
         if (sing_now) pk = (S)1;
         S inv = 0;
-        if (c == k) inv = (S)1 / pk;
+        if (c == k) inv = recip_nr(pk);
         inv = __shfl_sync(0xffffffffu, inv, owner);
-        int e;
-        mant *= frexp(fabs((double)pk), &e);
-        expo += e;
-        mant = frexp(mant, &e);
-        expo += e;
+        mant = mant_mul_norm(mant, fabs((double)pk), expo);
         if (pk < (S)0) sg = -sg;
         if (INV) {
             // Gauss-Jordan: scale row k, eliminate all other rows with the broadcast column-k entries
@@ -186,23 +219,6 @@ k_slogdet_reg(const float* __restrict__ MO, int n, int T, int nmat, double* __re
 // step the rows shift one column to the left, so the pivot column is always register a[0] and
 // every register index is static (the pivot loop itself is not unrolled). The pivot product is
 // kept as a mantissa and a binary exponent (frexp), with one log per matrix.
-// 1/d by Newton-Raphson iteration x <- x + x (1 - d x), seeded with the approximate FP32
-// reciprocal (about 2^-22 relative); each step squares the relative error, so two steps reach
-// FP64 precision. Divisions stay exact outside the FP32 exponent range.
-__device__ __forceinline__ double recip_nr(double d) {
-    const double ad = fabs(d);
-    if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
-    double x = (double)__fdividef(1.0f, (float)d);
-    x = fma(x, fma(-d, x, 1.0), x);
-    x = fma(x, fma(-d, x, 1.0), x);
-    return x;
-}
-__device__ __forceinline__ float recip_nr(float d) { return 1.0f / d; }
-
-template <class S> __device__ __forceinline__ int mag_key(S v);
-template <> __device__ __forceinline__ int mag_key<double>(double v) { return __double2hiint(v) & 0x7fffffff; }
-template <> __device__ __forceinline__ int mag_key<float>(float v) { return __float_as_int(v) & 0x7fffffff; }
-
 template <class S, int NMAX>
 __global__ void __launch_bounds__(128)
 k_slogdet_rows(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
@@ -288,20 +304,6 @@ k_slogdet_rows(const float* __restrict__ MO, int n, int T, int nmat, double* __r
 // exchanged physically, so ties are resolved in the current row order exactly as getrf does.
 // The pivot product is kept as a mantissa in [0.5, 1) and a binary exponent, normalised with
 // integer operations, and one log is taken per matrix.
-__device__ __forceinline__ double mant_mul_norm(double mant, double a, int& expo) {
-    double m = mant * a;                                  // a = |pivot| > 0, mant in [0.5, 1)
-    const int hi = __double2hiint(m), lo = __double2loint(m);
-    const int eb = (hi >> 20) & 0x7ff;
-    if (eb == 0 || eb == 0x7ff) {                         // subnormal / overflow: library frexp
-        int e;
-        m = frexp(m, &e);
-        expo += e;
-        return m;
-    }
-    expo += eb - 1022;
-    return __hiloint2double((hi & 0x800fffff) | 0x3fe00000, lo);
-}
-
 template <int NMAX, int TPB>
 __global__ void __launch_bounds__(TPB)
 k_slogdet_thread(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
@@ -572,9 +574,127 @@ k_det_tangents_warp(const float* __restrict__ MO, const float* __restrict__ Ainv
     if (lane == 0) lapdet[mat] = lap_acc;
 }
 
+// Register-tiled determinant tangents, one block of 128 threads per (walker, determinant).
+// For every channel t: C_t = A^-1 D_t (D_t = channel t of the Slater matrix), g_t = tr C_t and,
+// for the 3n gradient channels, tr(C_t^2) = sum_aj C_aj C_ja. Each thread forms one 4 x 4 tile
+// of C_t from float4 shared-memory loads (16 FMAs per two 16-byte loads), stages it, reads the
+// transposed tile for its part of tr(C_t^2), and the tile partials (FP32 sums of 16 products)
+// are added in FP64 per channel; the Laplacian trace lap = tr(A^-1 Lap A) - sum_t tr(C_t^2) is
+// accumulated in FP64. Matrices are zero-padded to NP = round_up(n, 4) <= 32.
+template <int NP>
+__global__ void __launch_bounds__(128)
+k_det_tangents_tile(const float* __restrict__ MO, const float* __restrict__ Ainv, const double* __restrict__ sign,
+                    int n, int T, double* __restrict__ g, double* __restrict__ lapdet) {
+    constexpr int NB = NP / 4;                   // tile rows / columns
+    constexpr int TPC = NB * NB;                 // tiles (threads) per channel
+    constexpr int CPR = 128 / TPC;               // channels per round
+    constexpr int PP = NP * NP + 4;              // channel plane pitch (floats), offset to spread banks
+    __shared__ __align__(16) float AT[NP * NP];  // AT[k][a] = Ainv[a][k]
+    __shared__ __align__(16) float Ds[CPR * PP];
+    __shared__ double part[2][128];
+    __shared__ double tr1[3 * 32 + 2], tr2[3 * 32 + 2];
+    const int mat = blockIdx.x, tid = threadIdx.x;
+    if (sign[mat] == 0.0) {
+        for (int t = tid; t < 3 * n; t += 128) g[(int64_t)mat * 3 * n + t] = 0.0;
+        if (tid == 0) lapdet[mat] = 0.0;
+        return;
+    }
+    for (int e = tid; e < NP * NP; e += 128) {
+        const int k = e / NP, a = e % NP;
+        AT[e] = (k < n && a < n) ? __ldg(Ainv + (int64_t)mat * n * n + a * n + k) : 0.f;
+    }
+    const int c = tid / TPC, tile = tid % TPC, ab = tile / NB, jb = tile % NB;
+    const int nn = n * n;
+    for (int t0 = 1; t0 < T; t0 += CPR) {
+        const int nc = min(CPR, T - t0);
+        __syncthreads();                         // previous round's readers of Ds are done
+        // stage channels t0 .. t0 + nc - 1 (contiguous in MO), zero-padded to NP x NP
+        const float* src = MO + ((int64_t)mat * T + t0) * nn;
+        for (int e = tid; e < CPR * NP * NP; e += 128) {
+            const int cc = e / (NP * NP), r = e % (NP * NP), i = r / NP, j = r % NP;
+            Ds[cc * PP + r] = (cc < nc && i < n && j < n) ? __ldg(src + (int64_t)cc * nn + i * n + j) : 0.f;
+        }
+        __syncthreads();
+        float acc[4][4];
+        #pragma unroll
+        for (int x = 0; x < 4; ++x)
+            #pragma unroll
+            for (int y = 0; y < 4; ++y) acc[x][y] = 0.f;
+        const bool on = c < nc;
+        if (on) {
+            const float* dp = Ds + c * PP + 4 * jb;
+            const float* ap = AT + 4 * ab;
+            #pragma unroll 4
+            for (int k = 0; k < n; ++k) {
+                const float4 av = *reinterpret_cast<const float4*>(ap + k * NP);
+                const float4 dv = *reinterpret_cast<const float4*>(dp + k * NP);
+                const float a4[4] = {av.x, av.y, av.z, av.w}, d4[4] = {dv.x, dv.y, dv.z, dv.w};
+                #pragma unroll
+                for (int x = 0; x < 4; ++x)
+                    #pragma unroll
+                    for (int y = 0; y < 4; ++y) acc[x][y] = fmaf(a4[x], d4[y], acc[x][y]);
+            }
+        }
+        __syncthreads();                         // Ds is reused for C
+        if (on) {
+            float* cp = Ds + c * PP;
+            #pragma unroll
+            for (int x = 0; x < 4; ++x)
+                *reinterpret_cast<float4*>(cp + (4 * ab + x) * NP + 4 * jb) =
+                    make_float4(acc[x][0], acc[x][1], acc[x][2], acc[x][3]);
+        }
+        __syncthreads();
+        float p1 = 0.f, p2 = 0.f;
+        if (on) {
+            // transposed tile: C[4 jb + y][4 ab + x]
+            const float* cp = Ds + c * PP;
+            #pragma unroll
+            for (int y = 0; y < 4; ++y) {
+                const float4 ct = *reinterpret_cast<const float4*>(cp + (4 * jb + y) * NP + 4 * ab);
+                p2 = fmaf(acc[0][y], ct.x, p2);
+                p2 = fmaf(acc[1][y], ct.y, p2);
+                p2 = fmaf(acc[2][y], ct.z, p2);
+                p2 = fmaf(acc[3][y], ct.w, p2);
+            }
+            if (ab == jb) p1 = acc[0][0] + acc[1][1] + acc[2][2] + acc[3][3];
+        }
+        part[0][tid] = (double)p1;
+        part[1][tid] = (double)p2;
+        __syncthreads();
+        if (tid < nc) {
+            double s1 = 0.0, s2 = 0.0;
+            for (int q = 0; q < TPC; ++q) { s1 += part[0][tid * TPC + q]; s2 += part[1][tid * TPC + q]; }
+            tr1[t0 + tid] = s1;
+            tr2[t0 + tid] = s2;
+        }
+    }
+    __syncthreads();
+    for (int t = 1 + tid; t < T - 1; t += 128) g[(int64_t)mat * 3 * n + (t - 1)] = tr1[t];
+    if (tid < 32) {
+        double s = 0.0;
+        for (int t = 1 + tid; t < T - 1; t += 32) s += tr2[t];
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (tid == 0) lapdet[mat] = tr1[T - 1] - s;
+    }
+}
+
 void launch_det_tangents(const float* MO, const float* Ainv, const double* sign, const Dims& d, int B,
                          double* g, double* lapdet, cudaStream_t s) {
     int nmat = B * d.K;
+    if (d.n <= 32 && d.T == 3 * d.n + 2) {
+        auto go = [&](auto kern) { kern<<<nmat, 128, 0, s>>>(MO, Ainv, sign, d.n, d.T, g, lapdet); };
+        if (d.n <= 4) go(k_det_tangents_tile<4>);
+        else if (d.n <= 8) go(k_det_tangents_tile<8>);
+        else if (d.n <= 12) go(k_det_tangents_tile<12>);
+        else if (d.n <= 16) go(k_det_tangents_tile<16>);
+        else if (d.n <= 20) go(k_det_tangents_tile<20>);
+        else if (d.n <= 24) go(k_det_tangents_tile<24>);
+        else if (d.n <= 28) go(k_det_tangents_tile<28>);
+        else go(k_det_tangents_tile<32>);
+        count_launch();
+        return;
+    }
     if (d.n <= 32) {
         const int n = d.n, G = 32 / n, wpb = 4;
         const int ais = (n * n + 1) & ~1, cgs = ((n * (n + 1) > 4 * n ? n * (n + 1) : 4 * n) + 1) & ~1;
@@ -591,25 +711,28 @@ void launch_det_tangents(const float* MO, const float* Ainv, const double* sign,
 }
 
 // ------------------------------------------------------------------ Coulomb (hamiltonian.py:17-39)
+// Pair terms in FP32 (each difference of two FP32 coordinates is correctly rounded, so every
+// 1/r carries a few FP32 ulps of relative error, as in the reference's FP32 arithmetic), summed
+// in FP64.
 __device__ double coulomb_walker(const float* rb, int n, const float* R, const int32_t* Z, int N, int lane) {
     double e = 0.0;
     for (int p = lane; p < n * n; p += 32) {
         int i = p / n, j = p % n;
         if (j <= i) continue;
-        double dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
-        e += 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+        const float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
+        e += (double)(1.f / sqrtf(dx * dx + dy * dy + dz * dz));
     }
     for (int p = lane; p < n * N; p += 32) {
         int i = p / N, I = p % N;
         if (Z[I] <= 0) continue;                                  // padding ion
-        double dx = rb[i * 3] - R[I * 3], dy = rb[i * 3 + 1] - R[I * 3 + 1], dz = rb[i * 3 + 2] - R[I * 3 + 2];
-        e -= (double)Z[I] / sqrt(dx * dx + dy * dy + dz * dz);
+        const float dx = rb[i * 3] - R[I * 3], dy = rb[i * 3 + 1] - R[I * 3 + 1], dz = rb[i * 3 + 2] - R[I * 3 + 2];
+        e -= (double)((float)Z[I] / sqrtf(dx * dx + dy * dy + dz * dz));
     }
     for (int p = lane; p < N * N; p += 32) {
         int I = p / N, J = p % N;
         if (J <= I || Z[I] <= 0 || Z[J] <= 0) continue;
-        double dx = R[J * 3] - R[I * 3], dy = R[J * 3 + 1] - R[I * 3 + 1], dz = R[J * 3 + 2] - R[I * 3 + 2];
-        e += (double)Z[I] * Z[J] / sqrt(dx * dx + dy * dy + dz * dz);
+        const float dx = R[J * 3] - R[I * 3], dy = R[J * 3 + 1] - R[I * 3 + 1], dz = R[J * 3 + 2] - R[I * 3 + 2];
+        e += (double)((float)(Z[I] * Z[J]) / sqrtf(dx * dx + dy * dy + dz * dz));
     }
     return warp_sum(e);
 }
@@ -641,10 +764,18 @@ __global__ void k_combine(const double* __restrict__ logdet, const double* __res
     const int b = warp, K = d.K, n3 = 3 * d.n;
     const double* ld = logdet + (int64_t)b * K;
     const double* sg = sign + (int64_t)b * K;
+    // lane-parallel log-sum-exp over the determinants: first maximal log|det| (ties: lowest k)
     double lmax = -INFINITY; int ks = 0;
-    for (int k = 0; k < K; ++k) if (ld[k] > lmax) { lmax = ld[k]; ks = k; }
+    for (int k = lane; k < K; k += 32) if (ld[k] > lmax) { lmax = ld[k]; ks = k; }
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, lmax, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, ks, o);
+        if (ov > lmax || (ov == lmax && oi < ks)) { lmax = ov; ks = oi; }
+    }
     double psi = 0.0;
-    for (int k = 0; k < K; ++k) psi += sg[k] * exp(ld[k] - lmax);
+    for (int k = lane; k < K; k += 32) psi += sg[k] * exp(ld[k] - lmax);
+    psi = warp_sum(psi);
     const double eps = 1e-8;
     double u = fabs(psi), sgn = psi < 0 ? -1.0 : 1.0;
     double f = log(u + eps) + lmax;

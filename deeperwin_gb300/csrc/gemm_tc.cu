@@ -4,15 +4,17 @@
 //
 // * A and W are BF16 (NP = 1) or split-BF16 (NP = 2: x = hi + lo, three MMAs per K step:
 //   A_hi W_hi + A_hi W_lo + A_lo W_hi, all accumulated in FP32 in TMEM).
-// * Warp roles (192 threads): warp 0 = TMA producer, warp 1 = MMA issuer (one elected lane),
-//   warps 2-5 = epilogue (warp w drains TMEM lanes 32 (w % 4) .. +31).
+// * Warp roles (320 threads): warp 0 = TMA producer, warp 1 = MMA issuer (one elected lane),
+//   warps 2-9 = epilogue (warp w drains TMEM lanes 32 (w % 4) .. +31; the two warps of a lane
+//   quarter take alternate 32-column chunks).
 // * Shared-memory ring of S stages (128-byte swizzled K-major tiles), two TMEM accumulators
 //   so the epilogue of tile i overlaps the main loop of tile i + 1, one CTA per SM looping
 //   over output tiles.
 // * Epilogue: value-channel bias, per-(walker, channel) row bias, and either tanh on value
 //   rows or the forward-Laplacian tanh across the Tp channel rows of each electron
 //   (y = tanh z; y_t = (1 - y^2) z_t; y_lap = (1 - y^2) z_lap - 2 y (1 - y^2) sum_t z_t^2).
-//   Results are written to swizzled shared-memory staging tiles and stored with TMA.
+//   Results are written to swizzled shared-memory staging tiles (two per warp, so the staging
+//   of one chunk overlaps the TMA store of the previous one) and stored with TMA.
 // Every mbarrier wait is bounded; on timeout the kernel records an error flag, stops
 // issuing, waits (bounded) for its TMA loads in flight, frees its TMEM and returns.
 #include "gemm_tc.cuh"
@@ -28,7 +30,9 @@ __device__ int g_tc_error = 0;
 namespace {
 
 constexpr int BM = 128, BK = 64;
-constexpr int kThreads = 192;
+constexpr int kEpiWarps = 8;                         // two per TMEM lane quarter
+constexpr int kThreads = 64 + 32 * kEpiWarps;        // producer warp, MMA warp, epilogue warps
+constexpr int CW = 32;                               // columns per epilogue chunk / staged store box
 constexpr uint32_t kSpinLimit = 1u << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -64,10 +68,12 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void*
                  ::"l"(map), "r"(smem_u32(src)), "r"(c0), "r"(c1) : "memory");
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+// named barriers: 1 = all epilogue warps, 2 + h = the four epilogue warps of column half h
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(32 * kEpiWarps) : "memory"); }
+__device__ __forceinline__ void half_bar(int h) { asm volatile("bar.sync %0, 128;" ::"r"(2 + h) : "memory"); }
 
 // UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart.
 __device__ __forceinline__ uint64_t smem_desc_sw128(const void* p) {
@@ -101,14 +107,17 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// 16-byte chunk j of row r in a 128-byte-swizzled staging tile (1024-byte aligned).
+// 16-byte chunk j of row r in a 128-byte-swizzled staging tile (128-byte rows, 1024-byte aligned).
 __device__ __forceinline__ uint32_t swz(int r, int j) { return (uint32_t)(r * 128 + ((j ^ (r & 7)) << 4)); }
+// 16-byte chunk j (0..3) of row r in a 64-byte-swizzled staging tile (64-byte rows): the chunk
+// index is XORed with address bits 7-8, i.e. with (r >> 1) & 3.
+__device__ __forceinline__ uint32_t swz64(int r, int j) { return (uint32_t)(r * 64 + ((j ^ ((r >> 1) & 3)) << 4)); }
 
 // Forward-Laplacian scratch per epilogue warp: four per-column arrays for up to four electron
 // groups (value-row z and the coefficient rows d1 = 1 - tanh^2, y0 = tanh(z0),
 // cl = -2 y0 d1 sum_t z_t^2), pitch kFlP floats (16-byte aligned), then a zero row.
-constexpr int kFlP = 68;
-constexpr int kFlWarp = 4 * 4 * kFlP + 64;
+constexpr int kFlP = CW + 4;
+constexpr int kFlWarp = 4 * 4 * kFlP + CW;
 
 struct TcArgs {
     int M, N, K, BN;
@@ -128,17 +137,16 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
           const __grid_constant__ CUtensorMap tmC0, const __grid_constant__ CUtensorMap tmC1, TcArgs a) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    constexpr int CW = OUT == 0 ? 32 : 64;             // columns per staged store box (128 bytes per row)
-    constexpr int SWB = OUT == 0 ? 4096 : 8192;        // staging bytes per warp (also holds 32 x CW fp32)
+    constexpr int SWB = 4096;                          // staging bytes per buffer (32 x CW fp32, or BF16 hi + lo)
     const int S = a.stages, BN = a.BN;
     const uint32_t a_bytes = BM * BK * 2, b_bytes = (uint32_t)BN * BK * 2;
     const uint32_t stage_bytes = NP * (a_bytes + b_bytes);
     auto sA = [&](int s, int part) { return smem + (size_t)s * stage_bytes + (size_t)part * a_bytes; };
     auto sB = [&](int s, int part) { return smem + (size_t)s * stage_bytes + (size_t)NP * a_bytes + (size_t)part * b_bytes; };
-    uint8_t* stage_out = smem + (size_t)S * stage_bytes;                   // [4 warps][SWB]
-    float* xchg = reinterpret_cast<float*>(stage_out + 4 * SWB);           // [2 bufs][2 arrays][4][64]
-    float* flbuf = xchg + 2 * 2 * 4 * 64;                                  // [4 warps][kFlWarp]
-    uint64_t* full = reinterpret_cast<uint64_t*>(flbuf + 4 * kFlWarp);
+    uint8_t* stage_out = smem + (size_t)S * stage_bytes;                   // [epilogue warp][2 buffers][SWB]
+    float* xchg = reinterpret_cast<float*>(stage_out + 2 * kEpiWarps * SWB); // [half][2 bufs][2 arrays][4][CW]
+    float* flbuf = xchg + 2 * 2 * 2 * 4 * CW;                              // [epilogue warp][kFlWarp]
+    uint64_t* full = reinterpret_cast<uint64_t*>(flbuf + kEpiWarps * kFlWarp);
     uint64_t* empty = full + S;
     uint64_t* tfull = empty + S;     // [2]
     uint64_t* tempty = tfull + 2;    // [2]
@@ -153,7 +161,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
         s_err = 0;
         s_epi_err = 0;
         for (int s = 0; s < S; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-        for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 4); }
+        for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], kEpiWarps); }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         fence_async_smem();
     }
@@ -228,11 +236,13 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
             if (err) atomicExch(&s_err, 1);
         }
     } else {
-        // ---------------- epilogue warps
+        // ---------------- epilogue warps: warp w drains TMEM lanes 32 (w % 4) .. +31; the two warps
+        // of one lane quarter take alternate CW-column chunks (column half h)
         const int q = warp & 3;                      // TMEM lane quarter
+        const int ew = warp - 2, h = ew >> 2;        // epilogue warp index, column half
         const GemmEpi& e = a.epi;
         const int Tp = e.Tp;
-        uint8_t* my_out = stage_out + (size_t)q * SWB;
+        uint32_t nchunk = 0;                         // chunks staged by this warp (selects the buffer)
         uint32_t it = 0;
         int xbuf = 0;
         for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++it) {
@@ -277,16 +287,16 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                 }
             };
             if (rb) {
-                // pull this row's row-bias segment into L1 while the accumulator is finished
-                for (int j = 0; j < BN && n0 + j < a.N; j += 32)
-                    asm volatile("prefetch.global.L1 [%0];" ::"l"(rb + n0 + j));
+                // pull this row's row-bias chunks into L1 while the accumulator is finished
+                for (int c0 = h * CW; c0 < BN && n0 + c0 < a.N; c0 += 2 * CW)
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(rb + n0 + c0));
             }
             const bool ready = mbar_wait(&tfull[acc], (it >> 1) & 1);
             if (!ready && lane == 0) s_epi_err = 1;
-            epi_bar();                               // all four epilogue warps agree before leaving
+            epi_bar();                               // all epilogue warps agree before leaving
             if (*(volatile int*)&s_epi_err) { if (lane == 0) atomicExch(&s_err, 1); break; }
             tc_fence_after();
-            for (int c0 = 0; c0 < BN; c0 += CW) {
+            for (int c0 = h * CW; c0 < BN; c0 += 2 * CW) {
                 float v[CW];
                 load_bias(c0);                        // issued before the TMEM reads of this chunk
                 const uint32_t base = tmem + acc * (uint32_t)BN + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
@@ -295,19 +305,23 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                 tmem_wait_ld();
                 #pragma unroll
                 for (int j = 0; j < CW; ++j) v[j] += rbv[j];
+                // double-buffered staging: the store issued from this buffer two chunks ago has
+                // finished reading it once at most one bulk group (the previous chunk's) is pending
+                uint8_t* my_out = stage_out + (size_t)(ew * 2 + (nchunk & 1)) * SWB;
+                ++nchunk;
+                if (lane == 0) bulk_wait_read1();
+                __syncwarp();
                 if (a.fl) {
                     // Forward-Laplacian tanh over the Tp channel rows of each electron:
                     // y_0 = tanh(z_0), y_t = d1 z_t (gradients), y_lap = d1 z_lap - 2 y0 d1 sum_t z_t^2,
                     // d1 = 1 - y0^2. Gradient rows stage their squares in the swizzled staging tile (free
-                    // here: the previous TMA store has finished reading it) and the value row its value
+                    // here: its last TMA store has finished reading it) and the value row its value
                     // in Z0. Lanes add float4 column chunks over 8-row blocks, the blocks of one electron
                     // are combined in-lane, by shuffles or (Tp > 32) across warps, and the lane holding a
                     // group's column sums writes that group's coefficient rows for its four columns.
                     // Each row then takes y = alpha v + beta with coefficient rows chosen by its type.
-                    if (lane == 0) bulk_wait_read0();
-                    __syncwarp();
                     float* sq = reinterpret_cast<float*>(my_out);          // [32 rows][CW] swizzled by 16 B chunks
-                    float* fb = flbuf + (size_t)q * kFlWarp;
+                    float* fb = flbuf + (size_t)ew * kFlWarp;
                     float* Z0 = fb;                                       // [group][kFlP]
                     float* D1 = fb + 4 * kFlP;
                     float* Y0 = fb + 8 * kFlP;
@@ -368,23 +382,23 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                             if (holder) coeffs(g, g4, *reinterpret_cast<const float4*>(Z0 + g * kFlP + 4 * jc));
                         } else {
                             // a group spans several warps: exchange the partial sums and the value row
-                            float* xs = xchg + (size_t)xbuf * 2 * 4 * 64;
+                            float* xs = xchg + (size_t)(h * 2 + xbuf) * 2 * 4 * CW;
                             const bool has_val = (q * 32) % Tp == 0;        // this warp holds the value row
                             if (holder) {
-                                *reinterpret_cast<float4*>(xs + q * 64 + 4 * jc) = g4;
+                                *reinterpret_cast<float4*>(xs + q * CW + 4 * jc) = g4;
                                 if (has_val)
-                                    *reinterpret_cast<float4*>(xs + 4 * 64 + q * 64 + 4 * jc) =
+                                    *reinterpret_cast<float4*>(xs + 4 * CW + q * CW + 4 * jc) =
                                         *reinterpret_cast<const float4*>(Z0 + 4 * jc);
                             }
-                            epi_bar();
+                            half_bar(h);
                             const int qs = Tp / 32, g0 = (q / qs) * qs;
                             if (holder) {
                                 float4 tot = make_float4(0.f, 0.f, 0.f, 0.f);
                                 for (int k = 0; k < qs; ++k) {
-                                    const float4 pk = *reinterpret_cast<const float4*>(xs + (g0 + k) * 64 + 4 * jc);
+                                    const float4 pk = *reinterpret_cast<const float4*>(xs + (g0 + k) * CW + 4 * jc);
                                     tot.x += pk.x; tot.y += pk.y; tot.z += pk.z; tot.w += pk.w;
                                 }
-                                coeffs(0, tot, *reinterpret_cast<const float4*>(xs + 4 * 64 + g0 * 64 + 4 * jc));
+                                coeffs(0, tot, *reinterpret_cast<const float4*>(xs + 4 * CW + g0 * CW + 4 * jc));
                             }
                             xbuf ^= 1;   // the other exchange buffer is written only after the next barrier
                         }
@@ -415,9 +429,8 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                     #pragma unroll
                     for (int j = 0; j < CW; ++j) v[j] = tanhf(v[j]);
                 }
-                // stage the 32 x CW sub-tile (128-byte swizzle) and store it with TMA
-                if (lane == 0) bulk_wait_read0();
-                __syncwarp();
+                // stage the 32 x CW sub-tile (128-byte swizzle for FP32 rows, 64-byte for BF16 rows) and
+                // store it with TMA
                 if (OUT == 0) {
                     #pragma unroll
                     for (int j = 0; j < 8; ++j)
@@ -425,7 +438,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                             make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
                 } else {
                     #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
+                    for (int j = 0; j < 4; ++j) {
                         uint32_t hw_[4], lw_[4];
                         #pragma unroll
                         for (int k = 0; k < 4; ++k) {
@@ -439,16 +452,16 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                                 lw_[k] = 0u;
                             }
                         }
-                        *reinterpret_cast<uint4*>(my_out + swz(lane, j)) = make_uint4(hw_[0], hw_[1], hw_[2], hw_[3]);
+                        *reinterpret_cast<uint4*>(my_out + swz64(lane, j)) = make_uint4(hw_[0], hw_[1], hw_[2], hw_[3]);
                         if (OUT == 2)
-                            *reinterpret_cast<uint4*>(my_out + 4096 + swz(lane, j)) = make_uint4(lw_[0], lw_[1], lw_[2], lw_[3]);
+                            *reinterpret_cast<uint4*>(my_out + 2048 + swz64(lane, j)) = make_uint4(lw_[0], lw_[1], lw_[2], lw_[3]);
                     }
                 }
                 fence_async_smem();
                 __syncwarp();
                 if (lane == 0) {
                     tma_store_2d(&tmC0, my_out, n0 + c0, m0 + q * 32);
-                    if (OUT == 2) tma_store_2d(&tmC1, my_out + 4096, n0 + c0, m0 + q * 32);
+                    if (OUT == 2) tma_store_2d(&tmC1, my_out + 2048, n0 + c0, m0 + q * 32);
                     bulk_commit();
                 }
             }
@@ -486,20 +499,22 @@ EncodeTiledFn encode_fn() {
 }
 
 // 2-D tensor map: dims {cols (inner), rows}, row stride ld elements, box {box_cols, box_rows},
-// 128-byte swizzle (box_cols * element size must be 128 bytes).
+// swizzle of box_cols * element size bytes (128 or 64).
 int make_map(CUtensorMap* map, const void* base, int64_t rows, int cols, int64_t ld, int box_cols, int box_rows,
              bool f32) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return DW_ERR_UNSUPPORTED;
     const int es = f32 ? 4 : 2;
-    if (((uintptr_t)base & 15) || (ld * es) % 16 || box_cols * es != 128) return DW_ERR_ARG;
+    const int span = box_cols * es;
+    if (((uintptr_t)base & 15) || (ld * es) % 16 || (span != 128 && span != 64)) return DW_ERR_ARG;
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)ld * es};
     cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                     const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    span == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? DW_OK : DW_ERR_ARG;
 }
 
@@ -520,7 +535,6 @@ template <int NP, int OUT>
 int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __nv_bfloat16* W1, void* C, int ldc,
               int M, int N, int K, const GemmEpi& epi, int fl, int n3, cudaStream_t s) {
     if (M <= 0 || N <= 0 || K <= 0) return DW_OK;
-    constexpr int CW = OUT == 0 ? 32 : 64;
     constexpr int BN_MAX = NP == 2 ? 128 : 256;      // keeps >= 2 pipeline stages in shared memory
     int ntn = (N + BN_MAX - 1) / BN_MAX;
     int BN = round_up((N + ntn - 1) / ntn, CW);
@@ -539,17 +553,16 @@ int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __
         DW_CHECK(make_map(&mc0, C, M, N, ldc, 32, 32, true));
         mc1 = mc0;
     } else if (OUT == 1) {
-        DW_CHECK(make_map(&mc0, C, M, N, ldc, 64, 32, false));
+        DW_CHECK(make_map(&mc0, C, M, N, ldc, 32, 32, false));
         mc1 = mc0;
     } else {
-        DW_CHECK(make_map(&mc0, C, M, N, (int64_t)2 * ldc, 64, 32, false));
-        DW_CHECK(make_map(&mc1, reinterpret_cast<const __nv_bfloat16*>(C) + ldc, M, N, (int64_t)2 * ldc, 64, 32, false));
+        DW_CHECK(make_map(&mc0, C, M, N, (int64_t)2 * ldc, 32, 32, false));
+        DW_CHECK(make_map(&mc1, reinterpret_cast<const __nv_bfloat16*>(C) + ldc, M, N, (int64_t)2 * ldc, 32, 32, false));
     }
     TcArgs a;
     a.M = M; a.N = N; a.K = K; a.BN = BN; a.epi = epi; a.fl = fl; a.n3 = n3;
     const int stage_bytes = NP * (BM * BK * 2 + BN * BK * 2);
-    const int swb = OUT == 0 ? 4096 : 8192;
-    const int fixed = 1024 + 4 * swb + 2 * 2 * 4 * 64 * 4 + 4 * kFlWarp * 4 + 256;
+    const int fixed = 1024 + 2 * kEpiWarps * 4096 + 2 * 2 * 2 * 4 * CW * 4 + kEpiWarps * kFlWarp * 4 + 256;
     a.stages = std::min(8, (220 * 1024 - fixed) / stage_bytes);
     if (a.stages < 2) return DW_ERR_ARCH;
     a.tmem_cols = 32;

@@ -977,8 +977,100 @@ void launch_conv(const float* r, const float* WPl, const float* HM, const float*
     }
     count_launch();
 }
+// Envelopes by rows: grid (walker groups of kEnvWG, column chunks, spin); each thread owns one
+// orbital column (k, o) of one spin. softplus(alpha) and the weight of every ion for that column
+// stay in registers across all rows of the block; per (electron, ion) the difference vector,
+// distance and inverse distance are formed once in shared memory (a negative distance marks a
+// padding ion of a packed geometry). Same mathematics as k_envelope.
+constexpr int kEnvWG = 4;
+constexpr int kEnvMaxIons = 16;
+__global__ void __launch_bounds__(256)
+k_envelope_rows(const float* __restrict__ r, const float* __restrict__ Rall, const int32_t* __restrict__ Zall,
+                const float* __restrict__ P, ParamLayout L, const float* __restrict__ spA, Dims d, int B,
+                const float* __restrict__ BF, int ldbf, float* __restrict__ MO) {
+    extern __shared__ float se[];                            // [row][ion][5]: dx, dy, dz, dist, 1/dist
+    const int spin = blockIdx.z;
+    const int ns = spin == 0 ? d.nu : d.nd, i0 = spin == 0 ? 0 : d.nu;
+    const int b0 = blockIdx.x * kEnvWG;
+    const int nb = min(kEnvWG, B - b0);
+    const int rows = nb * ns, N = d.N;
+    for (int e = threadIdx.x; e < rows * N; e += blockDim.x) {
+        const int rr = e / N, I = e % N;
+        const int b = b0 + rr / ns, i = i0 + rr % ns;
+        const int sg = seg_of(d, b);
+        const float* R = Rall + (size_t)sg * N * 3;
+        const float* ri = r + ((int64_t)b * d.n + i) * 3;
+        const float s0 = ri[0] - R[I * 3], s1 = ri[1] - R[I * 3 + 1], s2 = ri[2] - R[I * 3 + 2];
+        const float dd = sqrtf(s0 * s0 + s1 * s1 + s2 * s2);
+        float* o = se + (size_t)e * 5;
+        o[0] = s0; o[1] = s1; o[2] = s2;
+        o[3] = Zall[(size_t)sg * N + I] > 0 ? dd : -1.f;
+        o[4] = 1.f / dd;
+    }
+    __syncthreads();
+    const int col = blockIdx.y * blockDim.x + threadIdx.x;
+    if (col >= d.KN) return;
+    const float* spa = spA + (spin ? (size_t)N * d.KN : 0);   // softplus(alpha), prepared
+    const float* wts = P + (spin ? L.weights_dn : L.weights_up);
+    float av[kEnvMaxIons], wv[kEnvMaxIons];
+    #pragma unroll
+    for (int I = 0; I < kEnvMaxIons; ++I) {
+        av[I] = I < N ? __ldg(spa + (size_t)I * d.KN + col) : 0.f;
+        wv[I] = I < N ? __ldg(wts + (size_t)I * d.KN + col) : 0.f;
+    }
+    const int k = col / d.n, o = col - (col / d.n) * d.n;
+    const int64_t mstride = (int64_t)d.n * d.n;              // per channel
+    const bool tang = d.Tp > 1;
+    for (int rr = 0; rr < rows; ++rr) {
+        const int b = b0 + rr / ns, i = i0 + rr % ns;
+        const float* gv = se + (size_t)rr * N * 5;
+        float env = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, lapv = 0.f;
+        #pragma unroll
+        for (int I = 0; I < kEnvMaxIons; ++I) {
+            if (I >= N) break;
+            const float dd = gv[I * 5 + 3];
+            if (dd < 0.f) continue;                          // padding ion
+            const float a = av[I];
+            const float e = wv[I] * expf(-a * dd);
+            env += e;
+            if (tang) {
+                const float inv = gv[I * 5 + 4];
+                const float gs = -a * e * inv;
+                g0 += gs * gv[I * 5]; g1 += gs * gv[I * 5 + 1]; g2 += gs * gv[I * 5 + 2];
+                lapv += e * (a * a - 2.f * a * inv);
+            }
+        }
+        const float* bf = BF + ((int64_t)b * d.n + i) * d.Tp * ldbf + (spin ? d.KN : 0) + col;
+        float* mo = MO + (((int64_t)b * d.K + k) * d.T) * mstride + i * d.n + o;
+        const float bf0 = bf[0];
+        mo[0] = env * bf0;
+        if (!tang) continue;
+        for (int t = 1; t <= 3 * d.n; ++t) {
+            float v = env * bf[(int64_t)t * ldbf];
+            const unsigned c = (unsigned)(t - 1 - 3 * i);     // own coordinate channels
+            if (c < 3u) v += (c == 0 ? g0 : (c == 1 ? g1 : g2)) * bf0;
+            mo[t * mstride] = v;
+        }
+        float vl = env * bf[(int64_t)d.lap * ldbf] + lapv * bf0;
+        vl += 2.f * (g0 * bf[(int64_t)(1 + 3 * i) * ldbf] + g1 * bf[(int64_t)(2 + 3 * i) * ldbf] +
+                     g2 * bf[(int64_t)(3 + 3 * i) * ldbf]);
+        mo[d.lap * mstride] = vl;
+    }
+}
+
 void launch_envelope(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,
                      const float* sp_alpha, const Dims& d, int B, const float* BF, int ldbf, float* MO, cudaStream_t s) {
+    // value-only rows: row-blocked form (the tangent form writes 3n + 2 channels per element and
+    // keeps one thread per element for parallelism)
+    if (d.N <= kEnvMaxIons && d.Tp == 1) {
+        const int threads = std::min(256, round_up(d.KN, 32));
+        const int ns_max = std::max(d.nu, d.nd);
+        const size_t sm = (size_t)kEnvWG * ns_max * d.N * 5 * sizeof(float);
+        dim3 grid((unsigned)((B + kEnvWG - 1) / kEnvWG), (unsigned)((d.KN + threads - 1) / threads), d.nd > 0 ? 2 : 1);
+        k_envelope_rows<<<grid, threads, sm, s>>>(r, R, Z, P, L, sp_alpha, d, B, BF, ldbf, MO);
+        count_launch();
+        return;
+    }
     int64_t n = (int64_t)B * d.n * d.KN;
     k_envelope<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, R, Z, P, L, sp_alpha, d, B, BF, ldbf, MO); count_launch();
 }

@@ -370,6 +370,258 @@ k_slogdet_thread(const float* __restrict__ MO, int n, int T, int nmat, double* _
     sign[mat0 + tid] = singular ? 0.0 : sg;
 }
 
+// FP64 log|det| and inverse with one matrix per thread: in-place Gauss-Jordan elimination with
+// partial pivoting (first row of maximal |a_ik| at or below the diagonal, rows exchanged
+// physically as getrf does), n^3 FMAs per matrix. Pivot k: row k is scaled by 1/a_kk, every
+// other row i loses a_ik times it, and column k becomes the inverse's column (1/a_kk on the
+// diagonal, -a_ik/a_kk elsewhere). The result is (PA)^-1 = A^-1 P^T, so the recorded row
+// exchanges are undone on the columns in reverse order. Shared-memory layout and log-det
+// bookkeeping as in k_slogdet_thread; the inverse is written in FP32 (zeros when singular).
+template <int NMAX, int TPB>
+__global__ void __launch_bounds__(TPB)
+k_slogdet_inv_thread(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
+                     double* __restrict__ sign, float* __restrict__ Ainv) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int LD = TPB + 1;
+    double* sm = reinterpret_cast<double*>(smem_raw);
+    unsigned char* pivs = smem_raw + (size_t)NMAX * NMAX * LD * sizeof(double);   // [k][thread]
+    const int tid = threadIdx.x;
+    const int mat0 = blockIdx.x * TPB;
+    const int nm = min(TPB, nmat - mat0);
+    const int nn = n * n;
+    for (int q = tid; q < nm * nn; q += TPB) {
+        const int m = q / nn, e = q - m * nn;
+        const int i = e / n, j = e - i * n;
+        sm[(i * NMAX + j) * LD + m] = (double)__ldg(MO + (int64_t)(mat0 + m) * T * nn + e);
+    }
+    __syncthreads();
+    if (tid >= nm) return;
+    double* a = sm + tid;
+    auto at = [&](int i, int j) -> double& { return a[(i * NMAX + j) * LD]; };
+    double mant = 1.0, sg = 1.0;
+    int expo = 0;
+    bool singular = false;
+    #pragma unroll 1
+    for (int k = 0; k < n; ++k) {
+        long long best = __double_as_longlong(at(k, k)) & 0x7fffffffffffffffll;
+        int p = k;
+        #pragma unroll 1
+        for (int i = k + 1; i < n; ++i) {
+            const long long v = __double_as_longlong(at(i, k)) & 0x7fffffffffffffffll;
+            if (v > best) { best = v; p = i; }
+        }
+        if (best == 0) { singular = true; break; }
+        pivs[k * TPB + tid] = (unsigned char)p;
+        if (p != k) {
+            #pragma unroll 1
+            for (int j = 0; j < n; ++j) { const double t = at(k, j); at(k, j) = at(p, j); at(p, j) = t; }
+            sg = -sg;
+        }
+        const double pk = at(k, k);
+        if (pk < 0.0) sg = -sg;
+        mant = mant_mul_norm(mant, fabs(pk), expo);
+        const double rp = recip_nr(pk);
+        // scaled pivot row in registers (column k itself becomes 1 / a_kk)
+        double u[NMAX];
+        #pragma unroll
+        for (int j = 0; j < NMAX; ++j) {
+            if (j >= n) break;
+            const double x = (j == k) ? 1.0 : at(k, j);
+            u[j] = x * rp;
+            at(k, j) = u[j];
+        }
+        #pragma unroll 1
+        for (int i = 0; i < n; ++i) {
+            if (i == k) continue;
+            double* row = &at(i, 0);
+            const double f = row[k * LD];
+            #pragma unroll
+            for (int j = 0; j < NMAX; ++j) {
+                if (j >= n) break;
+                if (j == k) continue;
+                row[j * LD] = fma(-f, u[j], row[j * LD]);
+            }
+            row[k * LD] = -f * rp;
+        }
+    }
+    const int mat = mat0 + tid;
+    logdet[mat] = singular ? -INFINITY : log(mant) + (double)expo * 0.69314718055994530942;
+    sign[mat] = singular ? 0.0 : sg;
+    float* out = Ainv + (int64_t)mat * nn;
+    if (singular) {
+        for (int e = 0; e < nn; ++e) out[e] = 0.f;
+        return;
+    }
+    // undo the row exchanges on the columns, last exchange first
+    #pragma unroll 1
+    for (int k = n - 1; k >= 0; --k) {
+        const int p = pivs[k * TPB + tid];
+        if (p == k) continue;
+        #pragma unroll 1
+        for (int i = 0; i < n; ++i) { const double t = at(i, k); at(i, k) = at(i, p); at(i, p) = t; }
+    }
+    #pragma unroll 1
+    for (int i = 0; i < n; ++i)
+        #pragma unroll 1
+        for (int j = 0; j < n; ++j) out[i * n + j] = (float)at(i, j);
+}
+
+// FP64 log|det| (and, with INV, the inverse) with SPLIT lanes per matrix: the lanes of a matrix
+// own its rows cyclically (row i belongs to lane i % SPLIT) and run the same elimination as
+// k_slogdet_thread (LU) / k_slogdet_inv_thread (Gauss-Jordan) on their rows, exchanging the
+// pivot choice by shuffles and sharing rows through shared memory. For n > 12 the per-matrix
+// shared memory limits an SM to about a hundred matrices, so a single lane per matrix leaves
+// the FP64 pipe short of warps; splitting the rows multiplies the warps at nearly the same FP64
+// instruction count. Lanes of padding matrices (past nmat) eliminate an identity matrix so that
+// every lane runs every shuffle.
+template <int NMAX, int SPLIT, bool INV>
+__global__ void __launch_bounds__(32 * SPLIT)
+k_slogdet_split(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
+                double* __restrict__ sign, float* __restrict__ Ainv) {
+    constexpr int TPB = 32 * SPLIT, MPB = 32, LD = MPB + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* sm = reinterpret_cast<double*>(smem_raw);
+    unsigned char* pivs = smem_raw + (size_t)NMAX * NMAX * LD * sizeof(double);    // [k][matrix]
+    const int tid = threadIdx.x, m = tid / SPLIT, h = tid % SPLIT;
+    const int mat0 = blockIdx.x * MPB;
+    const int nm = min(MPB, nmat - mat0);
+    const int nn = n * n;
+    for (int q = tid; q < MPB * nn; q += TPB) {
+        const int mm = q / nn, e = q - mm * nn;
+        const int i = e / n, j = e - i * n;
+        sm[(i * NMAX + j) * LD + mm] = mm < nm ? (double)__ldg(MO + (int64_t)(mat0 + mm) * T * nn + e)
+                                               : (i == j ? 1.0 : 0.0);
+    }
+    __syncthreads();
+    double* a = sm + m;
+    auto at = [&](int i, int j) -> double& { return a[(i * NMAX + j) * LD]; };
+    double mant = 1.0, sg = 1.0;
+    int expo = 0;
+    bool singular = false;
+    #pragma unroll 1
+    for (int k = 0; k < n; ++k) {
+        // first own row at or below the diagonal
+        const int i0 = k + ((h - k % SPLIT) + SPLIT) % SPLIT;
+        long long best = -1;
+        int p = n;
+        #pragma unroll 1
+        for (int i = i0; i < n; i += SPLIT) {
+            const long long v = __double_as_longlong(at(i, k)) & 0x7fffffffffffffffll;
+            if (v > best) { best = v; p = i; }
+        }
+        #pragma unroll
+        for (int o = 1; o < SPLIT; o <<= 1) {
+            const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int op = __shfl_xor_sync(0xffffffffu, p, o);
+            if (ob > best || (ob == best && op < p)) { best = ob; p = op; }
+        }
+        const bool sing_now = best <= 0;
+        singular = singular || sing_now;
+        if (sing_now) p = k;
+        if (INV && h == 0) pivs[k * MPB + m] = (unsigned char)p;
+        if (p != k) {
+            #pragma unroll 1
+            for (int j = (INV ? 0 : k) + h; j < n; j += SPLIT) {
+                const double t = at(k, j); at(k, j) = at(p, j); at(p, j) = t;
+            }
+            sg = -sg;
+        }
+        __syncwarp();
+        double pk = at(k, k);
+        if (sing_now) pk = 1.0;
+        if (pk < 0.0) sg = -sg;
+        mant = mant_mul_norm(mant, fabs(pk), expo);
+        const double rp = recip_nr(pk);
+        if (!INV) {
+            const int rem = n - k - 1;
+            double u[NMAX - 1];
+            #pragma unroll
+            for (int c = 0; c < NMAX - 1; ++c) {
+                if (c >= rem) break;
+                u[c] = at(k, k + 1 + c);
+            }
+            #pragma unroll 1
+            for (int i = i0 + (i0 == k ? SPLIT : 0); i < n; i += SPLIT) {
+                double* row = &at(i, k);
+                const double l = row[0] * rp;
+                #pragma unroll
+                for (int c = 0; c < NMAX - 1; ++c) {
+                    if (c >= rem) break;
+                    row[(c + 1) * LD] = fma(-l, u[c], row[(c + 1) * LD]);
+                }
+            }
+        } else {
+            double u[NMAX];
+            #pragma unroll
+            for (int j = 0; j < NMAX; ++j) {
+                if (j >= n) break;
+                u[j] = (j == k ? 1.0 : at(k, j)) * rp;
+            }
+            __syncwarp();                                     // row k read by every lane of the matrix
+            if (k % SPLIT == h) {
+                #pragma unroll
+                for (int j = 0; j < NMAX; ++j) {
+                    if (j >= n) break;
+                    at(k, j) = u[j];
+                }
+            }
+            #pragma unroll 1
+            for (int i = h; i < n; i += SPLIT) {
+                if (i == k) continue;
+                double* row = &at(i, 0);
+                const double f = row[k * LD];
+                #pragma unroll
+                for (int j = 0; j < NMAX; ++j) {
+                    if (j >= n) break;
+                    if (j == k) continue;
+                    row[j * LD] = fma(-f, u[j], row[j * LD]);
+                }
+                row[k * LD] = -f * rp;
+            }
+        }
+        __syncwarp();
+    }
+    const bool active = m < nm;
+    const int mat = mat0 + m;
+    if (active && h == 0) {
+        logdet[mat] = singular ? -INFINITY : log(mant) + (double)expo * 0.69314718055994530942;
+        sign[mat] = singular ? 0.0 : sg;
+    }
+    if (!INV) return;
+    // undo the row exchanges on the columns, last exchange first (own rows)
+    #pragma unroll 1
+    for (int k = n - 1; k >= 0; --k) {
+        const int p = pivs[k * MPB + m];
+        if (p == k) continue;
+        #pragma unroll 1
+        for (int i = h; i < n; i += SPLIT) { const double t = at(i, k); at(i, k) = at(i, p); at(i, p) = t; }
+    }
+    if (!active) return;
+    float* out = Ainv + (int64_t)mat * nn;
+    #pragma unroll 1
+    for (int i = h; i < n; i += SPLIT)
+        #pragma unroll 1
+        for (int j = 0; j < n; ++j) out[i * n + j] = singular ? 0.f : (float)at(i, j);
+}
+
+template <int NMAX, int SPLIT, bool INV>
+static void launch_slogdet_split(const float* MO, int n, int T, int nmat, double* logdet, double* sign, float* Ainv,
+                                 cudaStream_t s) {
+    const size_t smem = (size_t)NMAX * NMAX * 33 * sizeof(double) + (size_t)NMAX * 32;
+    cudaFuncSetAttribute(k_slogdet_split<NMAX, SPLIT, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_slogdet_split<NMAX, SPLIT, INV><<<(unsigned)((nmat + 31) / 32), 32 * SPLIT, smem, s>>>(MO, n, T, nmat, logdet,
+                                                                                          sign, Ainv);
+}
+
+template <int NMAX, int TPB>
+static void launch_slogdet_inv_thread(const float* MO, int n, int T, int nmat, double* logdet, double* sign, float* Ainv,
+                                      cudaStream_t s) {
+    const size_t smem = (size_t)NMAX * NMAX * (TPB + 1) * sizeof(double) + (size_t)NMAX * TPB;
+    cudaFuncSetAttribute(k_slogdet_inv_thread<NMAX, TPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_slogdet_inv_thread<NMAX, TPB><<<(unsigned)((nmat + TPB - 1) / TPB), TPB, smem, s>>>(MO, n, T, nmat, logdet, sign,
+                                                                                       Ainv);
+}
+
 template <int NMAX, int TPB>
 static void launch_slogdet_thread(const float* MO, int n, int T, int nmat, double* logdet, double* sign, cudaStream_t s) {
     const size_t smem = (size_t)NMAX * NMAX * (TPB + 1) * sizeof(double);
@@ -401,7 +653,7 @@ void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, 
             else if (n <= 8) launch_slogdet_thread<8, 64>(MO, n, d.T, nmat, logdet, sign, s);
             else if (n <= 10) launch_slogdet_thread<10, 64>(MO, n, d.T, nmat, logdet, sign, s);
             else if (n <= 12) launch_slogdet_thread<12, 64>(MO, n, d.T, nmat, logdet, sign, s);
-            else launch_slogdet_thread<16, 32>(MO, n, d.T, nmat, logdet, sign, s);
+            else launch_slogdet_split<16, 2, false>(MO, n, d.T, nmat, logdet, sign, nullptr, s);
             count_launch();
             return;
         }
@@ -414,6 +666,15 @@ void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, 
             else if (n <= 16) rows(k_slogdet_rows<S, 16>);
             else if (n <= 24) rows(k_slogdet_rows<S, 24>);
             else rows(k_slogdet_rows<S, 32>);
+            count_launch();
+            return;
+        }
+        if (std::is_same<S, double>::value && n <= 16) {
+            if (n <= 4) launch_slogdet_inv_thread<4, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
+            else if (n <= 8) launch_slogdet_inv_thread<8, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
+            else if (n <= 10) launch_slogdet_inv_thread<10, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
+            else if (n <= 12) launch_slogdet_inv_thread<12, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
+            else launch_slogdet_split<16, 2, true>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
             count_launch();
             return;
         }

@@ -310,16 +310,37 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         ldin = kXW;
     }
     const Act* H = xin;   // final embedding, logical row width kXW
-    // backflow (envelope_orbitals.py:46-75): every row times [W_up | W_dn]; the envelope kernel
-    // takes the half that matches the electron's spin
-    {
+    // backflow (envelope_orbitals.py:46-75). Tensor-core tangent passes: one GEMM per spin over
+    // that spin's electron rows of every walker (walker-block tensor maps), so each row gets only
+    // its own spin's KN columns. Otherwise every row times [W_up | W_dn] and the envelope kernel
+    // takes the half that matches the electron's spin.
+    int ldbf = 2 * d.KN, spin_cols = d.KN;
+    const bool per_spin = tang && pt >= 1 && (d.nu * d.Tp) % 32 == 0 && (d.nd * d.Tp) % 32 == 0 && d.KN % 4 == 0;
+    if (per_spin) {
+        ldbf = d.KN;
+        spin_cols = 0;
+        timer_begin("backflow_gemm", s);
+        for (int spin = 0; spin < 2; ++spin) {
+            const int i0 = spin == 0 ? 0 : d.nu, ns = spin == 0 ? d.nu : d.nd;
+            WalkerBlocks wb;
+            wb.nw = Bc;
+            wb.rows = ns * d.Tp;
+            wb.a_wstride = (int64_t)d.n * d.Tp * kXW * ActIO<Act>::kParts;
+            wb.c_wstride = (int64_t)d.n * d.Tp * d.KN;
+            const int64_t wrow = (int64_t)spin * d.KN * d.D;           // W_up / W_dn rows of the K-major copy
+            DW_CHECK(gemm_tc_wb(pt, H + act_off<Act>((int64_t)i0 * d.Tp, kXW), kXW, pre.bf_bf[0] + wrow,
+                                pt >= 2 ? pre.bf_bf[1] + wrow : nullptr, p.BF + (int64_t)i0 * d.Tp * d.KN, d.KN, wb,
+                                d.KN, d.D, s));
+        }
+        timer_end("backflow_gemm", s, 0.0, 0.0);
+    } else {
         GemmEpi e0; e0.Tp = d.Tp; e0.rows_per_walker = d.n * d.Tp;
         WRef wb; wb.f32 = pre.bf_cat; wb.ldw = 2 * d.KN;
         if (pt >= 1) wb.hi = pre.bf_bf[0];
         if (pt >= 2) wb.lo = pre.bf_bf[1];
         DW_TIMED("backflow_gemm", DW_CHECK(MM<Act>::mm(H, kXW, wb, p.BF, 2 * d.KN, rows, 2 * d.KN, d.D, e0, s)));
     }
-    DW_TIMED("envelope", launch_envelope(r, R, Z, P, L, pre.sp_alpha, d, Bc, p.BF, 2 * d.KN, p.MO, s));
+    DW_TIMED("envelope", launch_envelope(r, R, Z, P, L, pre.sp_alpha, d, Bc, p.BF, ldbf, spin_cols, p.MO, s));
     if (precision == DW_PRECISION_FP32) DW_TIMED("slogdet", launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
     else DW_TIMED("slogdet", launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
     if (tang) DW_TIMED("det_tangents", launch_det_tangents(p.MO, p.Ainv, p.sign, d, Bc, p.g, p.lapdet, s));

@@ -454,7 +454,7 @@ static int backward_chunk(const Bwd& w, int Bc, const float* P, const ParamLayou
     }
     GemmEpi e0;
     gemm_f32(w.H4, d.D, bf_cat, 2 * d.KN, w.BF, 2 * d.KN, rows, 2 * d.KN, d.D, e0, 1, 0, 0, s);
-    launch_envelope(r, R, Z, P, L, spA, d, Bc, w.BF, 2 * d.KN, w.MO, s);
+    launch_envelope(r, R, Z, P, L, spA, d, Bc, w.BF, 2 * d.KN, d.KN, w.MO, s);
     launch_slogdet_inv(w.MO, d, Bc, w.logdet, w.sign, w.Ainv, s);
     GemmEpi j0; j0.bias = P + L.jas_b[0]; j0.act = 1;
     GemmEpi j1; j1.bias = P + L.jas_b[1]; j1.act = 1;

@@ -839,9 +839,10 @@ k_det_tangents_warp(const float* __restrict__ MO, const float* __restrict__ Ainv
 // For every channel t: C_t = A^-1 D_t (D_t = channel t of the Slater matrix), g_t = tr C_t and,
 // for the 3n gradient channels, tr(C_t^2) = sum_aj C_aj C_ja. Each thread forms one 4 x 4 tile
 // of C_t from float4 shared-memory loads (16 FMAs per two 16-byte loads), stages it, reads the
-// transposed tile for its part of tr(C_t^2), and the tile partials (FP32 sums of 16 products)
-// are added in FP64 per channel; the Laplacian trace lap = tr(A^-1 Lap A) - sum_t tr(C_t^2) is
-// accumulated in FP64. Matrices are zero-padded to NP = round_up(n, 4) <= 32.
+// transposed tile for its part of tr(C_t^2). A channel's traces are FP32 sums of products of
+// FP32 entries (as C_t itself is FP32), formed from the tile partials by one lane per channel;
+// the traces of all channels are accumulated in FP64 into
+// lap = tr(A^-1 Lap A) - sum_t tr(C_t^2). Matrices are zero-padded to NP = round_up(n, 4) <= 32.
 template <int NP>
 __global__ void __launch_bounds__(128)
 k_det_tangents_tile(const float* __restrict__ MO, const float* __restrict__ Ainv, const double* __restrict__ sign,
@@ -852,7 +853,7 @@ k_det_tangents_tile(const float* __restrict__ MO, const float* __restrict__ Ainv
     constexpr int PP = NP * NP + 4;              // channel plane pitch (floats), offset to spread banks
     __shared__ __align__(16) float AT[NP * NP];  // AT[k][a] = Ainv[a][k]
     __shared__ __align__(16) float Ds[CPR * PP];
-    __shared__ double part[2][128];
+    __shared__ float part[2][128];
     __shared__ double tr1[3 * 32 + 2], tr2[3 * 32 + 2];
     const int mat = blockIdx.x, tid = threadIdx.x;
     if (sign[mat] == 0.0) {
@@ -919,14 +920,15 @@ k_det_tangents_tile(const float* __restrict__ MO, const float* __restrict__ Ainv
             }
             if (ab == jb) p1 = acc[0][0] + acc[1][1] + acc[2][2] + acc[3][3];
         }
-        part[0][tid] = (double)p1;
-        part[1][tid] = (double)p2;
+        part[0][tid] = p1;
+        part[1][tid] = p2;
         __syncthreads();
         if (tid < nc) {
-            double s1 = 0.0, s2 = 0.0;
+            float s1 = 0.f, s2 = 0.f;
+            #pragma unroll 4
             for (int q = 0; q < TPC; ++q) { s1 += part[0][tid * TPC + q]; s2 += part[1][tid * TPC + q]; }
-            tr1[t0 + tid] = s1;
-            tr2[t0 + tid] = s2;
+            tr1[t0 + tid] = (double)s1;
+            tr2[t0 + tid] = (double)s2;
         }
     }
     __syncthreads();

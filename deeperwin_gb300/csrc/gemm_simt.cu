@@ -7,6 +7,17 @@
 
 namespace dw {
 
+static int num_sms_simt() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 148;
+    }
+    return n;
+}
+
 template <int BM, int BN, int BK, int TM, int TN, bool TRANS_W = false, bool ACC = false>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 k_gemm_f32(const float* __restrict__ A, int lda, const float* __restrict__ W, int ldw, float* __restrict__ C, int ldc,
@@ -108,10 +119,9 @@ void gemm_f32_nt(const float* A, int lda, const float* W, int ldw, float* C, int
     count_launch();
 }
 
-// Weight gradient: 64 x 64 output tiles, rows split into segments over grid.z; each block
-// stages 32-row slabs of A and G in shared memory and accumulates a 4 x 4 patch per thread.
+// Weight gradient for narrow shapes: 64 x 64 output tiles, 32-row slabs, a 4 x 4 patch per thread.
 __global__ void __launch_bounds__(256)
-k_wgrad_f32(const float* __restrict__ A, int lda, const float* __restrict__ G, int ldg, int rows, int K, int N,
+k_wgrad_f32_64(const float* __restrict__ A, int lda, const float* __restrict__ G, int ldg, int rows, int K, int N,
             float* __restrict__ dW, int lddw, float* __restrict__ dB, const int8_t* __restrict__ sel, int want,
             int rows_per_seg) {
     __shared__ float As[32][64 + 1];
@@ -164,15 +174,96 @@ k_wgrad_f32(const float* __restrict__ A, int lda, const float* __restrict__ G, i
     }
 }
 
+// Weight gradient dW[K, N] += sum_r A[r, k] G[r, n]: 128 x 128 output tiles, rows split into
+// segments over grid.z and accumulated atomically; each block stages 16-row slabs of A and G in
+// shared memory and accumulates an 8 x 8 patch per thread.
+__global__ void __launch_bounds__(256)
+k_wgrad_f32(const float* __restrict__ A, int lda, const float* __restrict__ G, int ldg, int rows, int K, int N,
+            float* __restrict__ dW, int lddw, float* __restrict__ dB, const int8_t* __restrict__ sel, int want,
+            int rows_per_seg) {
+    // 128 x 128 tile of dW per block, 8 x 8 per thread (two 4-wide groups in each direction so that
+    // the 16-byte shared-memory reads of a warp are consecutive), 16 rows staged per step.
+    constexpr int TB = 128, RB = 16;
+    __shared__ __align__(16) float As[RB][TB];
+    __shared__ __align__(16) float Gs[RB][TB];
+    const int k0 = blockIdx.y * TB, n0 = blockIdx.x * TB;
+    const int r_begin = blockIdx.z * rows_per_seg, r_end = min(rows, r_begin + rows_per_seg);
+    const int tid = threadIdx.x, tk = tid / 16, tn = tid % 16;
+    float acc[8][8];
+    #pragma unroll
+    for (int u = 0; u < 8; ++u)
+        #pragma unroll
+        for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+    float bacc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const bool do_bias = dB && blockIdx.y == 0 && tk == 0;
+    for (int r0 = r_begin; r0 < r_end; r0 += RB) {
+        for (int e = tid; e < RB * TB; e += 256) {
+            const int rr = e / TB, cc = e % TB, r = r0 + rr;
+            const bool ok = r < r_end && (!sel || sel[r] == want);
+            As[rr][cc] = (ok && k0 + cc < K) ? __ldg(A + (int64_t)r * lda + k0 + cc) : 0.f;
+            Gs[rr][cc] = (ok && n0 + cc < N) ? __ldg(G + (int64_t)r * ldg + n0 + cc) : 0.f;
+        }
+        __syncthreads();
+        #pragma unroll 2
+        for (int rr = 0; rr < RB; ++rr) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[rr][4 * tk]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[rr][64 + 4 * tk]);
+            const float4 g0 = *reinterpret_cast<const float4*>(&Gs[rr][4 * tn]);
+            const float4 g1 = *reinterpret_cast<const float4*>(&Gs[rr][64 + 4 * tn]);
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float g[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+            #pragma unroll
+            for (int u = 0; u < 8; ++u)
+                #pragma unroll
+                for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(a[u], g[v], acc[u][v]);
+            if (do_bias) {
+                #pragma unroll
+                for (int v = 0; v < 8; ++v) bacc[v] += g[v];
+            }
+        }
+        __syncthreads();
+    }
+    #pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        const int k = k0 + (u < 4 ? 4 * tk + u : 64 + 4 * tk + u - 4);
+        if (k >= K) continue;
+        #pragma unroll
+        for (int v = 0; v < 8; ++v) {
+            const int n = n0 + (v < 4 ? 4 * tn + v : 64 + 4 * tn + v - 4);
+            if (n < N) atomicAdd(dW + (int64_t)k * lddw + n, acc[u][v]);
+        }
+    }
+    if (do_bias) {
+        #pragma unroll
+        for (int v = 0; v < 8; ++v) {
+            const int n = n0 + (v < 4 ? 4 * tn + v : 64 + 4 * tn + v - 4);
+            if (n < N) atomicAdd(dB + n, bacc[v]);
+        }
+    }
+}
+
 void wgrad_f32(const float* A, int lda, const float* G, int ldg, int rows, int K, int N, float* dW, int lddw,
                float* dB, const int8_t* sel, int want, cudaStream_t s) {
     if (rows <= 0 || K <= 0 || N <= 0) return;
-    const int tiles = ((K + 63) / 64) * ((N + 63) / 64);
-    int segs = std::max(1, std::min((rows + 255) / 256, (4 * 152 + tiles - 1) / tiles));
+    if (K < 128 || N < 128) {
+        // narrow shapes: 64 x 64 tiles waste less of each thread's patch
+        const int tiles = ((K + 63) / 64) * ((N + 63) / 64);
+        int segs = std::max(1, std::min((rows + 255) / 256, (4 * num_sms_simt() + tiles - 1) / tiles));
+        int rps = (rows + segs - 1) / segs;
+        rps = (rps + 31) / 32 * 32;
+        segs = (rows + rps - 1) / rps;
+        dim3 g((N + 63) / 64, (K + 63) / 64, segs);
+        k_wgrad_f32_64<<<g, 256, 0, s>>>(A, lda, G, ldg, rows, K, N, dW, lddw, dB, sel, want, rps);
+        count_launch();
+        return;
+    }
+    const int tiles = ((K + 127) / 128) * ((N + 127) / 128);
+    // row segments: enough blocks for two waves over the SMs, at least 64 rows per segment
+    int segs = std::max(1, std::min((rows + 63) / 64, (2 * num_sms_simt() + tiles - 1) / tiles));
     int rps = (rows + segs - 1) / segs;
-    rps = (rps + 31) / 32 * 32;
+    rps = (rps + 15) / 16 * 16;
     segs = (rows + rps - 1) / rps;
-    dim3 g((N + 63) / 64, (K + 63) / 64, segs);
+    dim3 g((N + 127) / 128, (K + 127) / 128, segs);
     k_wgrad_f32<<<g, 256, 0, s>>>(A, lda, G, ldg, rows, K, N, dW, lddw, dB, sel, want, rps);
     count_launch();
 }

@@ -63,6 +63,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
         ::"r"(smem_u32(dst)), "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1) : "memory");
 }
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];"
+        ::"r"(smem_u32(dst)), "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2) : "memory");
+}
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* src, int c0, int c1, int c2) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];"
+                 ::"l"(map), "r"(smem_u32(src)), "r"(c0), "r"(c1), "r"(c2) : "memory");
+}
 __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void* src, int c0, int c1) {
     asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%2, %3}], [%1];"
                  ::"l"(map), "r"(smem_u32(src)), "r"(c0), "r"(c1) : "memory");
@@ -127,6 +136,11 @@ struct TcArgs {
     int stages;
     uint32_t tmem_cols;
     int n_tiles_n, n_tiles;
+    // Walker-block mode (nrb > 0): A and C are 3-D tensors {K or N, rows per walker block, walkers};
+    // M tile mi covers row block (mi % nrb) of 32 rows in walkers 4 (mi / nrb) .. + 3, and epilogue
+    // warp q stores the rows of walker 4 (mi / nrb) + q. Plain epilogue only (no bias, tanh or
+    // forward-Laplacian rows).
+    int nrb;
 };
 
 // OUT: 0 = fp32 C, 1 = bf16 C, 2 = split-BF16 C.
@@ -188,12 +202,16 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                     const uint32_t use = cnt / S;
                     if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1)) { err = true; break; }
                     mbar_expect_tx(&full[s], stage_bytes);
-                    tma_load_2d(sA(s, 0), &tmA0, &full[s], kt * BK, m0);
-                    tma_load_2d(sB(s, 0), &tmB0, &full[s], kt * BK, n0);
-                    if (NP == 2) {
-                        tma_load_2d(sA(s, 1), &tmA1, &full[s], kt * BK, m0);
-                        tma_load_2d(sB(s, 1), &tmB1, &full[s], kt * BK, n0);
+                    if (a.nrb) {
+                        const int mi = tile / a.n_tiles_n, rb = (mi % a.nrb) * 32, w0 = (mi / a.nrb) * 4;
+                        tma_load_3d(sA(s, 0), &tmA0, &full[s], kt * BK, rb, w0);
+                        if (NP == 2) tma_load_3d(sA(s, 1), &tmA1, &full[s], kt * BK, rb, w0);
+                    } else {
+                        tma_load_2d(sA(s, 0), &tmA0, &full[s], kt * BK, m0);
+                        if (NP == 2) tma_load_2d(sA(s, 1), &tmA1, &full[s], kt * BK, m0);
                     }
+                    tma_load_2d(sB(s, 0), &tmB0, &full[s], kt * BK, n0);
+                    if (NP == 2) tma_load_2d(sB(s, 1), &tmB1, &full[s], kt * BK, n0);
                     issued[s] = use + 1;
                 }
             }
@@ -460,8 +478,13 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                 fence_async_smem();
                 __syncwarp();
                 if (lane == 0) {
-                    tma_store_2d(&tmC0, my_out, n0 + c0, m0 + q * 32);
-                    if (OUT == 2) tma_store_2d(&tmC1, my_out + 2048, n0 + c0, m0 + q * 32);
+                    if (a.nrb) {
+                        const int mi = tile / a.n_tiles_n;
+                        tma_store_3d(&tmC0, my_out, n0 + c0, (mi % a.nrb) * 32, (mi / a.nrb) * 4 + q);
+                    } else {
+                        tma_store_2d(&tmC0, my_out, n0 + c0, m0 + q * 32);
+                        if (OUT == 2) tma_store_2d(&tmC1, my_out + 2048, n0 + c0, m0 + q * 32);
+                    }
                     bulk_commit();
                 }
             }
@@ -518,6 +541,26 @@ int make_map(CUtensorMap* map, const void* base, int64_t rows, int cols, int64_t
     return r == CUDA_SUCCESS ? DW_OK : DW_ERR_ARG;
 }
 
+// 3-D tensor map {cols (inner), rows, walkers}: row stride ld and walker stride wstride elements,
+// box {box_cols, box_rows, box_w}, swizzle of box_cols * element size bytes (128 or 64).
+int make_map3(CUtensorMap* map, const void* base, int64_t nw, int rows, int cols, int64_t ld, int64_t wstride,
+              int box_cols, int box_rows, int box_w, bool f32) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return DW_ERR_UNSUPPORTED;
+    const int es = f32 ? 4 : 2;
+    const int span = box_cols * es;
+    if (((uintptr_t)base & 15) || (ld * es) % 16 || (wstride * es) % 16 || (span != 128 && span != 64)) return DW_ERR_ARG;
+    cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)nw};
+    cuuint64_t strides[2] = {(cuuint64_t)ld * es, (cuuint64_t)wstride * es};
+    cuuint32_t box[3] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows, (cuuint32_t)box_w};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
+                    const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    span == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? DW_OK : DW_ERR_ARG;
+}
+
 int num_sms() {
     static int n = 0;
     if (!n) {
@@ -531,9 +574,15 @@ int num_sms() {
 
 // A: NP parts of a logical [M, lda] activation (NP = 2: [hi | lo] rows of width 2 lda).
 // W0/W1: [N, round_up(K, 64)] K-major weight parts. C: logical [M, ldc].
+// wb != nullptr: walker-block mode (FP32 output, plain epilogue); M is then ignored.
 template <int NP, int OUT>
 int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __nv_bfloat16* W1, void* C, int ldc,
-              int M, int N, int K, const GemmEpi& epi, int fl, int n3, cudaStream_t s) {
+              int M, int N, int K, const GemmEpi& epi, int fl, int n3, cudaStream_t s, const WalkerBlocks* wb = nullptr) {
+    if (wb) {
+        if (OUT != 0 || fl || epi.bias || epi.rowbias || epi.act || wb->rows % 32) return DW_ERR_ARG;
+        if (wb->nw <= 0) return DW_OK;
+        M = ((wb->nw + 3) / 4) * (wb->rows / 32) * BM;
+    }
     if (M <= 0 || N <= 0 || K <= 0) return DW_OK;
     constexpr int BN_MAX = NP == 2 ? 128 : 256;      // keeps >= 2 pipeline stages in shared memory
     int ntn = (N + BN_MAX - 1) / BN_MAX;
@@ -541,15 +590,22 @@ int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __
     while (BN > BN_MAX) { ntn += 1; BN = round_up((N + ntn - 1) / ntn, CW); }
     const int Kp = round_up(K, 64);
     CUtensorMap ma0, ma1, mb0, mb1, mc0, mc1;
-    DW_CHECK(make_map(&ma0, A, M, K, (int64_t)NP * lda, 64, BM, false));
-    DW_CHECK(make_map(&mb0, W0, N, K, Kp, 64, BN, false));
-    if (NP == 2) {
-        DW_CHECK(make_map(&ma1, A + lda, M, K, (int64_t)NP * lda, 64, BM, false));
-        DW_CHECK(make_map(&mb1, W1, N, K, Kp, 64, BN, false));
+    if (wb) {
+        DW_CHECK(make_map3(&ma0, A, wb->nw, wb->rows, K, (int64_t)NP * lda, wb->a_wstride, 64, 32, 4, false));
+        if (NP == 2) DW_CHECK(make_map3(&ma1, A + lda, wb->nw, wb->rows, K, (int64_t)NP * lda, wb->a_wstride, 64, 32, 4, false));
+        else ma1 = ma0;
     } else {
-        ma1 = ma0; mb1 = mb0;
+        DW_CHECK(make_map(&ma0, A, M, K, (int64_t)NP * lda, 64, BM, false));
+        if (NP == 2) DW_CHECK(make_map(&ma1, A + lda, M, K, (int64_t)NP * lda, 64, BM, false));
+        else ma1 = ma0;
     }
-    if (OUT == 0) {
+    DW_CHECK(make_map(&mb0, W0, N, K, Kp, 64, BN, false));
+    if (NP == 2) DW_CHECK(make_map(&mb1, W1, N, K, Kp, 64, BN, false));
+    else mb1 = mb0;
+    if (wb) {
+        DW_CHECK(make_map3(&mc0, C, wb->nw, wb->rows, N, ldc, wb->c_wstride, 32, 32, 1, true));
+        mc1 = mc0;
+    } else if (OUT == 0) {
         DW_CHECK(make_map(&mc0, C, M, N, ldc, 32, 32, true));
         mc1 = mc0;
     } else if (OUT == 1) {
@@ -561,6 +617,7 @@ int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __
     }
     TcArgs a;
     a.M = M; a.N = N; a.K = K; a.BN = BN; a.epi = epi; a.fl = fl; a.n3 = n3;
+    a.nrb = wb ? wb->rows / 32 : 0;
     const int stage_bytes = NP * (BM * BK * 2 + BN * BK * 2);
     const int fixed = 1024 + 2 * kEpiWarps * 4096 + 2 * 2 * 2 * 4 * CW * 4 + kEpiWarps * kFlWarp * 4 + 256;
     a.stages = std::min(8, (220 * 1024 - fixed) / stage_bytes);
@@ -593,6 +650,15 @@ bool tc_available() {
                   encode_fn() != nullptr) ? 1 : 0;
     }
     return cached == 1;
+}
+
+int gemm_tc_wb(int np, const void* A, int lda, const __nv_bfloat16* W0, const __nv_bfloat16* W1, float* C, int ldc,
+               const WalkerBlocks& wb, int N, int K, cudaStream_t s) {
+    const __nv_bfloat16* a = reinterpret_cast<const __nv_bfloat16*>(A);
+    GemmEpi e;
+    if (np == 1) return launch_tc<1, 0>(a, lda, W0, W1, C, ldc, 0, N, K, e, 0, 0, s, &wb);
+    if (np == 2) return launch_tc<2, 0>(a, lda, W0, W1, C, ldc, 0, N, K, e, 0, 0, s, &wb);
+    return DW_ERR_ARG;
 }
 
 int gemm_tc(int np, int out, const void* A, int lda, const __nv_bfloat16* W0, const __nv_bfloat16* W1, void* C, int ldc,

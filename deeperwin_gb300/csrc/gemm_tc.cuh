@@ -15,4 +15,14 @@ bool tc_available();
 int gemm_tc(int np, int out, const void* A, int lda, const __nv_bfloat16* W0, const __nv_bfloat16* W1, void* C, int ldc,
             int M, int N, int K, const GemmEpi& epi, int fl, int n3, cudaStream_t s);
 
+// Walker-block operands: per walker `rows` consecutive rows (a multiple of 32) of A (row stride
+// np * lda) and C (row stride ldc), walkers a_wstride / c_wstride elements apart.
+struct WalkerBlocks {
+    int nw, rows;
+    int64_t a_wstride, c_wstride;
+};
+// C (fp32) = A @ W^T over the rows of every walker block, plain epilogue.
+int gemm_tc_wb(int np, const void* A, int lda, const __nv_bfloat16* W0, const __nv_bfloat16* W1, float* C, int ldc,
+               const WalkerBlocks& wb, int N, int K, cudaStream_t s);
+
 }  // namespace dw

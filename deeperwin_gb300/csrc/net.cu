@@ -843,7 +843,7 @@ k_conv_walker(const float* __restrict__ r, const float* __restrict__ WPl, const 
 // env = sum_I w_I exp(-softplus(alpha_I) d_iI); grad/Laplacian w.r.t. r_i only.
 __global__ void k_envelope(const float* __restrict__ r, const float* __restrict__ Rall, const int32_t* __restrict__ Zall,
                            const float* __restrict__ P, ParamLayout L, const float* __restrict__ spA, Dims d, int B,
-                           const float* __restrict__ BF, int ldbf, float* __restrict__ MO) {
+                           const float* __restrict__ BF, int ldbf, int spin_cols, float* __restrict__ MO) {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)B * d.n * d.KN) return;
     int col = idx % d.KN;
@@ -871,7 +871,7 @@ __global__ void k_envelope(const float* __restrict__ r, const float* __restrict_
             lapv += e * (a * a - 2.f * a / dd);
         }
     }
-    const float* bf = BF + bi * d.Tp * ldbf + (up ? 0 : d.KN) + col;
+    const float* bf = BF + bi * d.Tp * ldbf + (up ? 0 : spin_cols) + col;
     int64_t mstride = (int64_t)d.n * d.n;                    // per channel
     float* mo = MO + (((int64_t)b * d.K + k) * d.T) * mstride + i * d.n + o;
     float bf0 = bf[0];
@@ -987,7 +987,7 @@ constexpr int kEnvMaxIons = 16;
 __global__ void __launch_bounds__(256)
 k_envelope_rows(const float* __restrict__ r, const float* __restrict__ Rall, const int32_t* __restrict__ Zall,
                 const float* __restrict__ P, ParamLayout L, const float* __restrict__ spA, Dims d, int B,
-                const float* __restrict__ BF, int ldbf, float* __restrict__ MO) {
+                const float* __restrict__ BF, int ldbf, int spin_cols, float* __restrict__ MO) {
     extern __shared__ float se[];                            // [row][ion][5]: dx, dy, dz, dist, 1/dist
     const int spin = blockIdx.z;
     const int ns = spin == 0 ? d.nu : d.nd, i0 = spin == 0 ? 0 : d.nu;
@@ -1040,7 +1040,7 @@ k_envelope_rows(const float* __restrict__ r, const float* __restrict__ Rall, con
                 lapv += e * (a * a - 2.f * a * inv);
             }
         }
-        const float* bf = BF + ((int64_t)b * d.n + i) * d.Tp * ldbf + (spin ? d.KN : 0) + col;
+        const float* bf = BF + ((int64_t)b * d.n + i) * d.Tp * ldbf + (spin ? spin_cols : 0) + col;
         float* mo = MO + (((int64_t)b * d.K + k) * d.T) * mstride + i * d.n + o;
         const float bf0 = bf[0];
         mo[0] = env * bf0;
@@ -1059,7 +1059,8 @@ k_envelope_rows(const float* __restrict__ r, const float* __restrict__ Rall, con
 }
 
 void launch_envelope(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,
-                     const float* sp_alpha, const Dims& d, int B, const float* BF, int ldbf, float* MO, cudaStream_t s) {
+                     const float* sp_alpha, const Dims& d, int B, const float* BF, int ldbf, int spin_cols, float* MO,
+                     cudaStream_t s) {
     // value-only rows: row-blocked form (the tangent form writes 3n + 2 channels per element and
     // keeps one thread per element for parallelism)
     if (d.N <= kEnvMaxIons && d.Tp == 1) {
@@ -1067,12 +1068,13 @@ void launch_envelope(const float* r, const float* R, const int32_t* Z, const flo
         const int ns_max = std::max(d.nu, d.nd);
         const size_t sm = (size_t)kEnvWG * ns_max * d.N * 5 * sizeof(float);
         dim3 grid((unsigned)((B + kEnvWG - 1) / kEnvWG), (unsigned)((d.KN + threads - 1) / threads), d.nd > 0 ? 2 : 1);
-        k_envelope_rows<<<grid, threads, sm, s>>>(r, R, Z, P, L, sp_alpha, d, B, BF, ldbf, MO);
+        k_envelope_rows<<<grid, threads, sm, s>>>(r, R, Z, P, L, sp_alpha, d, B, BF, ldbf, spin_cols, MO);
         count_launch();
         return;
     }
     int64_t n = (int64_t)B * d.n * d.KN;
-    k_envelope<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, R, Z, P, L, sp_alpha, d, B, BF, ldbf, MO); count_launch();
+    k_envelope<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, R, Z, P, L, sp_alpha, d, B, BF, ldbf, spin_cols, MO);
+    count_launch();
 }
 template <class Act>
 void launch_jastrow_out(const Act* J2, int ldj, const float* w2, const Dims& d, int B, double* jas, cudaStream_t s) {

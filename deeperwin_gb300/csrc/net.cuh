@@ -77,8 +77,11 @@ template <class Act> void launch_spin_means(const Act* X, int ldx, int hw, const
 template <class Act> void launch_tanh_fl(const float* Zb, int ldz, int ncols, int groups, const Dims& d, Act* Y, int ldy, cudaStream_t s);
 template <class Act> void launch_conv(const float* r, const float* WPl, const float* HM, const float* HEl, const float* himl,
                                       const Dims& d, int l, int B, Act* X, int ldx, cudaStream_t s);
+// BF rows hold the backflow of each electron; the down-spin electrons' columns start at column
+// spin_cols (KN when both spin blocks are stored side by side, 0 when each row holds its own spin's).
 void launch_envelope(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,
-                     const float* sp_alpha, const Dims& d, int B, const float* BF, int ldbf, float* MO, cudaStream_t s);
+                     const float* sp_alpha, const Dims& d, int B, const float* BF, int ldbf, int spin_cols, float* MO,
+                     cudaStream_t s);
 template <class Act> void launch_jastrow_out(const Act* J2, int ldj, const float* w2, const Dims& d, int B, double* jas, cudaStream_t s);
 
 // gemm_simt.cu: C[m, n] = sum_k A[m, k] W[k, n] with epilogue.

@@ -161,20 +161,24 @@ __global__ void k_bwd_envelope(const float* __restrict__ r, const float* __restr
     dENV[bi * d.KN + col] = dmo * bf;
 }
 
-// alpha / weights gradients: block per (spin, ion, 32 columns), rows of that spin strided over
-// the block's 8 row lanes, then a shared-memory reduction.
+// alpha / weights gradients: block per (spin, ion, 32 columns, row segment), the segment's rows of
+// that spin strided over the block's 8 row lanes, then a shared-memory reduction and one atomic
+// add per column and segment.
 __global__ void k_bwd_env_params(const float* __restrict__ r, const float* __restrict__ R, const float* __restrict__ P,
                                  ParamLayout L, Dims d, int B, const float* __restrict__ dENV,
-                                 float* __restrict__ grad) {
+                                 float* __restrict__ grad, int col_chunks, int rows_per_seg) {
     __shared__ float red[2][8][33];
-    const int spin = blockIdx.z, I = blockIdx.y, col = blockIdx.x * 32 + (threadIdx.x & 31), lane8 = threadIdx.x >> 5;
+    const int spin = blockIdx.z, I = blockIdx.y, lane8 = threadIdx.x >> 5;
+    const int cchunk = blockIdx.x % col_chunks, seg = blockIdx.x / col_chunks;
+    const int col = cchunk * 32 + (threadIdx.x & 31);
     const int i0 = spin == 0 ? 0 : d.nu, ns = spin == 0 ? d.nu : d.nd;
+    const int e_begin = seg * rows_per_seg, e_end = min(B * ns, e_begin + rows_per_seg);
     float ga = 0.f, gw = 0.f;
     if (col < d.KN) {
         const float al = P[(spin == 0 ? L.alpha_up : L.alpha_dn) + I * d.KN + col];
         const float w = P[(spin == 0 ? L.weights_up : L.weights_dn) + I * d.KN + col];
         const float a = softplus_f(al), sig = 1.f / (1.f + expf(-al));
-        for (int e = lane8; e < B * ns; e += 8) {
+        for (int e = e_begin + lane8; e < e_end; e += 8) {
             const int b = e / ns, i = i0 + e % ns;
             const int64_t bi = (int64_t)b * d.n + i;
             const float* ri = r + bi * 3;
@@ -466,7 +470,13 @@ static int backward_chunk(const Bwd& w, int Bc, const float* P, const ParamLayou
     // determinants -> Slater matrices -> backflow / envelopes
     k_bwd_dets<<<Bc, 256, 0, s>>>(w.logdet, w.sign, w.Ainv, coeff, d.K, d.n, w.dMO);
     k_bwd_envelope<<<nblk((int64_t)rows * d.KN), 256, 0, s>>>(r, R, P, L, spA, d, Bc, w.BF, w.dMO, w.dBF, w.dENV);
-    k_bwd_env_params<<<dim3((d.KN + 31) / 32, d.N, 2), 256, 0, s>>>(r, R, P, L, d, Bc, w.dENV, grad);
+    {
+        // row segments: about four blocks per SM in total
+        const int cc = (d.KN + 31) / 32, ns_max = std::max(d.nu, d.nd);
+        int segs = std::max(1, std::min((Bc * ns_max + 63) / 64, (4 * 152 + cc * d.N * 2 - 1) / (cc * d.N * 2)));
+        const int rps = (Bc * ns_max + segs - 1) / segs;
+        k_bwd_env_params<<<dim3(cc * segs, d.N, 2), 256, 0, s>>>(r, R, P, L, d, Bc, w.dENV, grad, cc, rps);
+    }
     wgrad_f32(w.H4, d.D, w.dBF, 2 * d.KN, rows, d.D, d.KN, grad + L.bf_up, d.KN, nullptr, nullptr, 0, s);
     wgrad_f32(w.H4, d.D, w.dBF + d.KN, 2 * d.KN, rows, d.D, d.KN, grad + L.bf_dn, d.KN, nullptr, nullptr, 0, s);
     gemm_f32_nt(w.dBF, 2 * d.KN, bf_cat, 2 * d.KN, w.dH, d.D, rows, d.D, 2 * d.KN, 0, s);

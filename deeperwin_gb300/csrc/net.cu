@@ -1021,6 +1021,38 @@ k_envelope_rows(const float* __restrict__ r, const float* __restrict__ Rall, con
     const int k = col / d.n, o = col - (col / d.n) * d.n;
     const int64_t mstride = (int64_t)d.n * d.n;              // per channel
     const bool tang = d.Tp > 1;
+    if (!tang) {
+        // value rows four at a time: the four backflow loads are in flight together
+        for (int r4 = 0; r4 < rows; r4 += 4) {
+            float bfv[4], env4[4];
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int rr = min(r4 + u, rows - 1);
+                const int b = b0 + rr / ns, i = i0 + rr % ns;
+                bfv[u] = __ldg(BF + ((int64_t)b * d.n + i) * ldbf + (spin ? spin_cols : 0) + col);
+            }
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float* gv = se + (size_t)min(r4 + u, rows - 1) * N * 5;
+                float env = 0.f;
+                #pragma unroll
+                for (int I = 0; I < kEnvMaxIons; ++I) {
+                    if (I >= N) break;
+                    const float dd = gv[I * 5 + 3];
+                    if (dd < 0.f) continue;                  // padding ion
+                    env += wv[I] * expf(-av[I] * dd);
+                }
+                env4[u] = env;
+            }
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (r4 + u >= rows) break;
+                const int rr = r4 + u, b = b0 + rr / ns, i = i0 + rr % ns;
+                MO[((int64_t)b * d.K + k) * mstride + i * d.n + o] = env4[u] * bfv[u];
+            }
+        }
+        return;
+    }
     for (int rr = 0; rr < rows; ++rr) {
         const int b = b0 + rr / ns, i = i0 + rr % ns;
         const float* gv = se + (size_t)rr * N * 5;

@@ -192,10 +192,15 @@ static Plan<Act> carve_plan(const Dims& d, int Bc, void* ws) {
 
 static const size_t kChunkBudget = (size_t)6 << 30;   // bytes of activations per walker chunk
 
+// Walkers per chunk: the marginal workspace of one walker (the plan also holds fixed buffers,
+// such as the per-geometry ion maps, that do not grow with the chunk) against the budget.
 template <class Act>
 static int choose_chunk(const Dims& d, int B) {
-    size_t per = carve_plan<Act>(d, 1, nullptr).bytes;
-    int bc = (int)std::max<size_t>(1, kChunkBudget / std::max<size_t>(per, 1));
+    const size_t one = carve_plan<Act>(d, 1, nullptr).bytes, two = carve_plan<Act>(d, 2, nullptr).bytes;
+    const size_t per = std::max<size_t>(two > one ? two - one : one, 1);
+    const size_t fixed = one > per ? one - per : 0;
+    const size_t avail = kChunkBudget > fixed ? kChunkBudget - fixed : per;
+    int bc = (int)std::max<size_t>(1, avail / per);
     return std::min(bc, B);
 }
 

@@ -411,6 +411,219 @@ k_ei_mlp(const float* __restrict__ r, const float* __restrict__ Rall, const int3
     }
 }
 
+// ------------------------------------------------------------------ tangent-mode stream MLPs
+// The same block-level chains with Taylor channels: every entry (pair or electron-ion) is CH
+// consecutive rows (value, derivatives, Laplacian). The dense part of a layer is one
+// [rows x in] x [in x 32] product (bias on value rows only) with 4 x 4 register tiles; the
+// pre-activations go through shared memory, where one thread per (entry, feature) applies the
+// channel-coupling tanh (tanh_taylor) and the residual. Same mathematics as
+// k_pair_streams<3> / k_ei_streams<5>.
+struct MlpSmemT {
+    float H[2][32][kRB + 4];     // activations [buffer][feature][row]
+    float Zs[32][kRB + 4];       // pre-activations of the current layer
+    float W[32 * 32];
+    float bias[32];
+};
+
+// Zs[f][row] = sum_k H[cur][k][row] W[k][f] (+ bias[f] on value rows), 4 x 4 tiles
+template <int CH>
+__device__ __forceinline__ void mlp_tile_t(MlpSmemT& sm, int cur, int in_w) {
+    const int rg = threadIdx.x >> 3, fg = threadIdx.x & 7;
+    float z[4][4];
+    const float4 b4 = *reinterpret_cast<const float4*>(&sm.bias[4 * fg]);
+    #pragma unroll
+    for (int rr = 0; rr < 4; ++rr) {
+        const bool val = ((4 * rg + rr) % CH) == 0;
+        z[rr][0] = val ? b4.x : 0.f; z[rr][1] = val ? b4.y : 0.f; z[rr][2] = val ? b4.z : 0.f; z[rr][3] = val ? b4.w : 0.f;
+    }
+    #pragma unroll 8
+    for (int k = 0; k < in_w; ++k) {
+        const float4 h4 = *reinterpret_cast<const float4*>(&sm.H[cur][k][4 * rg]);
+        const float4 w4 = *reinterpret_cast<const float4*>(&sm.W[k * 32 + 4 * fg]);
+        const float hv[4] = {h4.x, h4.y, h4.z, h4.w};
+        #pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+            z[rr][0] = fmaf(hv[rr], w4.x, z[rr][0]); z[rr][1] = fmaf(hv[rr], w4.y, z[rr][1]);
+            z[rr][2] = fmaf(hv[rr], w4.z, z[rr][2]); z[rr][3] = fmaf(hv[rr], w4.w, z[rr][3]);
+        }
+    }
+    #pragma unroll
+    for (int ff = 0; ff < 4; ++ff)
+        *reinterpret_cast<float4*>(&sm.Zs[4 * fg + ff][4 * rg]) = make_float4(z[0][ff], z[1][ff], z[2][ff], z[3][ff]);
+}
+
+__device__ __forceinline__ void mlp_load_wt(MlpSmemT& sm, const float* __restrict__ W, const float* __restrict__ b,
+                                            int in_w) {
+    for (int e = threadIdx.x; e < in_w * 32; e += blockDim.x) sm.W[e] = __ldg(W + e);
+    if (threadIdx.x < 32) sm.bias[threadIdx.x] = __ldg(b + threadIdx.x);
+}
+
+// 2-el streams with 1-D Taylor channels (f, f', f'' in d_ij): EPB = kRB / 3 unordered pairs
+// per block; WP[l][b][i n + j][3][32] for both orders.
+__global__ void __launch_bounds__(128)
+k_pair_mlp_t(const float* __restrict__ r, const float* __restrict__ P, ParamLayout L, Dims d, int B, int blocks_same,
+             float* __restrict__ WP) {
+    constexpr int CH = 3, EPB = kRB / CH;
+    __shared__ __align__(16) MlpSmemT sm;
+    __shared__ int rw[EPB], ri[EPB], rj[EPB];
+    const int tid = threadIdx.x;
+    const int n = d.n, nu = d.nu, nd = d.nd;
+    const bool same = (int)blockIdx.x < blocks_same;
+    const int cu = nu * (nu + 1) / 2;
+    const int npt = same ? cu + nd * (nd + 1) / 2 : nu * nd;
+    const int64_t g0 = (int64_t)(same ? blockIdx.x : blockIdx.x - blocks_same) * EPB;
+    const int64_t total = (int64_t)B * npt;
+    for (int e = tid; e < 32 * (kRB + 4); e += blockDim.x) sm.H[0][e / (kRB + 4)][e % (kRB + 4)] = 0.f;
+    __syncthreads();
+    for (int q = tid; q < EPB; q += blockDim.x) {
+        const int64_t g = g0 + q;
+        int b = -1, i = 0, j = 0;
+        if (g < total) {
+            b = (int)(g / npt);
+            int p = (int)(g % npt);
+            if (same) {
+                int m = nu, base = 0;
+                if (p >= cu) { p -= cu; m = nd; base = nu; }
+                int a = 0;
+                while (p >= m - a) { p -= m - a; ++a; }
+                i = base + a; j = base + a + p;
+            } else {
+                i = p / nd; j = nu + p % nd;
+            }
+        }
+        rw[q] = b; ri[q] = i; rj[q] = j;
+        float dd = 0.f;
+        if (b >= 0 && i != j) {
+            const float* rb = r + (int64_t)b * n * 3;
+            const float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
+            dd = sqrtf(dx * dx + dy * dy + dz * dz);
+        }
+        // input feature [dist]: value d, d' = 1, d'' = 0; the diagonal is the constant 0 (utils.py:297-300)
+        sm.H[0][0][q * CH] = dd;
+        sm.H[0][0][q * CH + 1] = (b >= 0 && i != j) ? 1.f : 0.f;
+        sm.H[0][0][q * CH + 2] = 0.f;
+    }
+    const int64_t plane = (int64_t)B * n * n;
+    const float rs = 0.70710678118654752f;
+    int cur = 0;
+    for (int l = 0; l < 4; ++l) {
+        const int in_w = d.eew[l];
+        __syncthreads();
+        mlp_load_wt(sm, P + (same ? L.w_same_w[l] : L.w_diff_w[l]), P + (same ? L.w_same_b[l] : L.w_diff_b[l]), in_w);
+        __syncthreads();
+        mlp_tile_t<CH>(sm, cur, in_w);
+        __syncthreads();
+        for (int it = tid; it < EPB * 32; it += blockDim.x) {
+            const int q = it / 32, f = it % 32, b = rw[q];
+            if (b < 0) continue;
+            float z[CH], y[CH];
+            #pragma unroll
+            for (int c = 0; c < CH; ++c) z[c] = sm.Zs[f][q * CH + c];
+            tanh_taylor<CH>(z, y);
+            const int i = ri[q], j = rj[q];
+            const int64_t wb = (int64_t)l * plane + (int64_t)b * n * n;
+            #pragma unroll
+            for (int c = 0; c < CH; ++c) {
+                WP[((wb + i * n + j) * CH + c) * 32 + f] = y[c];
+                if (i != j) WP[((wb + j * n + i) * CH + c) * 32 + f] = y[c];
+            }
+        }
+        if (l == 3) break;
+        __syncthreads();
+        mlp_load_wt(sm, P + (same ? L.h_same_w[l] : L.h_diff_w[l]), P + (same ? L.h_same_b[l] : L.h_diff_b[l]), in_w);
+        __syncthreads();
+        mlp_tile_t<CH>(sm, cur, in_w);
+        __syncthreads();
+        for (int it = tid; it < EPB * 32; it += blockDim.x) {
+            const int q = it / 32, f = it % 32;
+            float z[CH], y[CH];
+            #pragma unroll
+            for (int c = 0; c < CH; ++c) z[c] = sm.Zs[f][q * CH + c];
+            tanh_taylor<CH>(z, y);
+            #pragma unroll
+            for (int c = 0; c < CH; ++c)
+                sm.H[cur ^ 1][f][q * CH + c] = l > 0 ? (sm.H[cur][f][q * CH + c] + y[c]) * rs : y[c];
+        }
+        cur ^= 1;
+    }
+}
+
+// El-ion stream with (value, 3 gradients w.r.t. r_i, Laplacian) channels: EPB = kRB / 5 entries
+// (walker, electron, ion) per block; HE[l][entry][5][32] for levels 0..3; padding ions give
+// zero entries.
+__global__ void __launch_bounds__(128)
+k_ei_mlp_t(const float* __restrict__ r, const float* __restrict__ Rall, const int32_t* __restrict__ Zall,
+           const float* __restrict__ P, ParamLayout L, Dims d, int B, float* __restrict__ HE) {
+    constexpr int CH = 5, EPB = kRB / CH;
+    __shared__ __align__(16) MlpSmemT sm;
+    __shared__ int rok[EPB];
+    const int tid = threadIdx.x;
+    const int nei = d.n * d.N;
+    const int64_t total = (int64_t)B * nei;
+    const int64_t g0 = (int64_t)blockIdx.x * EPB;
+    for (int e = tid; e < 32 * (kRB + 4); e += blockDim.x) sm.H[0][e / (kRB + 4)][e % (kRB + 4)] = 0.f;
+    __syncthreads();
+    for (int q = tid; q < EPB; q += blockDim.x) {
+        const int64_t g = g0 + q;
+        int ok = 0;
+        if (g < total) {
+            const int b = (int)(g / nei), p = (int)(g % nei), i = p / d.N, I = p % d.N;
+            const int sg = seg_of(d, b);
+            if (Zall[(size_t)sg * d.N + I] > 0) {
+                const float* R = Rall + (size_t)sg * d.N * 3;
+                const float* rr = r + ((int64_t)b * d.n + i) * 3;
+                const float sx = rr[0] - R[I * 3], sy = rr[1] - R[I * 3 + 1], sz = rr[2] - R[I * 3 + 2];
+                const float dd = sqrtf(sx * sx + sy * sy + sz * sz);
+                const float sv[3] = {sx, sy, sz};
+                // [d, sx, sy, sz] (input_features.py:56-66), its gradients and Laplacian in r_i
+                sm.H[0][0][q * CH] = dd;
+                #pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    sm.H[0][1 + c][q * CH] = sv[c];
+                    sm.H[0][0][q * CH + 1 + c] = sv[c] / dd;
+                    sm.H[0][1 + c][q * CH + 1 + c] = 1.f;
+                }
+                sm.H[0][0][q * CH + 4] = 2.f / dd;
+                ok = 1;
+            } else {
+                ok = 2;                  // padding ion
+            }
+        }
+        rok[q] = ok;
+    }
+    __syncthreads();
+    // level 0: the input features, zero padded to 32
+    for (int it = tid; it < EPB * CH * 32; it += blockDim.x) {
+        const int q = it / (CH * 32), rc = it % (CH * 32), c = rc / 32, f = rc % 32;
+        if (!rok[q]) continue;
+        HE[((g0 + q) * CH + c) * 32 + f] = rok[q] == 2 ? 0.f : sm.H[0][f][q * CH + c];
+    }
+    const float rs = 0.70710678118654752f;
+    int cur = 0;
+    for (int l = 0; l < 3; ++l) {
+        const int in_w = d.eiw[l];
+        __syncthreads();
+        mlp_load_wt(sm, P + L.h_ei_w[l], P + L.h_ei_b[l], in_w);
+        __syncthreads();
+        mlp_tile_t<CH>(sm, cur, in_w);
+        __syncthreads();
+        for (int it = tid; it < EPB * 32; it += blockDim.x) {
+            const int q = it / 32, f = it % 32;
+            float z[CH], y[CH];
+            #pragma unroll
+            for (int c = 0; c < CH; ++c) z[c] = sm.Zs[f][q * CH + c];
+            tanh_taylor<CH>(z, y);
+            #pragma unroll
+            for (int c = 0; c < CH; ++c) {
+                const float hn = rok[q] == 2 ? 0.f : (l > 0 ? (sm.H[cur][f][q * CH + c] + y[c]) * rs : y[c]);
+                sm.H[cur ^ 1][f][q * CH + c] = hn;
+                if (rok[q]) HE[((int64_t)(l + 1) * total * CH + (g0 + q) * CH + c) * 32 + f] = hn;
+            }
+        }
+        cur ^= 1;
+    }
+}
+
 template <int CH>
 __global__ void __launch_bounds__(128)
 k_ei_streams(const float* __restrict__ r, const float* __restrict__ R, const int32_t* __restrict__ Z,
@@ -923,8 +1136,17 @@ void launch_streams(const float* r, const float* R, const int32_t* Z, const floa
         size_t sm3 = 128 * (3 * 32 + 1) * sizeof(float), sm5 = 128 * (5 * 32 + 1) * sizeof(float);
         cudaFuncSetAttribute(k_ei_streams<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm5);
         cudaFuncSetAttribute(k_pair_streams<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
-        k_pair_streams<3><<<blocks(npair), 128, sm3, s>>>(r, P, L, d, B, WP, nullptr);
-        k_ei_streams<5><<<blocks(nei), 128, sm5, s>>>(r, R, Z, P, L, d, B, HE);
+        if (d.E == 32 && d.EI == 32) {
+            constexpr int EP = kRB / 3, EE = kRB / 5;
+            const int64_t same_rows = (int64_t)B * (d.nu * (d.nu + 1) / 2 + d.nd * (d.nd + 1) / 2);
+            const int64_t diff_rows = (int64_t)B * d.nu * d.nd;
+            const int bs = (int)((same_rows + EP - 1) / EP), bd = (int)((diff_rows + EP - 1) / EP);
+            k_pair_mlp_t<<<bs + bd, 128, 0, s>>>(r, P, L, d, B, bs, WP);
+            k_ei_mlp_t<<<(unsigned)((nei + EE - 1) / EE), 128, 0, s>>>(r, R, Z, P, L, d, B, HE);
+        } else {
+            k_pair_streams<3><<<blocks(npair), 128, sm3, s>>>(r, P, L, d, B, WP, nullptr);
+            k_ei_streams<5><<<blocks(nei), 128, sm5, s>>>(r, R, Z, P, L, d, B, HE);
+        }
     } else {
         const int64_t same_rows = (int64_t)B * (d.nu * (d.nu + 1) / 2 + d.nd * (d.nd + 1) / 2);
         const int64_t diff_rows = (int64_t)B * d.nu * d.nd;

@@ -171,7 +171,7 @@ static Plan<Act> carve_plan(const Dims& d, int Bc, void* ws) {
     int pc = d.Tp > 1 ? 3 : 1, ec = d.Tp > 1 ? 5 : 1;
     p.WP = c.take<float>((int64_t)4 * Bc * d.n * d.n * pc * 32);
     p.HE = c.take<float>((int64_t)4 * Bc * d.n * d.N * ec * 32);
-    p.BF = c.take<float>(rows * 2 * d.KN);
+    p.BF = c.take<float>(rows * round_up(2 * d.KN, 4));   // row pitch padded to 16 bytes (TMA stores)
     p.MO = c.take<float>((int64_t)Bc * d.K * d.T * d.n * d.n);
     p.logdet = c.take<double>((int64_t)Bc * d.K);
     p.sign = c.take<double>((int64_t)Bc * d.K);
@@ -319,7 +319,7 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
     // that spin's electron rows of every walker (walker-block tensor maps), so each row gets only
     // its own spin's KN columns. Otherwise every row times [W_up | W_dn] and the envelope kernel
     // takes the half that matches the electron's spin.
-    int ldbf = 2 * d.KN, spin_cols = d.KN;
+    int ldbf = round_up(2 * d.KN, 4), spin_cols = d.KN;
     const bool per_spin = tang && pt >= 1 && (d.nu * d.Tp) % 32 == 0 && (d.nd * d.Tp) % 32 == 0 && d.KN % 4 == 0;
     if (per_spin) {
         ldbf = d.KN;
@@ -343,7 +343,7 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         WRef wb; wb.f32 = pre.bf_cat; wb.ldw = 2 * d.KN;
         if (pt >= 1) wb.hi = pre.bf_bf[0];
         if (pt >= 2) wb.lo = pre.bf_bf[1];
-        DW_TIMED("backflow_gemm", DW_CHECK(MM<Act>::mm(H, kXW, wb, p.BF, 2 * d.KN, rows, 2 * d.KN, d.D, e0, s)));
+        DW_TIMED("backflow_gemm", DW_CHECK(MM<Act>::mm(H, kXW, wb, p.BF, ldbf, rows, 2 * d.KN, d.D, e0, s)));
     }
     DW_TIMED("envelope", launch_envelope(r, R, Z, P, L, pre.sp_alpha, d, Bc, p.BF, ldbf, spin_cols, p.MO, s));
     if (precision == DW_PRECISION_FP32) DW_TIMED("slogdet", launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));

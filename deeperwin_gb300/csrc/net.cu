@@ -990,7 +990,7 @@ k_conv_walker(const float* __restrict__ r, const float* __restrict__ WPl, const 
     for (int e = threadIdx.x; e < n * Tp * 8; e += blockDim.x)
         reinterpret_cast<float4*>(hm)[e] = __ldg(reinterpret_cast<const float4*>(hmb) + e);
     const float* rb = r + (size_t)b * n * 3;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    for (int e = threadIdx.x; e < (Tp > 1 ? n * n : 0); e += blockDim.x) {   // pair geometry: tangent rows only
         const int i = e / n, j = e % n;
         float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
         if (i != j) {
@@ -1011,6 +1011,7 @@ k_conv_walker(const float* __restrict__ r, const float* __restrict__ WPl, const 
             if (col < E) {
                 const int f = col;
                 const float* wrow = wpb + (size_t)i * n * pch * 32 + f;      // record (i, j) at j * pch * 32
+                #pragma unroll 4
                 for (int j = 0; j < n; ++j) v += __ldg(wrow + j * pch * 32) * hm[(j * Tp + t) * 32 + f];
                 if (t >= 1 && t <= 3 * n) {
                     const int m = (t - 1) / 3, c = (t - 1) % 3;
@@ -1043,6 +1044,7 @@ k_conv_walker(const float* __restrict__ r, const float* __restrict__ WPl, const 
                 if (ch >= 0) {
                     const float* he = heb + (size_t)i * d.N * ech * 32;
                     const float* hs = himl + (size_t)seg_of(d, b) * 4 * d.N * 32;
+                    #pragma unroll 4
                     for (int I = 0; I < d.N; ++I) v += __ldg(he + (I * ech + ch) * 32 + f) * __ldg(hs + I * 32 + f);
                 }
             }

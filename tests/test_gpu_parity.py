@@ -195,3 +195,68 @@ def test_local_energy_many_channels(cuda, name):
         E = E.cpu().numpy().astype(np.float64)
         assert np.all(np.abs(E - E_ref) <= tol * S), (prec, E, E_ref, S)
         np.testing.assert_allclose(lp.cpu().numpy(), lp_ref, rtol=1e-4, atol=1e-3)
+
+
+def _count_case(n_el, K, seed):
+    """A molecule with n_el electrons: an H chain up to 16 atoms, heavier atoms beyond."""
+    heavy = {18: [8, 8, 1, 1], 21: [8, 7, 6], 26: [8, 8, 8, 1, 1]}
+    if n_el <= 16:
+        mol = A.h_chain(n_el, 1.6)
+    else:
+        Z = np.array(heavy[n_el])
+        R = np.zeros((len(Z), 3))
+        R[:, 0] = np.arange(len(Z)) * 2.4
+        R[:, 1] = (np.arange(len(Z)) % 2) * 1.1
+        mol = A.Molecule(R=R, Z=Z, n_el=n_el, n_up=(n_el + 1) // 2, name=f"Z{n_el}")
+    a = A.arch_for(mol, K)
+    p = P.init_params(a, seed, bias_std=0.1, envelope_jitter=0.2)
+    r = A.init_walkers(mol, 3, seed=seed + 5)
+    return mol, a, p, r
+
+
+def _slater_condition(p, a, r, mol):
+    """Largest 2-norm condition number over the determinants of each walker (oracle matrices)."""
+    tp = O.tparams(p)
+    h, de = O.embedding(tp, a, O._t(r), O._t(mol.R), mol.Z)
+    mo = O.orbitals(tp, a, h, de).numpy()
+    return np.array([max(np.linalg.cond(mo[b, k]) for k in range(mo.shape[1])) for b in range(mo.shape[0])])
+
+
+# Electron counts chosen to reach every determinant code path: one matrix per thread in shared
+# memory (n <= 4, 8, 10, 12), two lanes per matrix (13..16), lanes-in-registers and warp forms
+# (n > 16); determinant-tangent tiles of padded size 4 .. 28; per-spin and concatenated backflow
+# (odd K n, odd n_spin x Tp).
+# Tolerance per walker: log psi^2 = 2 log|det| inherits the relative error of the Slater-matrix
+# entries amplified by the condition number kappa of the matrices, so the bound is the form's
+# base tolerance plus kappa times the entry accuracy (1e-7 for FP32 entries and FP32 LU, 1e-5 for
+# split-BF16 GEMM entries: hi + lo represents each operand to about 2^-17, and sums of 256
+# products cancel). Random-init Slater matrices of the heavier atoms reach kappa ~ 1e6.
+@pytest.mark.parametrize("n_el,K", [(3, 2), (5, 3), (7, 2), (9, 4), (11, 2), (12, 3), (13, 2), (14, 4), (15, 2),
+                                    (18, 2), (21, 1), (26, 1)])
+def test_log_psi_across_electron_counts(cuda, n_el, K):
+    mol, a, p, r = _count_case(n_el, K, n_el)
+    lp_ref = O.log_psi_sqr(O.tparams(p), a, r, mol.R, mol.Z)[1].numpy()
+    kappa = _slater_condition(p, a, r, mol)
+    for prec, rtol, atol, eps in (("fp32", 1e-5, 1e-4, 1e-7), ("mixed", 1e-4, 1e-3, 1e-5)):
+        params = api.Params.from_dict(a, p, prec)
+        _, lp = api.log_psi_sqr(params, a.n_up, a.n_dn, r, mol.R, mol.Z)
+        err = np.abs(lp.cpu().numpy().astype(np.float64) - lp_ref)
+        bound = atol + rtol * np.abs(lp_ref) + eps * kappa
+        assert np.all(err <= bound), (prec, n_el, err, bound, kappa)
+
+
+@pytest.mark.parametrize("n_el,K", [(3, 2), (5, 3), (11, 2), (13, 2), (15, 2), (21, 1)])
+def test_local_energy_across_electron_counts(cuda, n_el, K):
+    mol, a, p, r = _count_case(n_el, K, 100 + n_el)
+    E_ref, lp_ref, g_ref, lap = [x.numpy() for x in O.local_energy(O.tparams(p), a, r, mol.R, mol.Z)]
+    S = 0.25 * np.abs(lap) + 0.125 * (g_ref ** 2).sum(-1) + np.abs(O.potential_energy(r, mol.R, mol.Z).numpy())
+    kappa = _slater_condition(p, a, r, mol)
+    # E_L bound: the form's tolerance on S plus a conditioning term (kappa times 1e-8 / 1e-7 of S)
+    for prec, tol, eps, eps_e in (("fp32", 5e-5, 1e-7, 1e-8), ("mixed", 1e-4, 1e-5, 1e-7)):
+        params = api.Params.from_dict(a, p, prec)
+        E, lp, _ = api.local_energy(params, (a.n_up, a.n_dn), r, mol.R, mol.Z, return_grad=True)
+        E = E.cpu().numpy().astype(np.float64)
+        bound = (tol + eps_e * kappa) * S
+        assert np.all(np.abs(E - E_ref) <= bound), (prec, n_el, E, E_ref, S, kappa)
+        lp_bound = 1e-3 + 1e-4 * np.abs(lp_ref) + 10 * eps * kappa
+        assert np.all(np.abs(lp.cpu().numpy() - lp_ref) <= lp_bound), (prec, n_el, lp.cpu().numpy(), lp_ref)

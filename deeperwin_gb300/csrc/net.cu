@@ -970,6 +970,68 @@ k_conv_tile(const float* __restrict__ r, const float* __restrict__ WPl, const fl
     }
 }
 
+// Value rows (Tp = 1): thread per (walker, electron, 8-column octet) of the conv_ee / conv_ei
+// block of the layer input. Each thread accumulates its 8 columns over the n pair records (or
+// the N ion records) with 16-byte loads of w_ij / h_ei and of h_map_j / the ion map (the latter
+// shared by all electrons of a walker, served from L1); no shared-memory staging or barriers.
+// Same mathematics as k_conv_walker on value rows.
+template <class Act>
+__global__ void __launch_bounds__(256)
+k_conv_value(const float* __restrict__ WPl, const float* __restrict__ HM, const float* __restrict__ HEl,
+             const float* __restrict__ himl, Dims d, int l, int B, Act* __restrict__ X, int ldx) {
+    const int n = d.n, N = d.N, E = d.E, eiw = d.eiw[l], hw = d.hw[l];
+    const int oe = E / 8, oi = (eiw + 7) / 8, octs = oe + oi;
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (int64_t)B * n * octs) return;
+    const int oct = (int)(gid % octs);
+    const int64_t bi = gid / octs;                 // walker * n + electron
+    const int b = (int)(bi / n), i = (int)(bi % n);
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int col, ncol;
+    if (oct < oe) {
+        const int f0 = 8 * oct;
+        const float* w = WPl + ((int64_t)b * n * n + (int64_t)i * n) * 32 + f0;
+        const float* h = HM + (int64_t)b * n * 32 + f0;
+        #pragma unroll 4
+        for (int j = 0; j < n; ++j) {
+            const float4 w0 = __ldg(reinterpret_cast<const float4*>(w + j * 32));
+            const float4 w1 = __ldg(reinterpret_cast<const float4*>(w + j * 32 + 4));
+            const float4 h0 = __ldg(reinterpret_cast<const float4*>(h + j * 32));
+            const float4 h1 = __ldg(reinterpret_cast<const float4*>(h + j * 32 + 4));
+            acc[0] = fmaf(w0.x, h0.x, acc[0]); acc[1] = fmaf(w0.y, h0.y, acc[1]);
+            acc[2] = fmaf(w0.z, h0.z, acc[2]); acc[3] = fmaf(w0.w, h0.w, acc[3]);
+            acc[4] = fmaf(w1.x, h1.x, acc[4]); acc[5] = fmaf(w1.y, h1.y, acc[5]);
+            acc[6] = fmaf(w1.z, h1.z, acc[6]); acc[7] = fmaf(w1.w, h1.w, acc[7]);
+        }
+        col = hw + f0;
+        ncol = 8;
+    } else {
+        const int f0 = 8 * (oct - oe);
+        const float* he = HEl + ((int64_t)b * n * N + (int64_t)i * N) * 32 + f0;
+        const float* hs = himl + (size_t)seg_of(d, b) * 4 * N * 32 + f0;
+        #pragma unroll 4
+        for (int I = 0; I < N; ++I) {
+            const float4 e0 = __ldg(reinterpret_cast<const float4*>(he + I * 32));
+            const float4 e1 = __ldg(reinterpret_cast<const float4*>(he + I * 32 + 4));
+            const float4 s0 = __ldg(reinterpret_cast<const float4*>(hs + I * 32));
+            const float4 s1 = __ldg(reinterpret_cast<const float4*>(hs + I * 32 + 4));
+            acc[0] = fmaf(e0.x, s0.x, acc[0]); acc[1] = fmaf(e0.y, s0.y, acc[1]);
+            acc[2] = fmaf(e0.z, s0.z, acc[2]); acc[3] = fmaf(e0.w, s0.w, acc[3]);
+            acc[4] = fmaf(e1.x, s1.x, acc[4]); acc[5] = fmaf(e1.y, s1.y, acc[5]);
+            acc[6] = fmaf(e1.z, s1.z, acc[6]); acc[7] = fmaf(e1.w, s1.w, acc[7]);
+        }
+        col = hw + E + f0;
+        ncol = min(8, eiw - f0);
+    }
+    if (ncol == 8 && (col % 8) == 0 && (ldx % 8) == 0) {
+        ActIO<Act>::store8(X, bi, ldx, col, acc);
+    } else {
+        #pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < ncol) ActIO<Act>::store(X, bi, ldx, col + k, acc[k]);
+    }
+}
+
 // Block per walker: the walker's h_map tangents (n x Tp x 32) and pair geometry are staged in
 // shared memory once, then every (electron, channel, column) output of conv_ee / conv_ei is
 // formed from shared memory. Same mathematics as k_conv.
@@ -1188,6 +1250,13 @@ void launch_conv(const float* r, const float* WPl, const float* HM, const float*
             case 4: go(k_conv_tile<Act, 4>); break;
             default: go(k_conv_tile<Act, 8>); break;
         }
+        count_launch();
+        return;
+    }
+    if (d.Tp == 1 && d.E % 8 == 0) {
+        const int octs = d.E / 8 + (d.eiw[l] + 7) / 8;
+        const int64_t threads = (int64_t)B * d.n * octs;
+        k_conv_value<Act><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(WPl, HM, HEl, himl, d, l, B, X, ldx);
         count_launch();
         return;
     }

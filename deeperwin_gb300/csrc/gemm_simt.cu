@@ -91,9 +91,109 @@ k_gemm_f32(const float* __restrict__ A, int lda, const float* __restrict__ W, in
     }
 }
 
+// Wide shapes (N >= 128, K and the leading dimensions multiples of 4, 16-byte aligned operands):
+// 128 x 128 tiles, 256 threads with an 8 x 8 patch each (two 4-wide groups per direction, so a
+// warp's 16-byte shared reads are consecutive: 4 LDS.128 feed 64 FMAs), 16-byte global loads
+// staged through registers into double-buffered shared memory. Same epilogue as k_gemm_f32.
+template <bool TRANS_W, bool ACC>
+__global__ void __launch_bounds__(256)
+k_gemm_f32v(const float* __restrict__ A, int lda, const float* __restrict__ W, int ldw, float* __restrict__ C, int ldc,
+            int M, int N, int K, GemmEpi epi, int64_t sA, int64_t sC) {
+    constexpr int BM = 128, BN = 128, BK = 8;
+    A += blockIdx.z * sA;
+    C += blockIdx.z * sC;
+    __shared__ __align__(16) float As[2][BK][BM];
+    __shared__ __align__(16) float Ws[2][BK][BN];
+    const int tid = threadIdx.x, tr = tid / 16, tc = tid % 16;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    float acc[8][8];
+    #pragma unroll
+    for (int i = 0; i < 8; ++i)
+        #pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    // per thread: one float4 of A (row tid / 2, k half tid % 2) and one of W
+    const int ar = tid / 2, ah = (tid % 2) * 4;
+    const int wk = tid / 32, wn = (tid % 32) * 4;          // non-transposed W: [K][N]
+    float4 ra, rw;
+    auto gload = [&](int k0) {
+        const int gm = m0 + ar, gk = k0 + ah;
+        ra = (gm < M && gk < K) ? __ldg(reinterpret_cast<const float4*>(A + (int64_t)gm * lda + gk))
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (TRANS_W) {
+            const int gn = n0 + ar;
+            rw = (gn < N && gk < K) ? __ldg(reinterpret_cast<const float4*>(W + (int64_t)gn * ldw + gk))
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            const int kk = k0 + wk, gn = n0 + wn;
+            rw = (kk < K && gn < N) ? __ldg(reinterpret_cast<const float4*>(W + (int64_t)kk * ldw + gn))
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+    auto sstore = [&](int buf) {
+        As[buf][ah + 0][ar] = ra.x; As[buf][ah + 1][ar] = ra.y; As[buf][ah + 2][ar] = ra.z; As[buf][ah + 3][ar] = ra.w;
+        if (TRANS_W) {
+            Ws[buf][ah + 0][ar] = rw.x; Ws[buf][ah + 1][ar] = rw.y; Ws[buf][ah + 2][ar] = rw.z; Ws[buf][ah + 3][ar] = rw.w;
+        } else {
+            *reinterpret_cast<float4*>(&Ws[buf][wk][wn]) = rw;
+        }
+    };
+    const int nk = (K + BK - 1) / BK;
+    gload(0);
+    sstore(0);
+    __syncthreads();
+    for (int kt = 0; kt < nk; ++kt) {
+        const int buf = kt & 1;
+        if (kt + 1 < nk) gload((kt + 1) * BK);
+        #pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][4 * tr]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][64 + 4 * tr]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&Ws[buf][kk][4 * tc]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&Ws[buf][kk][64 + 4 * tc]);
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+            #pragma unroll
+            for (int i = 0; i < 8; ++i)
+                #pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+        if (kt + 1 < nk) sstore(buf ^ 1);
+        __syncthreads();
+    }
+    #pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int m = m0 + (i < 4 ? 4 * tr + i : 64 + 4 * tr + i - 4);
+        if (m >= M) continue;
+        const int t = m % epi.Tp;
+        const float* rb = epi.rowbias ? epi.rowbias + ((int64_t)(m / epi.rows_per_walker) * epi.Tp + t) * epi.ldrb : nullptr;
+        #pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int n = n0 + (j < 4 ? 4 * tc + j : 64 + 4 * tc + j - 4);
+            if (n >= N) continue;
+            float v = acc[i][j];
+            if (epi.bias && t == 0) v += epi.bias[n];
+            if (rb) v += rb[n];
+            if (epi.act == 1) v = tanhf(v);
+            if (ACC) C[(int64_t)m * ldc + n] += v;
+            else C[(int64_t)m * ldc + n] = v;
+        }
+    }
+}
+
+static bool vec_ok(const float* A, int lda, const float* W, int ldw, int N, int K, bool trans_w) {
+    auto al = [](const void* p) { return ((uintptr_t)p & 15) == 0; };
+    return N >= 128 && K % 4 == 0 && lda % 4 == 0 && ldw % 4 == 0 && al(A) && al(W) && (trans_w || N % 4 == 0);
+}
+
 void gemm_f32(const float* A, int lda, const float* W, int ldw, float* C, int ldc, int M, int N, int K,
               const GemmEpi& epi, int batch, int64_t sA, int64_t sC, cudaStream_t s) {
     if (M <= 0 || N <= 0) return;
+    if (vec_ok(A, lda, W, ldw, N, K, false) && (batch == 1 || (sA % 4 == 0))) {
+        dim3 g((N + 127) / 128, (M + 127) / 128, batch);
+        k_gemm_f32v<false, false><<<g, 256, 0, s>>>(A, lda, W, ldw, C, ldc, M, N, K, epi, sA, sC);
+        count_launch();
+        return;
+    }
     if (N <= 32) {
         constexpr int BM = 128, BN = 32;
         dim3 g((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
@@ -110,6 +210,13 @@ void gemm_f32_nt(const float* A, int lda, const float* W, int ldw, float* C, int
                  int accumulate, cudaStream_t s) {
     if (M <= 0 || N <= 0) return;
     GemmEpi epi;
+    if (vec_ok(A, lda, W, ldw, N, K, true)) {
+        dim3 g((N + 127) / 128, (M + 127) / 128, 1);
+        if (accumulate) k_gemm_f32v<true, true><<<g, 256, 0, s>>>(A, lda, W, ldw, C, ldc, M, N, K, epi, 0, 0);
+        else k_gemm_f32v<true, false><<<g, 256, 0, s>>>(A, lda, W, ldw, C, ldc, M, N, K, epi, 0, 0);
+        count_launch();
+        return;
+    }
     constexpr int BM = 128, BN = 64;
     dim3 g((N + BN - 1) / BN, (M + BM - 1) / BM, 1);
     if (accumulate)

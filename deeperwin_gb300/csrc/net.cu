@@ -836,12 +836,11 @@ __global__ void k_conv(const float* __restrict__ r, const float* __restrict__ WP
 // j-sums of the electron's own gradient channels and of the Laplacian. Columns are then written
 // eight at a time (16-byte stores). conv_ei is non-zero on 5 channels per electron only. Same
 // mathematics as k_conv.
-template <class Act, int TT>
+template <class Act, int TT, int TI>
 __global__ void __launch_bounds__(512)
 k_conv_tile(const float* __restrict__ r, const float* __restrict__ WPl, const float* __restrict__ HM,
             const float* __restrict__ HEl, const float* __restrict__ himl, Dims d, int l, int B, Act* __restrict__ X,
             int ldx) {
-    constexpr int TI = 4;
     extern __shared__ __align__(16) float smc[];
     const int n = d.n, Tp = d.Tp, T = d.T;
     const int NW = Tp / TT;
@@ -1236,20 +1235,27 @@ template <class Act>
 void launch_conv(const float* r, const float* WPl, const float* HM, const float* HEl, const float* himl, const Dims& d,
                  int l, int B, Act* X, int ldx, cudaStream_t s) {
     if (d.Tp >= 8 && d.Tp <= 128 && d.E == 32) {
-        const unsigned grid = (unsigned)B * ((d.n + 3) / 4);
+        // 4 electrons per block (8 or 5 per block measured slower: larger shared-memory tiles and
+        // product-rule loops outweigh the extra reuse of each h_map load)
+        constexpr int TI = 4;
+        const unsigned grid = (unsigned)B * ((d.n + TI - 1) / TI);
         const int TT = d.Tp >= 64 ? 8 : d.Tp / 8;
         const int NW = d.Tp / TT;
-        const size_t smem = ((size_t)4 * d.Tp * 32 + (size_t)NW * 4 * 4 * 32 + 4 * 5 * 32) * sizeof(float);
+        const size_t smem = ((size_t)TI * d.Tp * 32 + (size_t)NW * TI * 4 * 32 + (size_t)TI * 5 * 32) * sizeof(float);
         auto go = [&](auto kern) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             kern<<<grid, NW * 32, smem, s>>>(r, WPl, HM, HEl, himl, d, l, B, X, ldx);
         };
-        switch (TT) {
-            case 1: go(k_conv_tile<Act, 1>); break;
-            case 2: go(k_conv_tile<Act, 2>); break;
-            case 4: go(k_conv_tile<Act, 4>); break;
-            default: go(k_conv_tile<Act, 8>); break;
-        }
+        auto pick = [&](auto ti) {
+            constexpr int T_I = decltype(ti)::value;
+            switch (TT) {
+                case 1: go(k_conv_tile<Act, 1, T_I>); break;
+                case 2: go(k_conv_tile<Act, 2, T_I>); break;
+                case 4: go(k_conv_tile<Act, 4, T_I>); break;
+                default: go(k_conv_tile<Act, 8, T_I>); break;
+            }
+        };
+        pick(std::integral_constant<int, TI>());
         count_launch();
         return;
     }

@@ -653,7 +653,7 @@ void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, 
             else if (n <= 8) launch_slogdet_thread<8, 64>(MO, n, d.T, nmat, logdet, sign, s);
             else if (n <= 10) launch_slogdet_thread<10, 64>(MO, n, d.T, nmat, logdet, sign, s);
             else if (n <= 12) launch_slogdet_thread<12, 64>(MO, n, d.T, nmat, logdet, sign, s);
-            else launch_slogdet_split<16, 2, false>(MO, n, d.T, nmat, logdet, sign, nullptr, s);
+            else launch_slogdet_split<16, 4, false>(MO, n, d.T, nmat, logdet, sign, nullptr, s);
             count_launch();
             return;
         }
@@ -674,7 +674,7 @@ void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, 
             else if (n <= 8) launch_slogdet_inv_thread<8, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
             else if (n <= 10) launch_slogdet_inv_thread<10, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
             else if (n <= 12) launch_slogdet_inv_thread<12, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
-            else launch_slogdet_split<16, 2, true>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
+            else launch_slogdet_split<16, 4, true>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
             count_launch();
             return;
         }

@@ -472,8 +472,12 @@ static int backward_chunk(const Bwd& w, int Bc, const float* P, const ParamLayou
     k_bwd_envelope<<<nblk((int64_t)rows * d.KN), 256, 0, s>>>(r, R, P, L, spA, d, Bc, w.BF, w.dMO, w.dBF, w.dENV);
     {
         // row segments: about four blocks per SM in total
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        sms = sms > 0 ? sms : 152;
         const int cc = (d.KN + 31) / 32, ns_max = std::max(d.nu, d.nd);
-        int segs = std::max(1, std::min((Bc * ns_max + 63) / 64, (4 * 152 + cc * d.N * 2 - 1) / (cc * d.N * 2)));
+        int segs = std::max(1, std::min((Bc * ns_max + 63) / 64, (4 * sms + cc * d.N * 2 - 1) / (cc * d.N * 2)));
         const int rps = (Bc * ns_max + segs - 1) / segs;
         k_bwd_env_params<<<dim3(cc * segs, d.N, 2), 256, 0, s>>>(r, R, P, L, d, Bc, w.dENV, grad, cc, rps);
     }

@@ -48,34 +48,42 @@ __global__ void k_ion_maps(const float* __restrict__ P, ParamLayout L, Dims d, c
 template <class Act>
 __global__ void k_features(const float* __restrict__ r, const float* __restrict__ Rall, const int32_t* __restrict__ Zall,
                            Dims d, int B, Act* __restrict__ X0) {
-    int bi = blockIdx.x;          // b * n + i
-    int i = bi % d.n;
+    __shared__ float geo[16][5];  // per ion: s_x, s_y, s_z, |s|, 1/|s|; |s| < 0 marks a padding ion
+    const int bi = blockIdx.x;    // b * n + i
+    const int i = bi % d.n;
     const int sg = seg_of(d, bi / d.n);
     const float* R = Rall + (size_t)sg * d.N * 3;
     const int32_t* Z = Zall + (size_t)sg * d.N;
     const float* ri = r + (int64_t)bi * 3;
-    int width = d.kw[0];
-    int nf = 4 * d.N;
-    int64_t row0 = (int64_t)bi * d.Tp;
-    for (int idx = threadIdx.x; idx < d.Tp * width; idx += blockDim.x) {
-        int t = idx / width, col = idx % width;
-        if (col >= nf && col < nf + d.E + 4) continue;   // conv columns written by k_conv
-        float v = 0.f;
-        if (col < nf && Z[col >> 2] > 0) {
-            int I = col >> 2, q = col & 3;
-            float sx = ri[0] - R[I * 3 + 0], sy = ri[1] - R[I * 3 + 1], sz = ri[2] - R[I * 3 + 2];
-            float dd = sqrtf(sx * sx + sy * sy + sz * sz);
-            float s[3] = {sx, sy, sz};
-            if (t == 0) {
-                v = q == 0 ? dd : s[q - 1];
-            } else if (t == d.lap) {
-                v = q == 0 ? 2.f / dd : 0.f;
-            } else if (t >= 1 && t <= 3 * d.n) {
-                int m = (t - 1) / 3, c = (t - 1) % 3;
-                if (m == i) v = q == 0 ? s[c] / dd : (q - 1 == c ? 1.f : 0.f);
+    if (threadIdx.x < d.N) {
+        const int I = threadIdx.x;
+        const float sx = ri[0] - R[I * 3 + 0], sy = ri[1] - R[I * 3 + 1], sz = ri[2] - R[I * 3 + 2];
+        const float dd = sqrtf(sx * sx + sy * sy + sz * sz);
+        geo[I][0] = sx; geo[I][1] = sy; geo[I][2] = sz;
+        geo[I][3] = Z[I] > 0 ? dd : -1.f;
+        geo[I][4] = 1.f / dd;
+    }
+    __syncthreads();
+    const int width = d.kw[0], nf = 4 * d.N;
+    const int64_t row0 = (int64_t)bi * d.Tp;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int t = warp; t < d.Tp; t += nwarps) {
+        // channel t: 0 value, 1 + 3 m + c derivative by r_m,c (non-zero for m == i only), lap
+        const int c = (t >= 1 && t <= 3 * d.n && (t - 1) / 3 == i) ? (t - 1) % 3 : -1;
+        for (int col = lane; col < width; col += 32) {
+            if (col >= nf && col < nf + d.E + 4) continue;   // conv columns written by the convolution
+            float v = 0.f;
+            if (col < nf) {
+                const int I = col >> 2, q = col & 3;
+                const float dd = geo[I][3];
+                if (dd >= 0.f) {
+                    if (t == 0) v = q == 0 ? dd : geo[I][q - 1];
+                    else if (t == d.lap) v = q == 0 ? 2.f * geo[I][4] : 0.f;
+                    else if (c >= 0) v = q == 0 ? geo[I][c] * geo[I][4] : (q - 1 == c ? 1.f : 0.f);
+                }
             }
+            ActIO<Act>::store(X0, row0 + t, width, col, v);
         }
-        ActIO<Act>::store(X0, row0 + t, width, col, v);
     }
 }
 
@@ -1188,7 +1196,8 @@ void launch_ion_maps(const float* P, const ParamLayout& L, const Dims& d, const 
 }
 template <class Act>
 void launch_features(const float* r, const float* R, const int32_t* Z, const Dims& d, int B, Act* X0, cudaStream_t s) {
-    k_features<Act><<<B * d.n, 256, 0, s>>>(r, R, Z, d, B, X0); count_launch();
+    const int fthreads = std::min(256, 32 * d.Tp);        // one warp per channel row, up to 8 warps
+    k_features<Act><<<B * d.n, fthreads, 0, s>>>(r, R, Z, d, B, X0); count_launch();
 }
 void launch_streams(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,
                     const Dims& d, int B, float* WP, float* HE, cudaStream_t s, float* HP) {

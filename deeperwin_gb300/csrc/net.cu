@@ -1161,11 +1161,22 @@ __global__ void k_envelope(const float* __restrict__ r, const float* __restrict_
     float bf0 = bf[0];
     mo[0] = env * bf0;
     if (d.Tp == 1) return;
-    for (int t = 1; t <= 3 * d.n; ++t) {
-        float v = env * bf[(int64_t)t * ldbf];
-        int m = (t - 1) / 3, c = (t - 1) % 3;
-        if (m == i) v += g[c] * bf0;
-        mo[t * mstride] = v;
+    // gradient channels four at a time (the four backflow loads in flight together); the
+    // electron's own three coordinates also carry the envelope gradient times the value row
+    const int n3 = 3 * d.n;
+    for (int t0 = 1; t0 <= n3; t0 += 4) {
+        float bv[4];
+        #pragma unroll
+        for (int u = 0; u < 4; ++u) bv[u] = t0 + u <= n3 ? __ldg(bf + (int64_t)(t0 + u) * ldbf) : 0.f;
+        #pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int t = t0 + u;
+            if (t > n3) break;
+            float v = env * bv[u];
+            const unsigned c = (unsigned)(t - 1 - 3 * i);
+            if (c < 3u) v += (c == 0 ? g[0] : (c == 1 ? g[1] : g[2])) * bf0;
+            mo[t * mstride] = v;
+        }
     }
     float vl = env * bf[(int64_t)d.lap * ldbf] + lapv * bf0;
     for (int c = 0; c < 3; ++c) vl += 2.f * g[c] * bf[(int64_t)(1 + 3 * i + c) * ldbf];

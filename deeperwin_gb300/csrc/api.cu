@@ -275,7 +275,10 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         return w;
     };
     DW_TIMED("features", launch_features<Act>(r, R, Z, d, Bc, p.X0, s));
-    DW_TIMED("streams", launch_streams(r, R, Z, P, L, d, Bc, p.WP, p.HE, s));
+    // el-ion stream reduced over the ions inside the stream kernel where possible (conv_ei per
+    // electron and level in the HE buffer instead of the full stream)
+    const bool ei_fused = ei_fusable(d);
+    DW_TIMED("streams", launch_streams(r, R, Z, P, L, d, Bc, p.WP, p.HE, s, nullptr, ei_fused ? p.him : nullptr));
     Act* xin = p.X0;
     int ldin = d.kw[0];
     int pc = tang ? 3 : 1, ec = tang ? 5 : 1;
@@ -293,9 +296,10 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         if (tang) DW_TIMED("map_gemm", DW_CHECK(MM<Act>::mm_fl(xin, ldin, wmap, p.HM, d.E, rows, d.E, hw, e2, d, p.Zb, s)));
         else DW_TIMED("map_gemm", DW_CHECK(MM<Act>::mm(xin, ldin, wmap, p.HM, d.E, rows, d.E, hw, e2, s)));
         // (c) SchNet convolutions into the input columns [hw, hw + E + eiw)
-        int64_t wp_plane = (int64_t)Bc * d.n * d.n * pc * 32, he_plane = (int64_t)Bc * d.n * d.N * ec * 32;
+        int64_t wp_plane = (int64_t)Bc * d.n * d.n * pc * 32;
+        int64_t he_plane = ei_fused ? (int64_t)Bc * d.n * ec * 32 : (int64_t)Bc * d.n * d.N * ec * 32;
         DW_TIMED("conv", launch_conv<Act>(r, p.WP + l * wp_plane, p.HM, p.HE + l * he_plane, p.him + l * d.N * 32, d, l,
-                                          Bc, xin, ldin, s));
+                                          Bc, xin, ldin, s, ei_fused ? 1 : 0));
         // (d) h_el = tanh([h | conv_ee | conv_ei] W_main + per-walker mean term)
         GemmEpi e3; e3.rowbias = p.WB; e3.ldrb = d.D; e3.Tp = d.Tp; e3.rows_per_walker = d.n * d.Tp; e3.act = tang ? 0 : 1;
         WRef wm = wref(pre.main[l], d.D, &pre.main_bf[0][0], l);

@@ -542,8 +542,9 @@ k_pair_mlp_t(const float* __restrict__ r, const float* __restrict__ P, ParamLayo
         __syncthreads();
         mlp_tile_t<CH>(sm, cur, in_w);
         __syncthreads();
+        // consecutive threads take consecutive pairs (row stride CH): conflict-free shared accesses
         for (int it = tid; it < EPB * 32; it += blockDim.x) {
-            const int q = it / 32, f = it % 32;
+            const int q = it % EPB, f = it / EPB;
             float z[CH], y[CH];
             #pragma unroll
             for (int c = 0; c < CH; ++c) z[c] = sm.Zs[f][q * CH + c];
@@ -629,6 +630,98 @@ k_ei_mlp_t(const float* __restrict__ r, const float* __restrict__ Rall, const in
             }
         }
         cur ^= 1;
+    }
+}
+
+// El-ion stream fused with its SchNet reduction (forward passes): the block holds the
+// electron-ion rows of EPB whole electrons (N ions x CH channels each) and, at every stream level
+// l = 0..3, writes conv_ei[l][electron][c][f] = sum_I h_l[electron, I][c][f] * ion_map_l[I][f]
+// (ferminet_embedding.py:171-175) instead of the stream itself, N times fewer values. The
+// stream layers are those of k_ei_mlp (CH = 1) and k_ei_mlp_t (CH = 5); padding ions (Z = 0)
+// have zero rows at every level. Requires N CH <= kRB.
+template <int CH>
+__global__ void __launch_bounds__(128)
+k_ei_conv(const float* __restrict__ r, const float* __restrict__ Rall, const int32_t* __restrict__ Zall,
+          const float* __restrict__ P, ParamLayout L, Dims d, int B, const float* __restrict__ him,
+          float* __restrict__ CEI) {
+    __shared__ __align__(16) MlpSmemT sm;
+    __shared__ unsigned char rok[kRB];     // per entry (electron, ion): 1 real ion, 2 padding ion
+    const int N = d.N, EPB = kRB / (N * CH);
+    const int tid = threadIdx.x;
+    const int64_t ne = (int64_t)B * d.n;
+    const int64_t e0 = (int64_t)blockIdx.x * EPB;
+    for (int e = tid; e < 32 * (kRB + 4); e += blockDim.x) sm.H[0][e / (kRB + 4)][e % (kRB + 4)] = 0.f;
+    __syncthreads();
+    for (int q = tid; q < EPB * N; q += blockDim.x) {
+        const int el = q / N, I = q % N;
+        const int64_t e = e0 + el;
+        unsigned char ok = 0;
+        if (e < ne) {
+            const int b = (int)(e / d.n);
+            const int sg = seg_of(d, b);
+            if (Zall[(size_t)sg * N + I] > 0) {
+                const float* R = Rall + (size_t)sg * N * 3;
+                const float* rr = r + e * 3;
+                const float sx = rr[0] - R[I * 3], sy = rr[1] - R[I * 3 + 1], sz = rr[2] - R[I * 3 + 2];
+                const float dd = sqrtf(sx * sx + sy * sy + sz * sz);
+                const float sv[3] = {sx, sy, sz};
+                const int row = q * CH;
+                // [d, sx, sy, sz] (input_features.py:56-66), with CH = 5 its gradients and Laplacian in r_i
+                sm.H[0][0][row] = dd;
+                #pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    sm.H[0][1 + c][row] = sv[c];
+                    if (CH == 5) {
+                        sm.H[0][0][row + 1 + c] = sv[c] / dd;
+                        sm.H[0][1 + c][row + 1 + c] = 1.f;
+                    }
+                }
+                if (CH == 5) sm.H[0][0][row + 4] = 2.f / dd;
+                ok = 1;
+            } else {
+                ok = 2;
+            }
+        }
+        rok[q] = ok;
+    }
+    __syncthreads();
+    auto write_cei = [&](int level, int buf) {
+        for (int it = tid; it < EPB * CH * 32; it += blockDim.x) {
+            const int el = it / (CH * 32), c = (it / 32) % CH, f = it % 32;
+            const int64_t e = e0 + el;
+            if (e >= ne) continue;
+            const int sg = seg_of(d, (int)(e / d.n));
+            const float* hs = him + ((size_t)sg * 4 + level) * N * 32 + f;
+            float v = 0.f;
+            for (int I = 0; I < N; ++I) v = fmaf(sm.H[buf][f][(el * N + I) * CH + c], __ldg(hs + I * 32), v);
+            CEI[(((int64_t)level * ne + e) * CH + c) * 32 + f] = v;
+        }
+    };
+    write_cei(0, 0);
+    const float rs = 0.70710678118654752f;
+    int cur = 0;
+    for (int l = 0; l < 3; ++l) {
+        const int in_w = d.eiw[l];
+        __syncthreads();
+        mlp_load_wt(sm, P + L.h_ei_w[l], P + L.h_ei_b[l], in_w);
+        __syncthreads();
+        mlp_tile_t<CH>(sm, cur, in_w);
+        __syncthreads();
+        // consecutive threads take consecutive entries (row stride CH): conflict-free shared accesses
+        for (int it = tid; it < EPB * N * 32; it += blockDim.x) {
+            const int q = it % (EPB * N), f = it / (EPB * N);
+            float z[CH], y[CH];
+            #pragma unroll
+            for (int c = 0; c < CH; ++c) z[c] = sm.Zs[f][q * CH + c];
+            tanh_taylor<CH>(z, y);
+            #pragma unroll
+            for (int c = 0; c < CH; ++c)
+                sm.H[cur ^ 1][f][q * CH + c] =
+                    rok[q] == 1 ? (l > 0 ? (sm.H[cur][f][q * CH + c] + y[c]) * rs : y[c]) : 0.f;
+        }
+        cur ^= 1;
+        __syncthreads();
+        write_cei(l + 1, cur);
     }
 }
 
@@ -848,7 +941,7 @@ template <class Act, int TT, int TI>
 __global__ void __launch_bounds__(512)
 k_conv_tile(const float* __restrict__ r, const float* __restrict__ WPl, const float* __restrict__ HM,
             const float* __restrict__ HEl, const float* __restrict__ himl, Dims d, int l, int B, Act* __restrict__ X,
-            int ldx) {
+            int ldx, int ei_fused) {
     extern __shared__ __align__(16) float smc[];
     const int n = d.n, Tp = d.Tp, T = d.T;
     const int NW = Tp / TT;
@@ -915,10 +1008,15 @@ k_conv_tile(const float* __restrict__ r, const float* __restrict__ WPl, const fl
     const float* hs = himl + (size_t)seg_of(d, b) * 4 * d.N * 32 + f;
     for (int it = w; it < ni * 5; it += NW) {
         const int ii = it / 5, ch = it % 5;
-        const float* he = HEl + ((size_t)b * n * d.N + (size_t)(i0 + ii) * d.N) * 5 * 32 + ch * 32 + f;
         float v = 0.f;
-        if (f < eiw)
-            for (int I = 0; I < d.N; ++I) v += __ldg(he + I * 5 * 32) * __ldg(hs + I * 32);
+        if (ei_fused) {
+            // already reduced over the ions by the el-ion stream kernel: CEI[electron][5][32]
+            v = __ldg(HEl + (((size_t)b * n + i0 + ii) * 5 + ch) * 32 + f);
+        } else {
+            const float* he = HEl + ((size_t)b * n * d.N + (size_t)(i0 + ii) * d.N) * 5 * 32 + ch * 32 + f;
+            if (f < eiw)
+                for (int I = 0; I < d.N; ++I) v += __ldg(he + I * 5 * 32) * __ldg(hs + I * 32);
+        }
         eiv[(ii * 5 + ch) * 32 + f] = v;
     }
     __syncthreads();
@@ -1210,9 +1308,18 @@ void launch_features(const float* r, const float* R, const int32_t* Z, const Dim
     const int fthreads = std::min(256, 32 * d.Tp);        // one warp per channel row, up to 8 warps
     k_features<Act><<<B * d.n, fthreads, 0, s>>>(r, R, Z, d, B, X0); count_launch();
 }
+// The fused el-ion reduction needs whole electrons in one block and a convolution kernel that
+// reads it (k_conv_tile, 8 <= Tp <= 128). It is used in tangent passes only: for value rows the
+// separate k_ei_mlp + k_conv_value pair measured faster (the fused kernel's extra shared-memory
+// pass costs more than the stream traffic it saves).
+bool ei_fusable(const Dims& d) {
+    return d.E == 32 && d.EI == 32 && d.Tp >= 8 && d.Tp <= 128 && d.N * 5 <= kRB;
+}
+
 void launch_streams(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,
-                    const Dims& d, int B, float* WP, float* HE, cudaStream_t s, float* HP) {
+                    const Dims& d, int B, float* WP, float* HE, cudaStream_t s, float* HP, const float* him) {
     const bool tang = d.Tp > 1;
+    if (him && !ei_fusable(d)) him = nullptr;
     const int64_t npair = (int64_t)B * d.n * (d.n + 1) / 2, nei = (int64_t)B * d.n * d.N;
     auto blocks = [](int64_t n) { return (unsigned)((n + 127) / 128); };
     if (tang) {
@@ -1225,7 +1332,12 @@ void launch_streams(const float* r, const float* R, const int32_t* Z, const floa
             const int64_t diff_rows = (int64_t)B * d.nu * d.nd;
             const int bs = (int)((same_rows + EP - 1) / EP), bd = (int)((diff_rows + EP - 1) / EP);
             k_pair_mlp_t<<<bs + bd, 128, 0, s>>>(r, P, L, d, B, bs, WP);
-            k_ei_mlp_t<<<(unsigned)((nei + EE - 1) / EE), 128, 0, s>>>(r, R, Z, P, L, d, B, HE);
+            if (him) {
+                const int epb = kRB / (d.N * 5);
+                k_ei_conv<5><<<(unsigned)(((int64_t)B * d.n + epb - 1) / epb), 128, 0, s>>>(r, R, Z, P, L, d, B, him, HE);
+            } else {
+                k_ei_mlp_t<<<(unsigned)((nei + EE - 1) / EE), 128, 0, s>>>(r, R, Z, P, L, d, B, HE);
+            }
         } else {
             k_pair_streams<3><<<blocks(npair), 128, sm3, s>>>(r, P, L, d, B, WP, nullptr);
             k_ei_streams<5><<<blocks(nei), 128, sm5, s>>>(r, R, Z, P, L, d, B, HE);
@@ -1235,7 +1347,12 @@ void launch_streams(const float* r, const float* R, const int32_t* Z, const floa
         const int64_t diff_rows = (int64_t)B * d.nu * d.nd;
         const int bs = (int)((same_rows + kRB - 1) / kRB), bd = (int)((diff_rows + kRB - 1) / kRB);
         k_pair_mlp<<<bs + bd, 128, 0, s>>>(r, P, L, d, B, bs, WP, HP);
-        k_ei_mlp<<<(unsigned)((nei + kRB - 1) / kRB), 128, 0, s>>>(r, R, Z, P, L, d, B, HE);
+        if (him) {
+            const int epb = kRB / d.N;
+            k_ei_conv<1><<<(unsigned)(((int64_t)B * d.n + epb - 1) / epb), 128, 0, s>>>(r, R, Z, P, L, d, B, him, HE);
+        } else {
+            k_ei_mlp<<<(unsigned)((nei + kRB - 1) / kRB), 128, 0, s>>>(r, R, Z, P, L, d, B, HE);
+        }
     }
     count_launch(2);
 }
@@ -1253,7 +1370,7 @@ void launch_tanh_fl(const float* Zb, int ldz, int ncols, int groups, const Dims&
 }
 template <class Act>
 void launch_conv(const float* r, const float* WPl, const float* HM, const float* HEl, const float* himl, const Dims& d,
-                 int l, int B, Act* X, int ldx, cudaStream_t s) {
+                 int l, int B, Act* X, int ldx, cudaStream_t s, int ei_fused) {
     if (d.Tp >= 8 && d.Tp <= 128 && d.E == 32) {
         // 4 electrons per block (8 or 5 per block measured slower: larger shared-memory tiles and
         // product-rule loops outweigh the extra reuse of each h_map load)
@@ -1264,7 +1381,7 @@ void launch_conv(const float* r, const float* WPl, const float* HM, const float*
         const size_t smem = ((size_t)TI * d.Tp * 32 + (size_t)NW * TI * 4 * 32 + (size_t)TI * 5 * 32) * sizeof(float);
         auto go = [&](auto kern) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            kern<<<grid, NW * 32, smem, s>>>(r, WPl, HM, HEl, himl, d, l, B, X, ldx);
+            kern<<<grid, NW * 32, smem, s>>>(r, WPl, HM, HEl, himl, d, l, B, X, ldx, ei_fused);
         };
         auto pick = [&](auto ti) {
             constexpr int T_I = decltype(ti)::value;
@@ -1279,7 +1396,7 @@ void launch_conv(const float* r, const float* WPl, const float* HM, const float*
         count_launch();
         return;
     }
-    if (d.Tp == 1 && d.E % 8 == 0) {
+    if (d.Tp == 1 && d.E % 8 == 0 && !ei_fused) {
         const int octs = d.E / 8 + (d.eiw[l] + 7) / 8;
         const int64_t threads = (int64_t)B * d.n * octs;
         k_conv_value<Act><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(WPl, HM, HEl, himl, d, l, B, X, ldx);
@@ -1439,7 +1556,7 @@ void launch_jastrow_out(const Act* J2, int ldj, const float* w2, const Dims& d, 
     template void launch_spin_means<Act>(const Act*, int, int, const Dims&, int, Act*, int, cudaStream_t);    \
     template void launch_tanh_fl<Act>(const float*, int, int, int, const Dims&, Act*, int, cudaStream_t);     \
     template void launch_conv<Act>(const float*, const float*, const float*, const float*, const float*,      \
-                                   const Dims&, int, int, Act*, int, cudaStream_t);                           \
+                                   const Dims&, int, int, Act*, int, cudaStream_t, int);                      \
     template void launch_jastrow_out<Act>(const Act*, int, const float*, const Dims&, int, double*, cudaStream_t);
 DW_INST(float)
 DW_INST(__nv_bfloat16)

@@ -71,12 +71,17 @@ template <> struct ActIO<Split> {
 void launch_ion_maps(const float* P, const ParamLayout& L, const Dims& d, const int32_t* Z, float* him, cudaStream_t s);
 template <class Act> void launch_features(const float* r, const float* R, const int32_t* Z, const Dims& d, int B, Act* X0,
                                           cudaStream_t s);
+// him != nullptr (forward passes, when ei_fusable(d)): HE receives the el-ion convolution already
+// reduced over the ions, conv_ei[level][walker * n + electron][channels][32], not the stream.
+bool ei_fusable(const Dims& d);
 void launch_streams(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,
-                    const Dims& d, int B, float* WP, float* HE, cudaStream_t s, float* HP = nullptr);
+                    const Dims& d, int B, float* WP, float* HE, cudaStream_t s, float* HP = nullptr,
+                    const float* him = nullptr);
 template <class Act> void launch_spin_means(const Act* X, int ldx, int hw, const Dims& d, int B, Act* M, int mw, cudaStream_t s);
 template <class Act> void launch_tanh_fl(const float* Zb, int ldz, int ncols, int groups, const Dims& d, Act* Y, int ldy, cudaStream_t s);
+// ei_fused = 1: HEl is conv_ei of this level (launch_streams with him), not the el-ion stream.
 template <class Act> void launch_conv(const float* r, const float* WPl, const float* HM, const float* HEl, const float* himl,
-                                      const Dims& d, int l, int B, Act* X, int ldx, cudaStream_t s);
+                                      const Dims& d, int l, int B, Act* X, int ldx, cudaStream_t s, int ei_fused = 0);
 // BF rows hold the backflow of each electron; the down-spin electrons' columns start at column
 // spin_cols (KN when both spin blocks are stored side by side, 0 when each row holds its own spin's).
 void launch_envelope(const float* r, const float* R, const int32_t* Z, const float* P, const ParamLayout& L,

@@ -525,15 +525,12 @@ static int backward_chunk(const Bwd& w, int Bc, const float* P, const ParamLayou
     for (int l = 0; l < 4; ++l) {
         const float* A = l == 0 ? w.HP0 : w.HP + (int64_t)(l - 1) * npair * 32;
         const int lda = l == 0 ? 1 : 32, in_w = d.eew[l];
-        for (int same = 0; same < 2; ++same) {
-            wgrad_f32(A, lda, w.dZp + (int64_t)l * npair * 32, 32, (int)npair, in_w, 32,
-                      grad + (same ? L.w_same_w[l] : L.w_diff_w[l]), 32, grad + (same ? L.w_same_b[l] : L.w_diff_b[l]),
-                      w.sel, same, s);
-            if (l < 3)
-                wgrad_f32(A, lda, w.dZp + (int64_t)(4 + l) * npair * 32, 32, (int)npair, in_w, 32,
-                          grad + (same ? L.h_same_w[l] : L.h_diff_w[l]), 32,
-                          grad + (same ? L.h_same_b[l] : L.h_diff_b[l]), w.sel, same, s);
-        }
+        // one pass over the pairs per weight: same-spin pairs (sel 1) and opposite-spin pairs (sel 0)
+        wgrad32_sel2(A, lda, w.dZp + (int64_t)l * npair * 32, 32, (int)npair, in_w, 32, w.sel,
+                     grad + L.w_diff_w[l], grad + L.w_diff_b[l], grad + L.w_same_w[l], grad + L.w_same_b[l], 32, s);
+        if (l < 3)
+            wgrad32_sel2(A, lda, w.dZp + (int64_t)(4 + l) * npair * 32, 32, (int)npair, in_w, 32, w.sel,
+                         grad + L.h_diff_w[l], grad + L.h_diff_b[l], grad + L.h_same_w[l], grad + L.h_same_b[l], 32, s);
     }
     // el-ion stream
     k_ei_bwd<<<nblk(nei, 128), 128, 0, s>>>(P, L, d, Bc, w.HE, w.dHE, w.dZe);

@@ -349,9 +349,112 @@ k_wgrad_f32(const float* __restrict__ A, int lda, const float* __restrict__ G, i
     }
 }
 
+// Narrow weight gradients (K, N <= 32), one pass over the rows for up to two outputs: rows with
+// sel[r] == 1 go to (dW1, dB1), the others to (dW0, dB0) (sel == NULL: all rows to output 0).
+// 256 threads = 4 row groups x 64 threads; a thread keeps a 4 x 4 patch of each 32 x 32 output
+// (two float4 shared loads feed 16 FMAs per row), the row groups are added in shared memory and
+// each block adds its segment with one atomic per output element.
+__global__ void __launch_bounds__(256)
+k_wgrad32(const float* __restrict__ A, int lda, const float* __restrict__ G, int ldg, int rows, int K, int N,
+          const int8_t* __restrict__ sel, float* __restrict__ dW0, float* __restrict__ dB0, float* __restrict__ dW1,
+          float* __restrict__ dB1, int lddw, int rows_per_seg) {
+    constexpr int RS = 32;                               // rows per shared-memory slab
+    __shared__ __align__(16) float As[RS][36];
+    __shared__ __align__(16) float Gs[RS][36];
+    __shared__ int8_t ss[RS];
+    __shared__ __align__(16) float red[4][2][32][33];
+    const int tid = threadIdx.x, grp = tid >> 6, t64 = tid & 63, kb = t64 >> 3, nb = t64 & 7;
+    const int r_begin = blockIdx.x * rows_per_seg, r_end = min(rows, r_begin + rows_per_seg);
+    float acc[2][4][4], bacc[2][4];
+    #pragma unroll
+    for (int o = 0; o < 2; ++o) {
+        #pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            bacc[o][u] = 0.f;
+            #pragma unroll
+            for (int v = 0; v < 4; ++v) acc[o][u][v] = 0.f;
+        }
+    }
+    for (int r0 = r_begin; r0 < r_end; r0 += RS) {
+        for (int e = tid; e < RS * 32; e += 256) {
+            const int rr = e >> 5, cc = e & 31, r = r0 + rr;
+            const bool ok = r < r_end;
+            As[rr][cc] = (ok && cc < K) ? __ldg(A + (int64_t)r * lda + cc) : 0.f;
+            Gs[rr][cc] = (ok && cc < N) ? __ldg(G + (int64_t)r * ldg + cc) : 0.f;
+        }
+        if (tid < RS) ss[tid] = (sel && r0 + tid < r_end) ? (sel[r0 + tid] == 1 ? 1 : 0) : 0;
+        __syncthreads();
+        #pragma unroll 2
+        for (int rr = grp; rr < RS; rr += 4) {
+            const float4 a4 = *reinterpret_cast<const float4*>(&As[rr][4 * kb]);
+            const float4 g4 = *reinterpret_cast<const float4*>(&Gs[rr][4 * nb]);
+            const float a[4] = {a4.x, a4.y, a4.z, a4.w}, g[4] = {g4.x, g4.y, g4.z, g4.w};
+            if (ss[rr]) {
+                #pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    #pragma unroll
+                    for (int v = 0; v < 4; ++v) acc[1][u][v] = fmaf(a[u], g[v], acc[1][u][v]);
+                #pragma unroll
+                for (int v = 0; v < 4; ++v) bacc[1][v] += g[v];
+            } else {
+                #pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    #pragma unroll
+                    for (int v = 0; v < 4; ++v) acc[0][u][v] = fmaf(a[u], g[v], acc[0][u][v]);
+                #pragma unroll
+                for (int v = 0; v < 4; ++v) bacc[0][v] += g[v];
+            }
+        }
+        __syncthreads();
+    }
+    const int nout = sel ? 2 : 1;
+    for (int o = 0; o < nout; ++o) {
+        #pragma unroll
+        for (int u = 0; u < 4; ++u)
+            #pragma unroll
+            for (int v = 0; v < 4; ++v) red[grp][o][4 * kb + u][4 * nb + v] = acc[o][u][v];
+    }
+    __syncthreads();
+    for (int e = tid; e < nout * 1024; e += 256) {
+        const int o = e >> 10, k = (e >> 5) & 31, n = e & 31;
+        if (k >= K || n >= N) continue;
+        const float v = red[0][o][k][n] + red[1][o][k][n] + red[2][o][k][n] + red[3][o][k][n];
+        atomicAdd((o ? dW1 : dW0) + (int64_t)k * lddw + n, v);
+    }
+    // bias: the kb == 0 threads of each row group hold the column sums of G
+    __syncthreads();
+    if (kb == 0) {
+        for (int o = 0; o < nout; ++o)
+            #pragma unroll
+            for (int v = 0; v < 4; ++v) red[grp][o][0][4 * nb + v] = bacc[o][v];
+    }
+    __syncthreads();
+    for (int e = tid; e < nout * 32; e += 256) {
+        const int o = e >> 5, n = e & 31;
+        float* dB = o ? dB1 : dB0;
+        if (!dB || n >= N) continue;
+        atomicAdd(dB + n, red[0][o][0][n] + red[1][o][0][n] + red[2][o][0][n] + red[3][o][0][n]);
+    }
+}
+
+void wgrad32_sel2(const float* A, int lda, const float* G, int ldg, int rows, int K, int N, const int8_t* sel,
+                  float* dW0, float* dB0, float* dW1, float* dB1, int lddw, cudaStream_t s) {
+    if (rows <= 0 || K <= 0 || N <= 0) return;
+    int segs = std::max(1, std::min((rows + 127) / 128, 2 * num_sms_simt()));
+    int rps = (rows + segs - 1) / segs;
+    rps = (rps + 31) / 32 * 32;
+    segs = (rows + rps - 1) / rps;
+    k_wgrad32<<<segs, 256, 0, s>>>(A, lda, G, ldg, rows, K, N, sel, dW0, dB0, dW1, dB1, lddw, rps);
+    count_launch();
+}
+
 void wgrad_f32(const float* A, int lda, const float* G, int ldg, int rows, int K, int N, float* dW, int lddw,
                float* dB, const int8_t* sel, int want, cudaStream_t s) {
     if (rows <= 0 || K <= 0 || N <= 0) return;
+    if (K <= 32 && N <= 32 && !sel) {
+        wgrad32_sel2(A, lda, G, ldg, rows, K, N, nullptr, dW, dB, nullptr, nullptr, lddw, s);
+        return;
+    }
     if (K < 128 || N < 128) {
         // narrow shapes: 64 x 64 tiles waste less of each thread's patch
         const int tiles = ((K + 63) / 64) * ((N + 63) / 64);

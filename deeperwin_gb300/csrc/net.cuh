@@ -107,6 +107,10 @@ void gemm_f32_nt(const float* A, int lda, const float* W, int ldw, float* C, int
 // dB[N] += sum_r G[r, n] when dB != NULL. Split over rows, atomically accumulated.
 void wgrad_f32(const float* A, int lda, const float* G, int ldg, int rows, int K, int N, float* dW, int lddw,
                float* dB, const int8_t* sel, int want, cudaStream_t s);
+// K, N <= 32: rows with sel[r] == 1 accumulate into (dW1, dB1), the others into (dW0, dB0), in one
+// pass (sel == NULL: every row into output 0).
+void wgrad32_sel2(const float* A, int lda, const float* G, int ldg, int rows, int K, int N, const int8_t* sel,
+                  float* dW0, float* dB0, float* dW1, float* dB1, int lddw, cudaStream_t s);
 
 // det.cu
 template <class S>

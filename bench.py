@@ -233,10 +233,13 @@ def run_ours(args, rank, world, dev):
         E_m = api.local_energy(params, spin, state.r, state.R, state.Z).double()
         E_p = api.local_energy(pparams, spin, state.r, state.R, state.Z).double()
         d = (E_m - E_p)
+        ad = d.abs().cpu().numpy() * 1e3
         plain = {"value": world * B / (ms_p / 1e3), "ms_per_step": ms_p,
                  "mixed_over_plain": ms_p / ms,
                  "mixed_minus_plain_mean_E_mHa": float(d.mean().item() * 1e3),
-                 "mixed_minus_plain_max_abs_mHa": float(d.abs().max().item() * 1e3)}
+                 "mixed_minus_plain_max_abs_mHa": float(ad.max()),
+                 "abs_mixed_minus_plain_quantiles_mHa": {q: float(np.quantile(ad, float(q) / 100))
+                                                         for q in ("50", "99", "99.9")}}
 
     out = None
     if rank == 0:
@@ -318,6 +321,25 @@ def cpu_baseline(args, a, mol, r_sample, gpu_E=None):
     return out, acc
 
 
+def worst_walkers(a, mol, state, params, k=4):
+    """The k walkers of the full batch where the mixed and plain forms differ most, each checked
+    against the FP64 oracle: the tail of the per-walker error (ill-conditioned Slater matrices)."""
+    import torch
+    from deeperwin_gb300 import api
+    from oracle import dpe4 as O
+    from deeperwin_gb300 import params as P
+    spin = (a.n_up, a.n_dn)
+    E_m = api.local_energy(params, spin, state.r, state.R, state.Z).double()
+    E_p = api.local_energy(params.with_precision("fp32"), spin, state.r, state.R, state.Z).double()
+    idx = torch.argsort((E_m - E_p).abs(), descending=True)[:k]
+    r = state.r[idx].double().cpu().numpy()
+    E_o = O.local_energy(O.tparams(P.init_params(a, seed=0)), a, r, mol.R, mol.Z)[0].numpy()
+    return {"selection": f"the {k} walkers of the full batch with the largest |E_mixed - E_plain|",
+            "E_oracle_Ha": [round(float(x), 6) for x in E_o],
+            "mixed_abs_err_mHa": [round(float(x), 3) for x in np.abs(E_m[idx].cpu().numpy() - E_o) * 1e3],
+            "fp32_abs_err_mHa": [round(float(x), 3) for x in np.abs(E_p[idx].cpu().numpy() - E_o) * 1e3]}
+
+
 def run_reference(args):
     """Reference arm: the reference's JAX code cannot run on this machine (no jax/haiku/folx),
     so the CPU restatement of its algorithm (the oracle port) is timed on the host cores."""
@@ -381,6 +403,8 @@ def main():
             cb, acc = cpu_baseline(args, a, mol, r_sample, gpu_E)
             out["cpu_baseline"] = cb
             out["accuracy_vs_fp64_oracle"] = acc
+            if w.precision != "fp32" and not args.no_plain:
+                out["accuracy_worst_walkers_vs_fp64_oracle"] = worst_walkers(a, mol, state, params)
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.barrier()

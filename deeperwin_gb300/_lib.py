@@ -71,6 +71,8 @@ _SIGS = {
     "dw_debug_gemm_bf16": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_int, _P]),
     "dw_debug_tc_error_flag": (ctypes.c_int, []),
+    "dw_debug_slogdet_small": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                              _P, _P, _P, _P]),
     "dw_timer_enable": (ctypes.c_int, [ctypes.c_int]),
     "dw_timer_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
                                      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),

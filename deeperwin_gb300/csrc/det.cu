@@ -1,6 +1,7 @@
 // Determinants, their forward-mode derivatives, the multi-determinant combine, the
 // Jastrow add, the kinetic energy and the Coulomb potential.
 #include "net.cuh"
+#include "ff.cuh"
 #include <type_traits>
 
 namespace dw {
@@ -39,6 +40,38 @@ __device__ __forceinline__ double mant_mul_norm(double mant, double a, int& expo
     expo += eb - 1022;
     return __hiloint2double((hi & 0x800fffff) | 0x3fe00000, lo);
 }
+
+// Scalar operations of the elimination kernels, for S = double (FP64) and S = FF (float-float).
+// Pivot keys: non-negative floating-point magnitudes order as their bit patterns.
+__device__ __forceinline__ long long lu_key(double v) { return __double_as_longlong(v) & 0x7fffffffffffffffll; }
+__device__ __forceinline__ int lu_key(FF v) { return __float_as_int(v.hi) & 0x7fffffff; }
+template <class S> __device__ __forceinline__ S lu_from(float x);
+template <> __device__ __forceinline__ double lu_from<double>(float x) { return (double)x; }
+template <> __device__ __forceinline__ FF lu_from<FF>(float x) { return ff_make(x); }
+__device__ __forceinline__ bool lu_neg(double v) { return v < 0.0; }
+__device__ __forceinline__ bool lu_neg(FF v) { return v.hi < 0.f; }
+__device__ __forceinline__ double lu_negate(double v) { return -v; }
+__device__ __forceinline__ FF lu_negate(FF v) { return ff_neg(v); }
+__device__ __forceinline__ double lu_fnma(double l, double u, double a) { return fma(-l, u, a); }   // a - l u
+__device__ __forceinline__ FF lu_fnma(FF l, FF u, FF a) { return ff_fnma(l, u, a); }
+__device__ __forceinline__ float lu_to_float(double v) { return (float)v; }
+__device__ __forceinline__ float lu_to_float(FF v) { return __fadd_rn(v.hi, v.lo); }
+// A pivot p with its reciprocal; lu_quot(a, q) = a / p. The float-float form divides instead of
+// multiplying when 1 / p.hi leaves the normal FP32 range (|p| < 2^-125 or > 2^125).
+struct PivD { double p, rp; };
+struct PivF { FF p, rp; bool ok; };
+__device__ __forceinline__ PivD lu_pivot(double p) { return PivD{p, recip_nr(p)}; }
+__device__ __forceinline__ PivF lu_pivot(FF p) {
+    const bool ok = ff_recip_ok(p);
+    return PivF{p, ok ? ff_recip(p) : FF{0.f, 0.f}, ok};
+}
+__device__ __forceinline__ double lu_quot(double a, const PivD& q) { return a * q.rp; }
+__device__ __forceinline__ FF lu_quot(FF a, const PivF& q) { return q.ok ? ff_mul(a, q.rp) : ff_div(a, q.p); }
+// Pivot-magnitude product as mantissa [0.5, 1) and binary exponent; one log per matrix.
+__device__ __forceinline__ void lu_mant_mul(double& m, double p, int& e) { m = mant_mul_norm(m, fabs(p), e); }
+__device__ __forceinline__ void lu_mant_mul(FF& m, FF p, int& e) { ff_mant_mul(m, p, e); }
+__device__ __forceinline__ double lu_log(double m, int e) { return log(m) + (double)e * 0.69314718055994530942; }
+__device__ __forceinline__ double lu_log(FF m, int e) { return ff_log_mant(m, e); }
 
 // One warp per (walker, determinant). Gauss-Jordan elimination with partial pivoting
 // (first maximal |pivot| wins, as LAPACK getrf) on [A | I] in scalar type S; in value-only
@@ -290,27 +323,32 @@ k_slogdet_rows(const float* __restrict__ MO, int n, int T, int nmat, double* __r
     }
 }
 
-// Value-only FP64 log|det| with one matrix per thread. On this part FP64 arithmetic issues at
-// a small fraction of the FP32 rate, so the LU is bound by the number of FP64 instructions;
-// giving each thread a whole matrix issues exactly the (n-k-1)^2 trailing-update FMAs and
-// (n-k-1) multiplier products of pivot k, plus one reciprocal and one mantissa product per
-// pivot -- with no lanes idling above the pivot and no per-lane copies of the per-pivot
-// work (about a quarter of the FP64 instructions of the rows-in-lanes form).
+// log|det| with one matrix per thread, in FP64 (S = double) or float-float (S = FF). On this
+// part FP64 arithmetic issues at about 1/100 of the FP32 rate, so the FP64 form is bound by the
+// number of FP64 instructions. The production forms use FP64: the LU is one of the steps kept in
+// FP64 for stability near nodal surfaces. The float-float instances (about 15 FP32 instructions
+// per elimination step, ~48-bit significands; measured 1.3-2.5x faster for n = 10..16, with
+// log|det| within ~1e-9 of FP64 on random matrices) are an evaluated alternative, reachable
+// through dw_debug_slogdet_small and tested there. Giving each thread a whole matrix issues
+// exactly the (n-k-1)^2 trailing-update steps and (n-k-1) multipliers of pivot k, plus one
+// reciprocal and one mantissa product per pivot, with no lanes idling above the pivot.
 // The matrices live in shared memory, element (i, j) of thread t at
-// sm[(i * NMAX + j) * LD + t] with LD = TPB + 1: accesses of one element by all threads are
-// consecutive words, and the odd stride keeps the cooperative staging of the row-major input
-// free of bank conflicts. Partial pivoting takes the first row of maximal |a_ik| at or below
-// the diagonal (as LAPACK getrf), comparing the full 64-bit magnitude patterns; rows are
-// exchanged physically, so ties are resolved in the current row order exactly as getrf does.
-// The pivot product is kept as a mantissa in [0.5, 1) and a binary exponent, normalised with
-// integer operations, and one log is taken per matrix.
-template <int NMAX, int TPB>
+// sm[(i * NMAX + j) * LD + t] with LD = TPB + 1 (8-byte elements): accesses of one element by
+// all threads are consecutive, and the odd stride keeps the cooperative staging of the
+// row-major input free of bank conflicts. Partial pivoting takes the first row of maximal
+// |a_ik| at or below the diagonal (as LAPACK getrf), comparing magnitude bit patterns (the
+// leading FP32 word in the float-float form); rows are exchanged physically, so ties are
+// resolved in the current row order exactly as getrf does. The pivot product is kept as a
+// mantissa in [0.5, 1) and a binary exponent, normalised with integer operations, and one log
+// is taken per matrix.
+template <class S, int NMAX, int TPB>
 __global__ void __launch_bounds__(TPB)
 k_slogdet_thread(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
                  double* __restrict__ sign) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int LD = TPB + 1;
-    double* sm = reinterpret_cast<double*>(smem_raw);
+    static_assert(sizeof(S) == 8, "8-byte elements");
+    S* sm = reinterpret_cast<S*>(smem_raw);
     const int tid = threadIdx.x;
     const int mat0 = blockIdx.x * TPB;
     const int nm = min(TPB, nmat - mat0);
@@ -319,37 +357,37 @@ k_slogdet_thread(const float* __restrict__ MO, int n, int T, int nmat, double* _
     for (int q = tid; q < nm * nn; q += TPB) {
         const int m = q / nn, e = q - m * nn;
         const int i = e / n, j = e - i * n;
-        sm[(i * NMAX + j) * LD + m] = (double)__ldg(MO + (int64_t)(mat0 + m) * T * nn + e);
+        sm[(i * NMAX + j) * LD + m] = lu_from<S>(__ldg(MO + (int64_t)(mat0 + m) * T * nn + e));
     }
     __syncthreads();
     if (tid >= nm) return;
-    double* a = sm + tid;
-    auto at = [&](int i, int j) -> double& { return a[(i * NMAX + j) * LD]; };
-    double mant = 1.0, sg = 1.0;
+    S* a = sm + tid;
+    auto at = [&](int i, int j) -> S& { return a[(i * NMAX + j) * LD]; };
+    S mant = lu_from<S>(1.f);
+    double sg = 1.0;
     int expo = 0;
     bool singular = false;
     #pragma unroll 1
     for (int k = 0; k < n; ++k) {
-        // pivot search on 64-bit magnitude patterns (non-negative doubles order as integers)
-        long long best = __double_as_longlong(at(k, k)) & 0x7fffffffffffffffll;
+        auto best = lu_key(at(k, k));
         int p = k;
         #pragma unroll 1
         for (int i = k + 1; i < n; ++i) {
-            const long long v = __double_as_longlong(at(i, k)) & 0x7fffffffffffffffll;
+            const auto v = lu_key(at(i, k));
             if (v > best) { best = v; p = i; }
         }
         if (best == 0) { singular = true; break; }
         if (p != k) {
             #pragma unroll 1
-            for (int j = k; j < n; ++j) { const double t = at(k, j); at(k, j) = at(p, j); at(p, j) = t; }
+            for (int j = k; j < n; ++j) { const S t = at(k, j); at(k, j) = at(p, j); at(p, j) = t; }
             sg = -sg;
         }
-        const double pk = at(k, k);
-        if (pk < 0.0) sg = -sg;
-        mant = mant_mul_norm(mant, fabs(pk), expo);
-        const double rp = recip_nr(pk);
+        const S pk = at(k, k);
+        if (lu_neg(pk)) sg = -sg;
+        lu_mant_mul(mant, pk, expo);
+        const auto piv = lu_pivot(pk);
         const int rem = n - k - 1;                       // trailing columns k+1 .. n-1
-        double u[NMAX - 1];
+        S u[NMAX - 1];
         #pragma unroll
         for (int c = 0; c < NMAX - 1; ++c) {
             if (c >= rem) break;
@@ -357,34 +395,36 @@ k_slogdet_thread(const float* __restrict__ MO, int n, int T, int nmat, double* _
         }
         #pragma unroll 1
         for (int i = k + 1; i < n; ++i) {
-            double* row = &at(i, k);
-            const double l = row[0] * rp;
+            S* row = &at(i, k);
+            const S l = lu_quot(row[0], piv);
             #pragma unroll
             for (int c = 0; c < NMAX - 1; ++c) {
                 if (c >= rem) break;
-                row[(c + 1) * LD] = fma(-l, u[c], row[(c + 1) * LD]);
+                row[(c + 1) * LD] = lu_fnma(l, u[c], row[(c + 1) * LD]);
             }
         }
     }
-    logdet[mat0 + tid] = singular ? -INFINITY : log(mant) + (double)expo * 0.69314718055994530942;
+    logdet[mat0 + tid] = singular ? -INFINITY : lu_log(mant, expo);
     sign[mat0 + tid] = singular ? 0.0 : sg;
 }
 
-// FP64 log|det| and inverse with one matrix per thread: in-place Gauss-Jordan elimination with
-// partial pivoting (first row of maximal |a_ik| at or below the diagonal, rows exchanged
-// physically as getrf does), n^3 FMAs per matrix. Pivot k: row k is scaled by 1/a_kk, every
-// other row i loses a_ik times it, and column k becomes the inverse's column (1/a_kk on the
-// diagonal, -a_ik/a_kk elsewhere). The result is (PA)^-1 = A^-1 P^T, so the recorded row
-// exchanges are undone on the columns in reverse order. Shared-memory layout and log-det
-// bookkeeping as in k_slogdet_thread; the inverse is written in FP32 (zeros when singular).
-template <int NMAX, int TPB>
+// log|det| and inverse with one matrix per thread (S = double or FF, as k_slogdet_thread):
+// in-place Gauss-Jordan elimination with partial pivoting (first row of maximal |a_ik| at or
+// below the diagonal, rows exchanged physically as getrf does), n^3 update steps per matrix.
+// Pivot k: row k is scaled by 1/a_kk, every other row i loses a_ik times it, and column k
+// becomes the inverse's column (1/a_kk on the diagonal, -a_ik/a_kk elsewhere). The result is
+// (PA)^-1 = A^-1 P^T, so the recorded row exchanges are undone on the columns in reverse order.
+// Shared-memory layout and log-det bookkeeping as in k_slogdet_thread; the inverse is written
+// in FP32 (zeros when singular).
+template <class S, int NMAX, int TPB>
 __global__ void __launch_bounds__(TPB)
 k_slogdet_inv_thread(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
                      double* __restrict__ sign, float* __restrict__ Ainv) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int LD = TPB + 1;
-    double* sm = reinterpret_cast<double*>(smem_raw);
-    unsigned char* pivs = smem_raw + (size_t)NMAX * NMAX * LD * sizeof(double);   // [k][thread]
+    static_assert(sizeof(S) == 8, "8-byte elements");
+    S* sm = reinterpret_cast<S*>(smem_raw);
+    unsigned char* pivs = smem_raw + (size_t)NMAX * NMAX * LD * sizeof(S);   // [k][thread]
     const int tid = threadIdx.x;
     const int mat0 = blockIdx.x * TPB;
     const int nm = min(TPB, nmat - mat0);
@@ -392,60 +432,61 @@ k_slogdet_inv_thread(const float* __restrict__ MO, int n, int T, int nmat, doubl
     for (int q = tid; q < nm * nn; q += TPB) {
         const int m = q / nn, e = q - m * nn;
         const int i = e / n, j = e - i * n;
-        sm[(i * NMAX + j) * LD + m] = (double)__ldg(MO + (int64_t)(mat0 + m) * T * nn + e);
+        sm[(i * NMAX + j) * LD + m] = lu_from<S>(__ldg(MO + (int64_t)(mat0 + m) * T * nn + e));
     }
     __syncthreads();
     if (tid >= nm) return;
-    double* a = sm + tid;
-    auto at = [&](int i, int j) -> double& { return a[(i * NMAX + j) * LD]; };
-    double mant = 1.0, sg = 1.0;
+    S* a = sm + tid;
+    auto at = [&](int i, int j) -> S& { return a[(i * NMAX + j) * LD]; };
+    const S one = lu_from<S>(1.f);
+    S mant = one;
+    double sg = 1.0;
     int expo = 0;
     bool singular = false;
     #pragma unroll 1
     for (int k = 0; k < n; ++k) {
-        long long best = __double_as_longlong(at(k, k)) & 0x7fffffffffffffffll;
+        auto best = lu_key(at(k, k));
         int p = k;
         #pragma unroll 1
         for (int i = k + 1; i < n; ++i) {
-            const long long v = __double_as_longlong(at(i, k)) & 0x7fffffffffffffffll;
+            const auto v = lu_key(at(i, k));
             if (v > best) { best = v; p = i; }
         }
         if (best == 0) { singular = true; break; }
         pivs[k * TPB + tid] = (unsigned char)p;
         if (p != k) {
             #pragma unroll 1
-            for (int j = 0; j < n; ++j) { const double t = at(k, j); at(k, j) = at(p, j); at(p, j) = t; }
+            for (int j = 0; j < n; ++j) { const S t = at(k, j); at(k, j) = at(p, j); at(p, j) = t; }
             sg = -sg;
         }
-        const double pk = at(k, k);
-        if (pk < 0.0) sg = -sg;
-        mant = mant_mul_norm(mant, fabs(pk), expo);
-        const double rp = recip_nr(pk);
+        const S pk = at(k, k);
+        if (lu_neg(pk)) sg = -sg;
+        lu_mant_mul(mant, pk, expo);
+        const auto piv = lu_pivot(pk);
         // scaled pivot row in registers (column k itself becomes 1 / a_kk)
-        double u[NMAX];
+        S u[NMAX];
         #pragma unroll
         for (int j = 0; j < NMAX; ++j) {
             if (j >= n) break;
-            const double x = (j == k) ? 1.0 : at(k, j);
-            u[j] = x * rp;
+            u[j] = lu_quot(j == k ? one : at(k, j), piv);
             at(k, j) = u[j];
         }
         #pragma unroll 1
         for (int i = 0; i < n; ++i) {
             if (i == k) continue;
-            double* row = &at(i, 0);
-            const double f = row[k * LD];
+            S* row = &at(i, 0);
+            const S f = row[k * LD];
             #pragma unroll
             for (int j = 0; j < NMAX; ++j) {
                 if (j >= n) break;
                 if (j == k) continue;
-                row[j * LD] = fma(-f, u[j], row[j * LD]);
+                row[j * LD] = lu_fnma(f, u[j], row[j * LD]);
             }
-            row[k * LD] = -f * rp;
+            row[k * LD] = lu_negate(lu_quot(f, piv));
         }
     }
     const int mat = mat0 + tid;
-    logdet[mat] = singular ? -INFINITY : log(mant) + (double)expo * 0.69314718055994530942;
+    logdet[mat] = singular ? -INFINITY : lu_log(mant, expo);
     sign[mat] = singular ? 0.0 : sg;
     float* out = Ainv + (int64_t)mat * nn;
     if (singular) {
@@ -458,30 +499,31 @@ k_slogdet_inv_thread(const float* __restrict__ MO, int n, int T, int nmat, doubl
         const int p = pivs[k * TPB + tid];
         if (p == k) continue;
         #pragma unroll 1
-        for (int i = 0; i < n; ++i) { const double t = at(i, k); at(i, k) = at(i, p); at(i, p) = t; }
+        for (int i = 0; i < n; ++i) { const S t = at(i, k); at(i, k) = at(i, p); at(i, p) = t; }
     }
     #pragma unroll 1
     for (int i = 0; i < n; ++i)
         #pragma unroll 1
-        for (int j = 0; j < n; ++j) out[i * n + j] = (float)at(i, j);
+        for (int j = 0; j < n; ++j) out[i * n + j] = lu_to_float(at(i, j));
 }
 
-// FP64 log|det| (and, with INV, the inverse) with SPLIT lanes per matrix: the lanes of a matrix
-// own its rows cyclically (row i belongs to lane i % SPLIT) and run the same elimination as
-// k_slogdet_thread (LU) / k_slogdet_inv_thread (Gauss-Jordan) on their rows, exchanging the
-// pivot choice by shuffles and sharing rows through shared memory. For n > 12 the per-matrix
-// shared memory limits an SM to about a hundred matrices, so a single lane per matrix leaves
-// the FP64 pipe short of warps; splitting the rows multiplies the warps at nearly the same FP64
-// instruction count. Lanes of padding matrices (past nmat) eliminate an identity matrix so that
-// every lane runs every shuffle.
-template <int NMAX, int SPLIT, bool INV>
+// log|det| (and, with INV, the inverse) with SPLIT lanes per matrix, S = double or FF: the
+// lanes of a matrix own its rows cyclically (row i belongs to lane i % SPLIT) and run the same
+// elimination as k_slogdet_thread (LU) / k_slogdet_inv_thread (Gauss-Jordan) on their rows,
+// exchanging the pivot choice by shuffles and sharing rows through shared memory. For n > 12
+// the per-matrix shared memory limits an SM to about a hundred matrices, so a single lane per
+// matrix leaves the arithmetic pipes short of warps; splitting the rows multiplies the warps
+// at nearly the same instruction count. Lanes of padding matrices (past nmat) eliminate an
+// identity matrix so that every lane runs every shuffle.
+template <class S, int NMAX, int SPLIT, bool INV>
 __global__ void __launch_bounds__(32 * SPLIT)
 k_slogdet_split(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
                 double* __restrict__ sign, float* __restrict__ Ainv) {
     constexpr int TPB = 32 * SPLIT, MPB = 32, LD = MPB + 1;
+    static_assert(sizeof(S) == 8, "8-byte elements");
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double* sm = reinterpret_cast<double*>(smem_raw);
-    unsigned char* pivs = smem_raw + (size_t)NMAX * NMAX * LD * sizeof(double);    // [k][matrix]
+    S* sm = reinterpret_cast<S*>(smem_raw);
+    unsigned char* pivs = smem_raw + (size_t)NMAX * NMAX * LD * sizeof(S);    // [k][matrix]
     const int tid = threadIdx.x, m = tid / SPLIT, h = tid % SPLIT;
     const int mat0 = blockIdx.x * MPB;
     const int nm = min(MPB, nmat - mat0);
@@ -489,29 +531,31 @@ k_slogdet_split(const float* __restrict__ MO, int n, int T, int nmat, double* __
     for (int q = tid; q < MPB * nn; q += TPB) {
         const int mm = q / nn, e = q - mm * nn;
         const int i = e / n, j = e - i * n;
-        sm[(i * NMAX + j) * LD + mm] = mm < nm ? (double)__ldg(MO + (int64_t)(mat0 + mm) * T * nn + e)
-                                               : (i == j ? 1.0 : 0.0);
+        sm[(i * NMAX + j) * LD + mm] = lu_from<S>(mm < nm ? __ldg(MO + (int64_t)(mat0 + mm) * T * nn + e)
+                                                          : (i == j ? 1.f : 0.f));
     }
     __syncthreads();
-    double* a = sm + m;
-    auto at = [&](int i, int j) -> double& { return a[(i * NMAX + j) * LD]; };
-    double mant = 1.0, sg = 1.0;
+    S* a = sm + m;
+    auto at = [&](int i, int j) -> S& { return a[(i * NMAX + j) * LD]; };
+    const S one = lu_from<S>(1.f);
+    S mant = one;
+    double sg = 1.0;
     int expo = 0;
     bool singular = false;
     #pragma unroll 1
     for (int k = 0; k < n; ++k) {
         // first own row at or below the diagonal
         const int i0 = k + ((h - k % SPLIT) + SPLIT) % SPLIT;
-        long long best = -1;
+        decltype(lu_key(one)) best = -1;
         int p = n;
         #pragma unroll 1
         for (int i = i0; i < n; i += SPLIT) {
-            const long long v = __double_as_longlong(at(i, k)) & 0x7fffffffffffffffll;
+            const auto v = lu_key(at(i, k));
             if (v > best) { best = v; p = i; }
         }
         #pragma unroll
         for (int o = 1; o < SPLIT; o <<= 1) {
-            const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const auto ob = __shfl_xor_sync(0xffffffffu, best, o);
             const int op = __shfl_xor_sync(0xffffffffu, p, o);
             if (ob > best || (ob == best && op < p)) { best = ob; p = op; }
         }
@@ -522,19 +566,19 @@ k_slogdet_split(const float* __restrict__ MO, int n, int T, int nmat, double* __
         if (p != k) {
             #pragma unroll 1
             for (int j = (INV ? 0 : k) + h; j < n; j += SPLIT) {
-                const double t = at(k, j); at(k, j) = at(p, j); at(p, j) = t;
+                const S t = at(k, j); at(k, j) = at(p, j); at(p, j) = t;
             }
             sg = -sg;
         }
         __syncwarp();
-        double pk = at(k, k);
-        if (sing_now) pk = 1.0;
-        if (pk < 0.0) sg = -sg;
-        mant = mant_mul_norm(mant, fabs(pk), expo);
-        const double rp = recip_nr(pk);
+        S pk = at(k, k);
+        if (sing_now) pk = one;
+        if (lu_neg(pk)) sg = -sg;
+        lu_mant_mul(mant, pk, expo);
+        const auto piv = lu_pivot(pk);
         if (!INV) {
             const int rem = n - k - 1;
-            double u[NMAX - 1];
+            S u[NMAX - 1];
             #pragma unroll
             for (int c = 0; c < NMAX - 1; ++c) {
                 if (c >= rem) break;
@@ -542,20 +586,20 @@ k_slogdet_split(const float* __restrict__ MO, int n, int T, int nmat, double* __
             }
             #pragma unroll 1
             for (int i = i0 + (i0 == k ? SPLIT : 0); i < n; i += SPLIT) {
-                double* row = &at(i, k);
-                const double l = row[0] * rp;
+                S* row = &at(i, k);
+                const S l = lu_quot(row[0], piv);
                 #pragma unroll
                 for (int c = 0; c < NMAX - 1; ++c) {
                     if (c >= rem) break;
-                    row[(c + 1) * LD] = fma(-l, u[c], row[(c + 1) * LD]);
+                    row[(c + 1) * LD] = lu_fnma(l, u[c], row[(c + 1) * LD]);
                 }
             }
         } else {
-            double u[NMAX];
+            S u[NMAX];
             #pragma unroll
             for (int j = 0; j < NMAX; ++j) {
                 if (j >= n) break;
-                u[j] = (j == k ? 1.0 : at(k, j)) * rp;
+                u[j] = lu_quot(j == k ? one : at(k, j), piv);
             }
             __syncwarp();                                     // row k read by every lane of the matrix
             if (k % SPLIT == h) {
@@ -568,15 +612,15 @@ k_slogdet_split(const float* __restrict__ MO, int n, int T, int nmat, double* __
             #pragma unroll 1
             for (int i = h; i < n; i += SPLIT) {
                 if (i == k) continue;
-                double* row = &at(i, 0);
-                const double f = row[k * LD];
+                S* row = &at(i, 0);
+                const S f = row[k * LD];
                 #pragma unroll
                 for (int j = 0; j < NMAX; ++j) {
                     if (j >= n) break;
                     if (j == k) continue;
-                    row[j * LD] = fma(-f, u[j], row[j * LD]);
+                    row[j * LD] = lu_fnma(f, u[j], row[j * LD]);
                 }
-                row[k * LD] = -f * rp;
+                row[k * LD] = lu_negate(lu_quot(f, piv));
             }
         }
         __syncwarp();
@@ -584,7 +628,7 @@ k_slogdet_split(const float* __restrict__ MO, int n, int T, int nmat, double* __
     const bool active = m < nm;
     const int mat = mat0 + m;
     if (active && h == 0) {
-        logdet[mat] = singular ? -INFINITY : log(mant) + (double)expo * 0.69314718055994530942;
+        logdet[mat] = singular ? -INFINITY : lu_log(mant, expo);
         sign[mat] = singular ? 0.0 : sg;
     }
     if (!INV) return;
@@ -594,39 +638,77 @@ k_slogdet_split(const float* __restrict__ MO, int n, int T, int nmat, double* __
         const int p = pivs[k * MPB + m];
         if (p == k) continue;
         #pragma unroll 1
-        for (int i = h; i < n; i += SPLIT) { const double t = at(i, k); at(i, k) = at(i, p); at(i, p) = t; }
+        for (int i = h; i < n; i += SPLIT) { const S t = at(i, k); at(i, k) = at(i, p); at(i, p) = t; }
     }
     if (!active) return;
     float* out = Ainv + (int64_t)mat * nn;
     #pragma unroll 1
     for (int i = h; i < n; i += SPLIT)
         #pragma unroll 1
-        for (int j = 0; j < n; ++j) out[i * n + j] = singular ? 0.f : (float)at(i, j);
+        for (int j = 0; j < n; ++j) out[i * n + j] = singular ? 0.f : lu_to_float(at(i, j));
 }
 
-template <int NMAX, int SPLIT, bool INV>
+template <class S, int NMAX, int SPLIT, bool INV>
 static void launch_slogdet_split(const float* MO, int n, int T, int nmat, double* logdet, double* sign, float* Ainv,
                                  cudaStream_t s) {
-    const size_t smem = (size_t)NMAX * NMAX * 33 * sizeof(double) + (size_t)NMAX * 32;
-    cudaFuncSetAttribute(k_slogdet_split<NMAX, SPLIT, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_slogdet_split<NMAX, SPLIT, INV><<<(unsigned)((nmat + 31) / 32), 32 * SPLIT, smem, s>>>(MO, n, T, nmat, logdet,
+    const size_t smem = (size_t)NMAX * NMAX * 33 * sizeof(S) + (size_t)NMAX * 32;
+    cudaFuncSetAttribute(k_slogdet_split<S, NMAX, SPLIT, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_slogdet_split<S, NMAX, SPLIT, INV><<<(unsigned)((nmat + 31) / 32), 32 * SPLIT, smem, s>>>(MO, n, T, nmat, logdet,
+                                                                                             sign, Ainv);
+}
+
+template <class S, int NMAX, int TPB>
+static void launch_slogdet_inv_thread(const float* MO, int n, int T, int nmat, double* logdet, double* sign, float* Ainv,
+                                      cudaStream_t s) {
+    const size_t smem = (size_t)NMAX * NMAX * (TPB + 1) * sizeof(S) + (size_t)NMAX * TPB;
+    cudaFuncSetAttribute(k_slogdet_inv_thread<S, NMAX, TPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_slogdet_inv_thread<S, NMAX, TPB><<<(unsigned)((nmat + TPB - 1) / TPB), TPB, smem, s>>>(MO, n, T, nmat, logdet,
                                                                                           sign, Ainv);
 }
 
-template <int NMAX, int TPB>
-static void launch_slogdet_inv_thread(const float* MO, int n, int T, int nmat, double* logdet, double* sign, float* Ainv,
-                                      cudaStream_t s) {
-    const size_t smem = (size_t)NMAX * NMAX * (TPB + 1) * sizeof(double) + (size_t)NMAX * TPB;
-    cudaFuncSetAttribute(k_slogdet_inv_thread<NMAX, TPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_slogdet_inv_thread<NMAX, TPB><<<(unsigned)((nmat + TPB - 1) / TPB), TPB, smem, s>>>(MO, n, T, nmat, logdet, sign,
-                                                                                       Ainv);
+template <class S, int NMAX, int TPB>
+static void launch_slogdet_thread(const float* MO, int n, int T, int nmat, double* logdet, double* sign, cudaStream_t s) {
+    const size_t smem = (size_t)NMAX * NMAX * (TPB + 1) * sizeof(S);
+    cudaFuncSetAttribute(k_slogdet_thread<S, NMAX, TPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_slogdet_thread<S, NMAX, TPB><<<(unsigned)((nmat + TPB - 1) / TPB), TPB, smem, s>>>(MO, n, T, nmat, logdet, sign);
 }
 
-template <int NMAX, int TPB>
-static void launch_slogdet_thread(const float* MO, int n, int T, int nmat, double* logdet, double* sign, cudaStream_t s) {
-    const size_t smem = (size_t)NMAX * NMAX * (TPB + 1) * sizeof(double);
-    cudaFuncSetAttribute(k_slogdet_thread<NMAX, TPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_slogdet_thread<NMAX, TPB><<<(unsigned)((nmat + TPB - 1) / TPB), TPB, smem, s>>>(MO, n, T, nmat, logdet, sign);
+// Elimination kernels for n <= 16 in scalar type S (double or FF). FP64: one matrix per thread
+// up to n = 12 (the FP64 pipe is the bound, and a thread per matrix issues the fewest FP64
+// instructions), four lanes per matrix above. Float-float: one matrix per thread up to n = 8,
+// four lanes per matrix above -- its ~15-instruction update chains are latency-bound at the
+// 8 warps per SM that a thread per matrix leaves in shared memory, and four lanes per matrix
+// measured 1.2-2.1x faster for n = 10 and 12 (two or eight lanes: slower than four).
+template <class S>
+static void launch_slogdet_small(const float* MO, int n, int T, int nmat, double* logdet, double* sign, float* Ainv,
+                                 bool want_inv, cudaStream_t s) {
+    constexpr bool ff = std::is_same<S, FF>::value;
+    if (n <= 8 || (!ff && n <= 12)) {
+        if (!want_inv) {
+            if (n <= 4) launch_slogdet_thread<S, 4, 64>(MO, n, T, nmat, logdet, sign, s);
+            else if (n <= 8) launch_slogdet_thread<S, 8, 64>(MO, n, T, nmat, logdet, sign, s);
+            else if (n <= 10) launch_slogdet_thread<S, 10, 64>(MO, n, T, nmat, logdet, sign, s);
+            else launch_slogdet_thread<S, 12, 64>(MO, n, T, nmat, logdet, sign, s);
+        } else {
+            if (n <= 4) launch_slogdet_inv_thread<S, 4, 64>(MO, n, T, nmat, logdet, sign, Ainv, s);
+            else if (n <= 8) launch_slogdet_inv_thread<S, 8, 64>(MO, n, T, nmat, logdet, sign, Ainv, s);
+            else if (n <= 10) launch_slogdet_inv_thread<S, 10, 64>(MO, n, T, nmat, logdet, sign, Ainv, s);
+            else launch_slogdet_inv_thread<S, 12, 64>(MO, n, T, nmat, logdet, sign, Ainv, s);
+        }
+        return;
+    }
+    auto go = [&](auto nmax) {
+        constexpr int NM = decltype(nmax)::value;
+        if (want_inv) launch_slogdet_split<S, NM, 4, true>(MO, n, T, nmat, logdet, sign, Ainv, s);
+        else launch_slogdet_split<S, NM, 4, false>(MO, n, T, nmat, logdet, sign, nullptr, s);
+    };
+    if constexpr (ff) {
+        if (n <= 10) go(std::integral_constant<int, 10>());
+        else if (n <= 12) go(std::integral_constant<int, 12>());
+        else go(std::integral_constant<int, 16>());
+    } else {
+        go(std::integral_constant<int, 16>());
+    }
 }
 
 template <class S>
@@ -648,12 +730,10 @@ void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, 
         const int teams = 32 / n;
         const int64_t warps = (nmat + teams - 1) / teams;
         const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
-        if (!want_inv && std::is_same<S, double>::value && n <= 16) {
-            if (n <= 4) launch_slogdet_thread<4, 64>(MO, n, d.T, nmat, logdet, sign, s);
-            else if (n <= 8) launch_slogdet_thread<8, 64>(MO, n, d.T, nmat, logdet, sign, s);
-            else if (n <= 10) launch_slogdet_thread<10, 64>(MO, n, d.T, nmat, logdet, sign, s);
-            else if (n <= 12) launch_slogdet_thread<12, 64>(MO, n, d.T, nmat, logdet, sign, s);
-            else launch_slogdet_split<16, 4, false>(MO, n, d.T, nmat, logdet, sign, nullptr, s);
+        // the high-precision form (S = double): FP64 elimination, one matrix per thread or four
+        // lanes per matrix, up to n = 16
+        if (std::is_same<S, double>::value && n <= 16) {
+            launch_slogdet_small<double>(MO, n, d.T, nmat, logdet, sign, Ainv, want_inv != 0, s);
             count_launch();
             return;
         }
@@ -669,35 +749,11 @@ void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, 
             count_launch();
             return;
         }
-        if (std::is_same<S, double>::value && n <= 16) {
-            if (n <= 4) launch_slogdet_inv_thread<4, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
-            else if (n <= 8) launch_slogdet_inv_thread<8, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
-            else if (n <= 10) launch_slogdet_inv_thread<10, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
-            else if (n <= 12) launch_slogdet_inv_thread<12, 64>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
-            else launch_slogdet_split<16, 4, true>(MO, n, d.T, nmat, logdet, sign, Ainv, s);
-            count_launch();
-            return;
-        }
         auto go = [&](auto kern) { kern<<<blocks, 128, 0, s>>>(MO, n, d.T, nmat, logdet, sign, Ainv); };
-        bool done = false;
-        if constexpr (std::is_same<S, double>::value) {
-            // exact-size instances of the FP64 form for the common electron counts
-            done = true;
-#define DW_SLOGDET_CASE(NN) case NN: if (want_inv) go(k_slogdet_reg<S, NN, true>); else go(k_slogdet_reg<S, NN, false>); break;
-            switch (n) {
-                DW_SLOGDET_CASE(2) DW_SLOGDET_CASE(3) DW_SLOGDET_CASE(4) DW_SLOGDET_CASE(5) DW_SLOGDET_CASE(6)
-                DW_SLOGDET_CASE(7) DW_SLOGDET_CASE(8) DW_SLOGDET_CASE(9) DW_SLOGDET_CASE(10) DW_SLOGDET_CASE(12)
-                DW_SLOGDET_CASE(14) DW_SLOGDET_CASE(16)
-                default: done = false;
-            }
-#undef DW_SLOGDET_CASE
-        }
-        if (!done) {
-            if (n <= 8) { if (want_inv) go(k_slogdet_reg<S, 8, true>); else go(k_slogdet_reg<S, 8, false>); }
-            else if (n <= 16) { if (want_inv) go(k_slogdet_reg<S, 16, true>); else go(k_slogdet_reg<S, 16, false>); }
-            else if (n <= 24) { if (want_inv) go(k_slogdet_reg<S, 24, true>); else go(k_slogdet_reg<S, 24, false>); }
-            else { if (want_inv) go(k_slogdet_reg<S, 32, true>); else go(k_slogdet_reg<S, 32, false>); }
-        }
+        if (n <= 8) { if (want_inv) go(k_slogdet_reg<S, 8, true>); else go(k_slogdet_reg<S, 8, false>); }
+        else if (n <= 16) { if (want_inv) go(k_slogdet_reg<S, 16, true>); else go(k_slogdet_reg<S, 16, false>); }
+        else if (n <= 24) { if (want_inv) go(k_slogdet_reg<S, 24, true>); else go(k_slogdet_reg<S, 24, false>); }
+        else { if (want_inv) go(k_slogdet_reg<S, 32, true>); else go(k_slogdet_reg<S, 32, false>); }
         count_launch();
         return;
     }
@@ -867,14 +923,32 @@ k_det_tangents_tile(const float* __restrict__ MO, const float* __restrict__ Ainv
     }
     const int c = tid / TPC, tile = tid % TPC, ab = tile / NB, jb = tile % NB;
     const int nn = n * n;
+    // n == NP (a multiple of 4): every channel plane is one contiguous, 16-byte aligned block
+    const bool vec_planes = n == NP && (((uintptr_t)MO) & 15) == 0;
     for (int t0 = 1; t0 < T; t0 += CPR) {
         const int nc = min(CPR, T - t0);
         __syncthreads();                         // previous round's readers of Ds are done
         // stage channels t0 .. t0 + nc - 1 (contiguous in MO), zero-padded to NP x NP
         const float* src = MO + ((int64_t)mat * T + t0) * nn;
-        for (int e = tid; e < CPR * NP * NP; e += 128) {
-            const int cc = e / (NP * NP), r = e % (NP * NP), i = r / NP, j = r % NP;
-            Ds[cc * PP + r] = (cc < nc && i < n && j < n) ? __ldg(src + (int64_t)cc * nn + i * n + j) : 0.f;
+        if (vec_planes) {
+            // a plain copy: consecutive threads move consecutive 16-byte words of a plane
+            constexpr int Q = NP * NP / 4;
+            for (int q = tid; q < CPR * Q; q += 128) {
+                const int cc = q / Q, r4 = q - cc * Q;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (cc < nc) v = __ldg(reinterpret_cast<const float4*>(src + (int64_t)cc * nn) + r4);
+                *reinterpret_cast<float4*>(Ds + cc * PP + 4 * r4) = v;
+            }
+        } else {
+            // one matrix row (channel cc, row i) per thread, its padding zeroed
+            for (int q = tid; q < CPR * NP; q += 128) {
+                const int cc = q / NP, i = q - cc * NP;
+                float* dst = Ds + cc * PP + i * NP;
+                const bool live = cc < nc && i < n;
+                const float* srow = src + (int64_t)cc * nn + i * n;
+                #pragma unroll
+                for (int j = 0; j < NP; ++j) dst[j] = (live && j < n) ? __ldg(srow + j) : 0.f;
+            }
         }
         __syncthreads();
         float acc[4][4];
@@ -1091,3 +1165,19 @@ void launch_combine(const double* logdet, const double* sign, const double* g, c
 }
 
 }  // namespace dw
+
+extern "C" {
+// Test entry: the elimination kernels for n <= 16 in a chosen scalar type (0 = FP64,
+// 1 = float-float) on nmat matrices of n x n FP32 entries at MO + m T n^2, with (want_inv) or
+// without the FP32 inverse. Lets the two forms be compared on the same inputs.
+int dw_debug_slogdet_small(const float* MO, int n, int T, int nmat, int scalar, int want_inv, double* logdet,
+                           double* sign, float* Ainv, void* stream) {
+    if (!MO || !logdet || !sign || n < 1 || n > 16 || T < 1 || nmat < 1 || (scalar != 0 && scalar != 1) ||
+        (want_inv && !Ainv))
+        return DW_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (scalar == 0) dw::launch_slogdet_small<double>(MO, n, T, nmat, logdet, sign, Ainv, want_inv != 0, s);
+    else dw::launch_slogdet_small<dw::FF>(MO, n, T, nmat, logdet, sign, Ainv, want_inv != 0, s);
+    return cudaGetLastError() == cudaSuccess ? DW_OK : DW_ERR_CUDA;
+}
+}  // extern "C"

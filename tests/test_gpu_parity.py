@@ -73,6 +73,83 @@ def test_tc_gemm_matches_torch(cuda, split):
         assert err <= tol * ref.abs().max().item() * (K ** 0.5), (M, N, K, err)
 
 
+def _slater_kinds(n, per_kind, rng):
+    """Matrices of several kinds: Gaussian, graded columns (1 .. 1e-6), near-singular (last row
+    = first + 1e-5 noise), tiny (1e-30) and large (1e30) scales, an exactly zero column, and
+    entries near 1e-37 (the float-float low word goes subnormal there)."""
+    base = rng.standard_normal((7, per_kind, n, n))
+    base[1] *= 10.0 ** (-6.0 * np.arange(n) / n)
+    base[2, :, -1, :] = base[2, :, 0, :] + 1e-5 * rng.standard_normal((per_kind, n))
+    base[3] *= 1e-30
+    base[4] *= 1e30
+    base[5, :, :, n // 2] = 0.0
+    base[6] *= 1e-37
+    return base.astype(np.float32)
+
+
+@pytest.mark.parametrize("n", [3, 7, 10, 12, 13, 16])
+def test_float_float_elimination(cuda, n):
+    """The FP64 elimination kernels (the production form for n <= 16) and their float-float
+    variants against numpy's FP64 slogdet / inverse, on the same matrices.
+    Error model: float-float keeps ~48 significant bits, so |d log|det|| <= c n kappa 2^-47 (FP64:
+    2^-52); the FP32 inverse agrees to a few FP32 ulps times kappa 2^-47."""
+    import ctypes
+    from deeperwin_gb300 import _lib
+    L = _lib.lib()
+    rng = np.random.default_rng(100 + n)
+    per = 256
+    A_ = _slater_kinds(n, per, rng)
+    kinds = np.repeat(np.arange(7), per)
+    M = A_.reshape(-1, n, n)
+    nmat, T = M.shape[0], 2
+    MO = np.zeros((nmat, T, n, n), np.float32)
+    MO[:, 0] = M
+    MO[:, 1] = np.float32(7.0)                       # a second channel the kernels must skip
+    d_MO = torch.from_numpy(MO).cuda()
+    out = {}
+    for scalar in (0, 1):
+        for inv in (0, 1):
+            ld = torch.empty(nmat, dtype=torch.float64, device="cuda")
+            sg = torch.empty(nmat, dtype=torch.float64, device="cuda")
+            Ai = torch.full((nmat, n, n), float("nan"), device="cuda")
+            st = L.dw_debug_slogdet_small(ctypes.c_void_p(d_MO.data_ptr()), n, T, nmat, scalar, inv,
+                                          ctypes.c_void_p(ld.data_ptr()), ctypes.c_void_p(sg.data_ptr()),
+                                          ctypes.c_void_p(Ai.data_ptr()), ctypes.c_void_p(0))
+            assert st == 0
+            torch.cuda.synchronize()
+            out[scalar, inv] = (ld.cpu().numpy(), sg.cpu().numpy(), Ai.cpu().numpy())
+    M64 = M.astype(np.float64)
+    sref, lref = np.linalg.slogdet(M64)
+    zero_col = kinds == 5
+    ok = ~zero_col
+    kappa = np.full(nmat, np.inf)
+    kappa[ok] = np.linalg.cond(M64[ok])
+    for (scalar, inv), (ld, sg, Ai) in out.items():
+        # exactly singular: -inf, sign 0, zero inverse
+        assert np.all(np.isneginf(ld[zero_col])) and np.all(sg[zero_col] == 0.0)
+        if inv:
+            assert np.all(Ai[zero_col] == 0.0)
+        unit = 2.0 ** -52 if scalar == 0 else 2.0 ** -47
+        tol = 1e-12 * np.abs(lref[ok]) + 8 * n * kappa[ok] * unit
+        # entries near 1e-37: the low word is subnormal and float-float falls back toward FP32
+        # accuracy (the reference's own LU is FP32 throughout)
+        tol[kinds[ok] == 6] = np.maximum(tol[kinds[ok] == 6], 2e-3 if scalar else 1e-12)
+        err = np.abs(ld[ok] - lref[ok])
+        assert np.all(err <= tol), (scalar, inv, int(np.argmax(err / tol)), float(np.max(err / tol)))
+        well = ok & (kappa * unit * 1e3 < 1) & (kinds != 6)
+        assert np.array_equal(sg[well], sref[well]), (scalar, inv)
+        if inv:
+            good = well & (kinds != 6)
+            ref = np.linalg.inv(M64[good])
+            scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
+            e = np.abs(Ai[good] - ref) / scale
+            lim = 4 * 2.0 ** -24 + 8 * n * kappa[good][:, None, None] * unit
+            assert np.all(e <= lim), (scalar, float(np.max(e / lim)))
+    # the two kernel forms agree with each other as closely as the error model says
+    d = np.abs(out[1, 0][0][ok] - out[0, 0][0][ok])
+    assert np.all(d <= 1e-12 * np.abs(lref[ok]) + 16 * n * kappa[ok] * 2.0 ** -47 + (kinds[ok] == 6) * 2e-3)
+
+
 @pytest.mark.parametrize("f", GOLDEN, ids=lambda f: f.split("/")[-1])
 def test_forward_plain_matches_reference_golden(cuda, f):
     d, a, p = _fixture(f)

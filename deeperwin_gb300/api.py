@@ -241,8 +241,19 @@ class MetropolisHastingsMonteCarlo:
         self._calls = 0
 
     def run_mcmc_steps(self, func, state: MCMCState, params: Params, n_up: int, n_dn: int, fixed_params=None,
-                       n_steps: int = 1, reevaluate: bool = True) -> MCMCState:
-        """mcmc.py:389-406: re-evaluate log psi^2, then n_steps fused propose/accept steps."""
+                       n_steps: int = 1, reevaluate: bool = True, group=None) -> MCMCState:
+        """mcmc.py:389-406: re-evaluate log psi^2, then n_steps fused propose/accept steps.
+
+        With several ranks (torch.distributed initialised; `group` or the default group) each
+        rank holds its own walkers and a distinct seed, and the acceptance rate is combined over
+        ranks after every step as the reference's pmean (mcmc.py:367): the steps then run one
+        per call (the noise is keyed by walker and step number, so n one-step calls give the
+        walkers of one n-step call) with the chain scalars averaged in between."""
+        from . import dist
+        if dist.world(group) > 1 and n_steps > 1:
+            for k in range(n_steps):
+                self.run_mcmc_steps(func, state, params, n_up, n_dn, fixed_params, 1, reevaluate and k == 0, group)
+            return state
         a = params.arch
         if (n_up, n_dn) != (a.n_up, a.n_dn):
             raise ValueError("spin state does not match the model")
@@ -258,6 +269,8 @@ class MetropolisHastingsMonteCarlo:
                                    _ptr(state.r), B, _ptr(state.R), _ptr(state.Z), _ptr(state.log_psi_sqr),
                                    _ptr(state.walker_age), _ptr(state.scalars), ctypes.byref(cfg), _ptr(ws), nbytes,
                                    _stream()), "dw_mcmc_steps")
+        if n_steps > 0:
+            dist.sync_chain_scalars_(state.scalars, group)
         return state
 
     def run_inter_steps(self, func, state, params, n_up, n_dn, fixed_params=None):

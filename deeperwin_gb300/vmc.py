@@ -14,6 +14,7 @@ from typing import Tuple
 import torch
 
 from . import _lib
+from . import dist
 from .api import Params, _WS, _geometry, _ptr, _stream, local_energy
 
 
@@ -83,9 +84,13 @@ def _clip(E: torch.Tensor, center: float, width: float, clip_by: float):
 
 
 def build_value_and_grad_func(log_psi_sqr_func=None, get_local_energy=None, clipping_config: ClippingConfig = None,
-                              is_complex: bool = False, kfac_register_complex: bool = False):
+                              is_complex: bool = False, kfac_register_complex: bool = False, group=None):
     """Returns value_and_grad(params, clipping_state, spin_state, batch) ->
-    ((loss, (clipping_state, aux)), grads) like the reference's jax.value_and_grad(total_energy)."""
+    ((loss, (clipping_state, aux)), grads) like the reference's jax.value_and_grad(total_energy).
+
+    With several ranks (torch.distributed initialised; `group` or the default group) each rank
+    passes its own walkers and the energy statistics, clipping state and gradients are combined
+    across ranks as the reference's pmean does (see deeperwin_gb300.dist)."""
     if is_complex:
         raise NotImplementedError("only real-valued wavefunctions are supported")
     cfg = clipping_config or ClippingConfig()
@@ -96,6 +101,19 @@ def build_value_and_grad_func(log_psi_sqr_func=None, get_local_energy=None, clip
         r, R, Z = batch[:3]
         E = local_energy(params, spin_state, r, R, Z)
         from .api import energy_stats
+        if dist.world(group) > 1:
+            def stats_fn(e):
+                s = energy_stats(e)
+                return s[0], s[1]
+
+            def clip_fn(e, c, w):
+                ec, o = _clip(e, c, w, cfg.clip_by)
+                return ec, o[0], o[1]
+
+            loss, new_state, aux, grads = dist.sharded_clipped_gradient(
+                E, clipping_state, cfg.clip_by, cfg.from_previous_step, stats_fn, clip_fn,
+                lambda coeff: log_psi_sqr_backward(params, r, R, Z, coeff.float()), group)
+            return (loss, (new_state, aux)), grads
         st = energy_stats(E)
         center, width = clipping_state
         if not cfg.from_previous_step:

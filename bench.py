@@ -139,8 +139,9 @@ def run_ours(args, rank, world, dev):
     L = _lib.lib()
     launches = [0]
 
-    from deeperwin_gb300 import vmc
+    from deeperwin_gb300 import vmc, optim
     clip_state = [vmc.init_clipping_state()]
+    optimizers = {}
 
     def step(prm):
         mh.run_mcmc_steps(None, state, prm, a.n_up, a.n_dn, None, n_steps=n_mh, reevaluate=True)
@@ -153,7 +154,14 @@ def run_ours(args, rank, world, dev):
             Ec, cs = vmc._clip(E, clip_state[0][0], clip_state[0][1], 5.0)
             launches[0] += 1
             coeff = ((Ec.double() - cs[0]) / B).float()
-            vmc.log_psi_sqr_backward(prm, state.r, state.R, state.Z, coeff)
+            g = vmc.log_psi_sqr_backward(prm, state.r, state.R, state.Z, coeff)
+            launches[0] += api.last_launch_count()
+            # Adam update of the packed weights (optax.adam on the inverse schedule,
+            # optimization/opt_utils.py:73-76) and the rebuilt derived weight copies
+            opt = optimizers.get(id(prm))
+            if opt is None:
+                opt = optimizers[id(prm)] = optim.Adam(prm.flat)
+            opt.step(prm, g)
             launches[0] += api.last_launch_count()
             c = cs[2:4].cpu()
             clip_state[0] = (float(c[0]), max(float(c[1]), 1e-12))
@@ -226,12 +234,15 @@ def run_ours(args, rank, world, dev):
 
     plain = None
     if not args.no_plain and w.precision != "fp32":
-        pparams = params.with_precision("fp32")
+        # with parameter updates the plain form optimises its own copy of the weights
+        pparams = (api.Params(a, params.flat.clone(), "fp32") if w.backward else params.with_precision("fp32"))
         kp = max(2, args.steps // 2)
         ms_p, E_plain, _, _, _ = timed(pparams, kp, 1)
-        # same walkers through both forms: accuracy of the mixed form against plain FP32 on the full batch
+        # same walkers and weights through both forms: accuracy of the mixed form against plain
+        # FP32 on the full batch
+        pcmp = params.with_precision("fp32") if w.backward else pparams
         E_m = api.local_energy(params, spin, state.r, state.R, state.Z).double()
-        E_p = api.local_energy(pparams, spin, state.r, state.R, state.Z).double()
+        E_p = api.local_energy(pcmp, spin, state.r, state.R, state.Z).double()
         d = (E_m - E_p)
         ad = d.abs().cpu().numpy() * 1e3
         plain = {"value": world * B / (ms_p / 1e3), "ms_per_step": ms_p,
@@ -282,7 +293,8 @@ def run_ours(args, rank, world, dev):
             "config": {"workload": w.name, "molecule": mol.name, "n_el": a.n_el, "n_up": a.n_up,
                        "n_ions": a.n_ions, "n_dets": a.n_dets, "walkers_per_gpu": B, "mh_steps_per_iter": n_mh,
                        "step": "reevaluate + %d MH forwards + forward-Laplacian E_L" % n_mh
-                               + (" + clipped VMC gradient (hand-written backward)" if w.backward else ""),
+                               + (" + clipped VMC gradient (hand-written backward) + Adam update"
+                                  if w.backward else ""),
                        "precision": w.precision, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set (activations, several GB per step) exceeds L2; no flush needed"},
             "e2e": e2e, "gpu_launches": int(n_launch), "clocks": clocks, "roofline": roof,
@@ -306,10 +318,10 @@ def cpu_sample(a, mol, p_dict, r_sample, threads):
     return time.perf_counter() - t0, E.numpy()
 
 
-def cpu_baseline(args, a, mol, r_sample, gpu_E=None):
+def cpu_baseline(args, a, mol, r_sample, gpu_E=None, p_dict=None):
     from deeperwin_gb300 import params as P
     threads = os.cpu_count() or 1
-    p_dict = P.init_params(a, seed=0)
+    p_dict = p_dict if p_dict is not None else P.init_params(a, seed=0)
     dt, E = cpu_sample(a, mol, p_dict, r_sample, threads)
     out = {"value": round(len(r_sample) / dt, 4), "unit": "walker-evals/s", "cores": threads, "kind": "port",
            "sample": f"{len(r_sample)} walkers x (11 log psi^2 forwards + E_L) of the same workload, FP64 oracle, "
@@ -321,7 +333,7 @@ def cpu_baseline(args, a, mol, r_sample, gpu_E=None):
     return out, acc
 
 
-def worst_walkers(a, mol, state, params, k=4):
+def worst_walkers(a, mol, state, params, p_dict=None, k=4):
     """The k walkers of the full batch where the mixed and plain forms differ most, each checked
     against the FP64 oracle: the tail of the per-walker error (ill-conditioned Slater matrices)."""
     import torch
@@ -333,7 +345,8 @@ def worst_walkers(a, mol, state, params, k=4):
     E_p = api.local_energy(params.with_precision("fp32"), spin, state.r, state.R, state.Z).double()
     idx = torch.argsort((E_m - E_p).abs(), descending=True)[:k]
     r = state.r[idx].double().cpu().numpy()
-    E_o = O.local_energy(O.tparams(P.init_params(a, seed=0)), a, r, mol.R, mol.Z)[0].numpy()
+    p_dict = p_dict if p_dict is not None else P.init_params(a, seed=0)
+    E_o = O.local_energy(O.tparams(p_dict), a, r, mol.R, mol.Z)[0].numpy()
     return {"selection": f"the {k} walkers of the full batch with the largest |E_mixed - E_plain|",
             "E_oracle_Ha": [round(float(x), 6) for x in E_o],
             "mixed_abs_err_mHa": [round(float(x), 3) for x in np.abs(E_m[idx].cpu().numpy() - E_o) * 1e3],
@@ -393,6 +406,7 @@ def main():
     if rank == 0:
         if not args.no_cpu_baseline:
             from deeperwin_gb300 import api
+            from deeperwin_gb300 import params as P
             state, params, a, mol, w = ctx
             r_sample = state.r[:8].double().cpu().numpy()
             gpu_E = {"mixed" if w.precision != "fp32" else "fp32":
@@ -400,11 +414,13 @@ def main():
             if w.precision != "fp32":
                 gpu_E["fp32"] = api.local_energy(params.with_precision("fp32"), (a.n_up, a.n_dn), r_sample, mol.R,
                                                  mol.Z).double().cpu().numpy()
-            cb, acc = cpu_baseline(args, a, mol, r_sample, gpu_E)
+            # the oracle evaluates the weights the GPU holds now (updated ones after optimisation steps)
+            p_now = P.unpack(a, params.flat.detach().cpu().numpy()) if w.backward else None
+            cb, acc = cpu_baseline(args, a, mol, r_sample, gpu_E, p_now)
             out["cpu_baseline"] = cb
             out["accuracy_vs_fp64_oracle"] = acc
             if w.precision != "fp32" and not args.no_plain:
-                out["accuracy_worst_walkers_vs_fp64_oracle"] = worst_walkers(a, mol, state, params)
+                out["accuracy_worst_walkers_vs_fp64_oracle"] = worst_walkers(a, mol, state, params, p_now)
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.barrier()

@@ -119,3 +119,29 @@ def test_autograd_function_and_value_and_grad(cuda):
     g3 = vmc.log_psi_sqr_backward(params, r, mol.R, mol.Z, coeff.float())
     torch.testing.assert_close(grads, g3, rtol=1e-4, atol=1e-6)
     assert state[1] == pytest.approx(5.0 * float(E.std(unbiased=False)), rel=1e-5)
+
+
+def test_vmc_optimisation_step_with_adam(cuda):
+    """One VMC optimisation step (the OptaxWrapper step, optimizers.py:113-140, with optax.adam):
+    clipped gradient from the hand-written backward, Adam update of the packed weights on the GPU,
+    derived weight copies rebuilt so that the next forward sees the new weights."""
+    from deeperwin_gb300 import optim
+    mol = A.lih()
+    a = A.arch_for(mol, 4)
+    params = api.Params.from_dict(a, P.init_params(a, 2, bias_std=0.1, envelope_jitter=0.2), "mixed")
+    r = torch.tensor(A.init_walkers(mol, 64, seed=1), dtype=torch.float32, device="cuda")
+    vg = vmc.build_value_and_grad_func()
+    (loss, (clip_state, aux)), g = vg(params, vmc.init_clipping_state(), (a.n_up, a.n_dn), (r, mol.R, mol.Z))
+    assert torch.isfinite(g).all() and g.abs().max() > 0
+    flat0 = params.flat.clone()
+    _, lp0 = api.log_psi_sqr(params, a.n_up, a.n_dn, r, mol.R, mol.Z)
+    opt = optim.Adam(params.flat)
+    opt.step(params, g)
+    # first Adam step: theta - lr(0) g / (|g| + eps), lr(0) = 1e-3
+    gd = g.double()
+    torch.testing.assert_close(params.flat.double(), flat0.double() - 1e-3 * gd / (gd.abs() + 1e-8), rtol=0, atol=2e-7)
+    _, lp1 = api.log_psi_sqr(params, a.n_up, a.n_dn, r, mol.R, mol.Z)
+    fresh = api.Params.from_dict(a, P.unpack(a, params.flat.cpu().numpy()), "mixed")
+    _, lp2 = api.log_psi_sqr(fresh, a.n_up, a.n_dn, r, mol.R, mol.Z)
+    torch.testing.assert_close(lp1, lp2, rtol=0, atol=0)
+    assert (lp1 - lp0).abs().max() > 1e-4

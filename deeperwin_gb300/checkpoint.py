@@ -20,11 +20,11 @@ method, ``parent/name`` in ``__call__``):
 packed name                 haiku path / parameter
 ==========================  =====================================================================
 ion_embed                   wf/~/input/h_ion : embeddings (``model/input_features.py:184-191``)
-symm{i}.{w_same,w_diff,     wf/~_calculate_embedding/ferminet_embedding/symm_features_{i}/
+symm{i}.{w_same,w_diff,     wf/~_calculate_embedding/fermi_net_embedding/symm_features_{i}/
 h_map,h_ion_map}.{w,b}      convolutional_features/{...}/linear_0 : w, b
                             (``model/embeddings/ferminet_embedding.py:97-175, 218``)
-h_el{i}.{w,b}               wf/~_calculate_embedding/ferminet_embedding/h_el_{i}/linear_0
-h_same{i}, h_diff{i},       .../ferminet_embedding/h_same_{i}, h_diff_{i}, h_el_ion_{i}/linear_0
+h_el{i}.{w,b}               wf/~_calculate_embedding/fermi_net_embedding/h_el_{i}/linear_0
+h_same{i}, h_diff{i},       .../fermi_net_embedding/h_same_{i}, h_diff_{i}, h_el_ion_{i}/linear_0
 h_ei{i}                     (``ferminet_embedding.py:233-262``)
 bf_up.w, bf_dn.w            wf/~/orbitals/envelope_orbitals/bf_up|bf_dn/linear_0 : w
                             (``model/orbitals/envelope_orbitals.py:46-70``)
@@ -32,9 +32,11 @@ alpha_*, weights_*          wf/~/orbitals/envelope_orbitals : alpha_up, ... (``:
 jas{l}.{w,b}                wf/~/jastrow_factor/mlp/linear_{l} (``model/wavefunction.py:42-60``)
 ==========================  =====================================================================
 
-Paths are matched with their ``~`` components removed, so both the spelling above and the one
-without them (as ``model/wavefunction.py:346-353`` indexes ``wf/orbitals/envelope_orbitals``)
-are read. Dense layers are haiku ``Linear`` (``w[d_in, d_out]``) in both layouts, and the rows of
+A module without a name is named after its class in snake case (``FermiNetEmbedding`` ->
+``fermi_net_embedding``). Paths are matched with their ``~`` components removed, so both the
+spelling above and the one without them (as ``model/wavefunction.py:346-353`` indexes
+``wf/orbitals/envelope_orbitals``) are read; the ``~``-free paths are pinned by the list of
+parameters the reference's own module code requests (``tests/golden/haiku_paths_lih_k8.txt``). Dense layers are haiku ``Linear`` (``w[d_in, d_out]``) in both layouts, and the rows of
 ``h_el0.w`` follow the reference's feature concatenation, so every tensor copies unchanged.
 """
 from __future__ import annotations
@@ -50,7 +52,7 @@ import numpy as np
 from .arch import Arch
 from .params import param_shapes
 
-_EMB = "wf/~_calculate_embedding/ferminet_embedding"
+_EMB = "wf/~_calculate_embedding/fermi_net_embedding"
 _ENV = "wf/~/orbitals/envelope_orbitals"
 
 

@@ -256,8 +256,10 @@ _MAP = [
 ]
 
 
-def provider_for(params: dict, seen: set):
+def provider_for(params: dict, seen: set, requested: dict = None):
     def fn(path, shape):
+        if requested is not None:
+            requested[path] = tuple(shape)
         for pat, name_fn in _MAP:
             m = re.search(pat, path)
             if m:
@@ -268,7 +270,7 @@ def provider_for(params: dict, seen: set):
     return fn
 
 
-def reference_forward(g: dict, arch: A.Arch, params: dict, r, R, Z):
+def reference_forward(g: dict, arch: A.Arch, params: dict, r, R, Z, requested: dict = None):
     cfg = g["cfg"]
     model_cfg = cfg.ModelConfigDeepErwin4(
         orbitals=cfg.OrbitalsConfigFermiNet(n_determinants=arch.n_dets),
@@ -276,7 +278,7 @@ def reference_forward(g: dict, arch: A.Arch, params: dict, r, R, Z):
         Z_min=arch.z_min, Z_max=arch.z_max)
     wdef = g["WavefunctionDefinition"](Z_max=arch.z_max, Z_min=arch.z_min)
     seen: set = set()
-    _PROVIDER["fn"] = provider_for(params, seen)
+    _PROVIDER["fn"] = provider_for(params, seen, requested)
     _COUNTS.clear()
     _STACK.clear()
     wf = g["Wavefunction"](model_cfg, wdef)
@@ -300,7 +302,7 @@ CASES = [
 ]
 
 
-def main(ref_root: str):
+def main(ref_root: str, paths_only: bool = False):
     g = load_reference(Path(ref_root))
     out_dir = Path(__file__).resolve().parent
     for name, mol_fn, K, B, bstd, jit in CASES:
@@ -308,7 +310,16 @@ def main(ref_root: str):
         arch = A.arch_for(mol, K)
         params = P.init_params(arch, seed=0, bias_std=bstd, envelope_jitter=jit)
         r = A.init_walkers(mol, B, seed=1)
-        phase, lp, mo = reference_forward(g, arch, params, r, mol.R, mol.Z)
+        requested: dict = {}
+        phase, lp, mo = reference_forward(g, arch, params, r, mol.R, mol.Z, requested)
+        if name == "lih_k8":
+            # every parameter path the reference's modules request (the stand-in names modules by
+            # nesting only, without haiku's "~" markers), with its shape
+            with open(out_dir / "haiku_paths_lih_k8.txt", "w") as f:
+                for path in sorted(requested):
+                    f.write(f"{path}\t{','.join(map(str, requested[path]))}\n")
+        if paths_only:
+            continue
         e_pot = g["get_potential_energy"](r, np.asarray(mol.R, np.float64), np.asarray(mol.Z, np.float64))
         # clipping statistics on a fixed synthetic energy vector (loss_function.py:44-72)
         rng = np.random.default_rng(3)
@@ -331,4 +342,5 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if a != "--paths-only"]
+    main(args[0] if args else "/root/reference", paths_only="--paths-only" in sys.argv)

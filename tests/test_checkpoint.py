@@ -26,13 +26,29 @@ def test_name_map_covers_every_tensor_once():
     assert len(set(names.values())) == len(names)
     assert names["ion_embed"] == ("wf/~/input/h_ion", "embeddings")
     assert names["symm1.w_same.b"] == (
-        "wf/~_calculate_embedding/ferminet_embedding/symm_features_1/convolutional_features/w_same/linear_0", "b")
-    assert names["h_ei2.w"] == ("wf/~_calculate_embedding/ferminet_embedding/h_el_ion_2/linear_0", "w")
-    assert names["h_el3.w"] == ("wf/~_calculate_embedding/ferminet_embedding/h_el_3/linear_0", "w")
+        "wf/~_calculate_embedding/fermi_net_embedding/symm_features_1/convolutional_features/w_same/linear_0", "b")
+    assert names["h_ei2.w"] == ("wf/~_calculate_embedding/fermi_net_embedding/h_el_ion_2/linear_0", "w")
+    assert names["h_el3.w"] == ("wf/~_calculate_embedding/fermi_net_embedding/h_el_3/linear_0", "w")
     assert names["bf_dn.w"] == ("wf/~/orbitals/envelope_orbitals/bf_dn/linear_0", "w")
     assert names["alpha_up"] == ("wf/~/orbitals/envelope_orbitals", "alpha_up")
     assert names["jas2.w"] == ("wf/~/jastrow_factor/mlp/linear_2", "w")
     assert "jas2.b" not in names                      # Jastrow output layer has no bias (wavefunction.py:58)
+
+
+def test_paths_match_what_the_reference_modules_request():
+    """tests/golden/haiku_paths_lih_k8.txt lists every parameter the reference's own module code
+    requests for LiH with 8 determinants (tests/golden/make_golden.py runs that code with a haiku
+    stand-in that names modules by nesting, without haiku's "~" markers), with its shape."""
+    from pathlib import Path
+    from deeperwin_gb300 import arch as A
+    a = A.arch_for(A.lih(), 8)
+    recorded = {}
+    for line in (Path(__file__).parent / "golden" / "haiku_paths_lih_k8.txt").read_text().splitlines():
+        path, shape = line.split("\t")
+        recorded[path] = tuple(int(x) for x in shape.split(","))
+    shapes = P.param_shapes(a)
+    ours = {C._canonical(mod) + "/" + p: shapes[name] for name, (mod, p) in C.haiku_names(a).items()}
+    assert ours == recorded
 
 
 def test_round_trip_through_haiku_tree():

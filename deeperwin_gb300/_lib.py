@@ -102,7 +102,14 @@ def exported_symbols():
     return list(_SIGS)
 
 
+# Launch count standing in for the library's own when one host-level call issued several library
+# calls (run_mcmc_steps with the steps split across ranks); any later checked call clears it.
+launch_override = None
+
+
 def check(status: int, what: str = "") -> None:
+    global launch_override
+    launch_override = None
     if status != 0:
         msg = lib().dw_status_string(status).decode()
         raise RuntimeError(f"{what}: dwgb status {status} ({msg})")

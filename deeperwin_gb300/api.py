@@ -251,8 +251,11 @@ class MetropolisHastingsMonteCarlo:
         walkers of one n-step call) with the chain scalars averaged in between."""
         from . import dist
         if dist.world(group) > 1 and n_steps > 1:
+            total = 0
             for k in range(n_steps):
                 self.run_mcmc_steps(func, state, params, n_up, n_dn, fixed_params, 1, reevaluate and k == 0, group)
+                total += last_launch_count()
+            _lib.launch_override = total         # last_launch_count() reports all n calls
             return state
         a = params.arch
         if (n_up, n_dn) != (a.n_up, a.n_dn):
@@ -288,4 +291,8 @@ def energy_stats(E: torch.Tensor) -> torch.Tensor:
 
 
 def last_launch_count() -> int:
+    """Kernel launches of the last library call on this thread (of all its one-step calls when
+    run_mcmc_steps split the steps across ranks)."""
+    if _lib.launch_override is not None:
+        return int(_lib.launch_override)
     return int(_lib.lib().dw_last_launch_count())

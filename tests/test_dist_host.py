@@ -128,6 +128,9 @@ def _mcmc_loop(rank: int):
         def dw_workspace_bytes(self, *a):
             return 0
 
+        def dw_last_launch_count(self):
+            return 2 + (calls[-1][1] if calls else 0)    # stand-in count: 2, plus 1 with re-evaluation
+
         def dw_mcmc_steps(self, arch, prec, flat, prepared, r, B, R, Z, lp, age, scalars, cfg, ws, nbytes, stream):
             c = cfg._obj
             calls.append((c.n_steps, c.reevaluate))
@@ -151,7 +154,10 @@ def _mcmc_loop(rank: int):
     mh = api.MetropolisHastingsMonteCarlo(api.MCMCConfig())
     mh.run_mcmc_steps(None, state, params, 2, 2, None, n_steps=5, reevaluate=True)
     fin = _lib.DwMcmcScalars.from_buffer_copy(bytes(state.scalars.numpy()))
-    return {"calls": calls, "acc_rate": fin.acc_rate, "step_nr": fin.step_nr}
+    launches = api.last_launch_count()
+    _lib.check(0)                                  # a later library call clears the sum
+    return {"calls": calls, "acc_rate": fin.acc_rate, "step_nr": fin.step_nr, "launches": launches,
+            "launches_after": api.last_launch_count()}
 
 
 def _run(case):
@@ -215,6 +221,7 @@ def test_mcmc_steps_sync_acceptance_every_step():
         acc = 0.9 * acc + 0.1 * np.mean([_accept_fraction(r, t) for r in range(WORLD)])
     for res in out:
         assert res["calls"] == [(1, 1), (1, 0), (1, 0), (1, 0), (1, 0)]
+        assert res["launches"] == 3 + 4 * 2 and res["launches_after"] == 2   # summed over the calls
         assert res["step_nr"] == 5
         np.testing.assert_allclose(res["acc_rate"], acc, rtol=1e-14)
 
@@ -232,5 +239,5 @@ def test_mcmc_steps_single_rank_one_call():
     acc = 0.5
     for t in range(5):
         acc = 0.9 * acc + 0.1 * _accept_fraction(0, t)
-    assert res["calls"] == [(5, 1)] and res["step_nr"] == 5
+    assert res["calls"] == [(5, 1)] and res["step_nr"] == 5 and res["launches"] == 3
     np.testing.assert_allclose(res["acc_rate"], acc, rtol=1e-14)

@@ -145,3 +145,33 @@ def test_vmc_optimisation_step_with_adam(cuda):
     _, lp2 = api.log_psi_sqr(fresh, a.n_up, a.n_dn, r, mol.R, mol.Z)
     torch.testing.assert_close(lp1, lp2, rtol=0, atol=0)
     assert (lp1 - lp0).abs().max() > 1e-4
+
+
+def test_sharded_gradient_composition_on_one_rank(cuda):
+    """deeperwin_gb300.dist.sharded_clipped_gradient over the GPU statistics, clipping and backward
+    kernels equals value_and_grad's single-rank result (loss, next clipping state, gradient)."""
+    from deeperwin_gb300 import dist
+    mol = A.lih()
+    a = A.arch_for(mol, 4)
+    params = api.Params.from_dict(a, P.init_params(a, 2, bias_std=0.1, envelope_jitter=0.2), "mixed")
+    r = torch.tensor(A.init_walkers(mol, 64, seed=1), dtype=torch.float32, device="cuda")
+    vg = vmc.build_value_and_grad_func()
+    for state in [(-7.5, 3.0), (0.0, 1e12)]:
+        (loss, (new_state, aux)), g = vg(params, state, (a.n_up, a.n_dn), (r, mol.R, mol.Z))
+        E = aux["E_loc"]
+
+        def stats_fn(e):
+            s = api.energy_stats(e)
+            return s[0], s[1]
+
+        def clip_fn(e, c, w):
+            ec, o = vmc._clip(e, c, w, 5.0)
+            return ec, o[0], o[1]
+
+        loss2, state2, aux2, g2 = dist.sharded_clipped_gradient(
+            E, state, 5.0, True, stats_fn, clip_fn,
+            lambda coeff: vmc.log_psi_sqr_backward(params, r, mol.R, mol.Z, coeff.float()))
+        assert float(loss2) == float(loss)
+        np.testing.assert_allclose(state2, new_state, rtol=1e-12)
+        # the weight-gradient reductions accumulate with atomics: equal up to summation order
+        torch.testing.assert_close(g2, g, rtol=1e-5, atol=1e-6 * float(g.abs().max()))

@@ -82,3 +82,40 @@ def test_max_age_forces_acceptance(cuda):
     torch.cuda.synchronize()
     assert (state.walker_age == 0).all()
     assert torch.isfinite(state.log_psi_sqr).all()
+
+
+def test_one_step_calls_reproduce_a_multi_step_call(cuda):
+    """n one-step calls (re-evaluation on the first only) give the walkers, log psi^2, ages and
+    chain scalars of one n-step call: the noise and the uniforms are keyed by (walker, step
+    number), and the accept-only phase updates the step size by the same rule as the fused
+    accept / propose phase. The multi-rank loop of run_mcmc_steps relies on this."""
+    mol, a, p, params, s1 = _setup("mixed", B=96, seed=3)
+    _, _, _, _, s2 = _setup("mixed", B=96, seed=3)
+    for s in (s1, s2):
+        s.seed = 77
+        s.scalars[:] = torch.frombuffer(bytearray(bytes(api._lib.DwMcmcScalars(0.4, 0.0, 0.05, 95, 0, 0))),
+                                        dtype=torch.uint8).cuda()
+    mh = api.MetropolisHastingsMonteCarlo(api.MCMCConfig(max_age=3, stepsize_update_interval=4))
+    mh.run_mcmc_steps(None, s1, params, a.n_up, a.n_dn, None, n_steps=9, reevaluate=True)
+    for k in range(9):
+        mh.run_mcmc_steps(None, s2, params, a.n_up, a.n_dn, None, n_steps=1, reevaluate=(k == 0))
+    torch.cuda.synchronize()
+    assert torch.equal(s1.r, s2.r)
+    assert torch.equal(s1.log_psi_sqr, s2.log_psi_sqr) and torch.equal(s1.walker_age, s2.walker_age)
+    h1, h2 = s1._host_scalars(), s2._host_scalars()
+    assert (h1.acc_rate, h1.last_acc, h1.stepsize, h1.step_nr) == (h2.acc_rate, h2.last_acc, h2.stepsize, h2.step_nr)
+    assert h1.step_nr == 104 and abs(h1.stepsize - 0.05) > 1e-3   # the step-size rule ran (steps 96, 100, 104)
+
+
+def test_evaluation_loop(cuda):
+    """evaluation.evaluate_wavefunction: burn-in, inter-steps and the FP64 energy mean per epoch
+    (optimization/evaluation.py:117-201), summarised with the autocorrelation-corrected sigma."""
+    from deeperwin_gb300 import evaluation
+    mol, a, p, params, state = _setup("mixed", B=128, seed=5)
+    mh = api.MetropolisHastingsMonteCarlo(api.MCMCConfig(n_burn_in=20, n_inter_steps=5))
+    hist, summ, st = evaluation.evaluate_wavefunction(params, state, mh, n_epochs=6)
+    assert len(hist["E_mean"]) == 6 and np.all(np.isfinite(hist["E_mean"])) and np.all(np.array(hist["E_var"]) >= 0)
+    E = api.local_energy(params, (a.n_up, a.n_dn), st.r, st.R, st.Z).double()
+    assert abs(hist["E_mean"][-1] - E.mean().item()) <= 1e-9 * max(1.0, abs(E.mean().item()))
+    assert st.step_nr == 20 + 6 * 5
+    assert summ["E_mean_sigma"] >= 0 and np.isfinite(summ["E_mean_sigma_corr"])

@@ -15,7 +15,10 @@ It writes ``tests/golden/*.npz``. The fixtures hold the walkers, nuclei, the see
 init settings of the weights (weights are regenerated by
 ``deeperwin_gb300.params.init_params``; a checksum of the packed weights is stored to
 catch drift) and the reference's outputs: log psi^2, phase, the Slater matrices, the
-potential energy and the energy-clipping statistics.
+potential energy and the energy-clipping statistics. It also writes
+``tests/golden/haiku_paths_lih_k8.txt``: every parameter path (module nesting as the stand-in
+names it, without haiku's "~" markers) and shape that the reference's modules request for the
+LiH case; ``--paths-only`` writes that list alone.
 """
 from __future__ import annotations
 

@@ -195,11 +195,11 @@ static const size_t kChunkBudget = (size_t)6 << 30;   // bytes of activations pe
 // Walkers per chunk: the marginal workspace of one walker (the plan also holds fixed buffers,
 // such as the per-geometry ion maps, that do not grow with the chunk) against the budget.
 template <class Act>
-static int choose_chunk(const Dims& d, int B) {
+static int choose_chunk(const Dims& d, int B, size_t budget = kChunkBudget) {
     const size_t one = carve_plan<Act>(d, 1, nullptr).bytes, two = carve_plan<Act>(d, 2, nullptr).bytes;
     const size_t per = std::max<size_t>(two > one ? two - one : one, 1);
     const size_t fixed = one > per ? one - per : 0;
-    const size_t avail = kChunkBudget > fixed ? kChunkBudget - fixed : per;
+    const size_t avail = budget > fixed ? budget - fixed : per;
     int bc = (int)std::max<size_t>(1, avail / per);
     return std::min(bc, B);
 }
@@ -372,11 +372,13 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
     return DW_OK;
 }
 
-// Calls f(tag) with a null pointer of the activation type of the precision form.
+// Calls f(tag) with a null pointer of the activation type of the precision form (double: the FP64
+// form of fp64.cu).
 template <class F>
 static int with_act(int precision, bool need_device, F&& f) {
     switch (precision) {
         case DW_PRECISION_FP32: return f((float*)nullptr);
+        case DW_PRECISION_FP64: return f((double*)nullptr);
         case DW_PRECISION_MIXED:
             if (need_device && !tc_available()) return DW_ERR_UNSUPPORTED;
             return f((Split*)nullptr);
@@ -389,22 +391,29 @@ static int with_act(int precision, bool need_device, F&& f) {
 template <class T> using act_of = typename std::remove_pointer<T>::type;
 
 template <class Act>
-static size_t plan_bytes(const DwArch* a, int B, bool tang) {
+static size_t plan_bytes(const DwArch* a, int B, bool tang, size_t budget = kChunkBudget) {
     Dims d = make_dims(a, tang);
-    return (carve_plan<Act>(d, choose_chunk<Act>(d, std::max(B, 1)), nullptr).bytes + 4096 + 255) / 256 * 256;
+    return (carve_plan<Act>(d, choose_chunk<Act>(d, std::max(B, 1), budget), nullptr).bytes + 4096 + 255) / 256 * 256;
+}
+
+// Workspace of one forward (value or tangent) and the forward itself, for every precision form.
+template <class Act>
+static size_t plan_bytes_any(const DwArch* a, int B, bool tang) {
+    if constexpr (std::is_same<Act, double>::value) return fp64_plan_bytes(a, B, tang);
+    else return plan_bytes<Act>(a, B, tang);
 }
 
 template <class Act>
 static size_t ws_bytes_t(const DwArch* a, int n_walkers, int mode) {
     if (mode == 3) return bwd_bytes(a, n_walkers, nullptr);
     if (mode == 2) {
-        size_t b = plan_bytes<Act>(a, n_walkers, false);
+        size_t b = plan_bytes_any<Act>(a, n_walkers, false);
         b += (size_t)n_walkers * a->n_el * 3 * sizeof(float) + 256;      // proposals
         b += (size_t)n_walkers * sizeof(float) + 256;                    // proposal log psi^2
         b += (size_t)mh_counts_needed(kMaxSeg) * sizeof(int) + 256;
         return b;
     }
-    size_t b = plan_bytes<Act>(a, n_walkers, mode == 1);
+    size_t b = plan_bytes_any<Act>(a, n_walkers, mode == 1);
     if (mode == 1) b += (size_t)n_walkers * sizeof(float) + 256;         // log psi^2 when not requested
     return b;
 }
@@ -412,7 +421,8 @@ static size_t ws_bytes_t(const DwArch* a, int n_walkers, int mode) {
 template <class Act>
 static int forward_all(const DwArch* a, int precision, const float* P, const void* prepared, const float* r, int B,
                        const float* R, const int32_t* Z, float* lp, float* phase, float* E, float* grad, bool tang,
-                       void* ws, size_t ws_bytes, cudaStream_t s, const int32_t* seg = nullptr, int nseg = 1) {
+                       void* ws, size_t ws_bytes, cudaStream_t s, const int32_t* seg = nullptr, int nseg = 1,
+                       size_t budget = kChunkBudget) {
     Dims d = make_dims(a, tang);
     if (nseg < 1 || nseg > kMaxSeg || (nseg > 1 && !seg)) return DW_ERR_ARG;
     // the fused forward-Laplacian epilogue keeps one electron's channels inside a 128-row tile
@@ -420,7 +430,7 @@ static int forward_all(const DwArch* a, int precision, const float* P, const voi
     ParamLayout L;
     make_layout(a, &L);
     Prepared pre = carve_prepared(a, precision, const_cast<void*>(prepared));
-    int bc = choose_chunk<Act>(d, B);
+    int bc = choose_chunk<Act>(d, B, budget);
     Plan<Act> p = carve_plan<Act>(d, bc, ws);
     if (p.bytes > ws_bytes) return DW_ERR_WORKSPACE;
     d.nseg = nseg;
@@ -436,18 +446,44 @@ static int forward_all(const DwArch* a, int precision, const float* P, const voi
     return DW_OK;
 }
 
+template <class Act>
+static int forward_any(const DwArch* a, int precision, const float* P, const void* prepared, const float* r, int B,
+                       const float* R, const int32_t* Z, float* lp, float* phase, float* E, float* grad, bool tang,
+                       void* ws, size_t ws_bytes, cudaStream_t s, const int32_t* seg = nullptr, int nseg = 1) {
+    if constexpr (std::is_same<Act, double>::value)
+        return fp64_forward_all(a, P, prepared, r, B, R, Z, lp, phase, E, grad, tang, ws, ws_bytes, s, seg, nseg, nullptr);
+    else
+        return forward_any<Act>(a, precision, P, prepared, r, B, R, Z, lp, phase, E, grad, tang, ws, ws_bytes, s, seg, nseg);
+}
+
+// FP32 row-gathered layer weights of a prepared buffer (the same offsets in every precision form).
+void prepared_fp32_layers(const DwArch* a, const void* prepared, const float* main[4], const float* mean[4]) {
+    Prepared p = carve_prepared(a, DW_PRECISION_FP32, const_cast<void*>(prepared));
+    for (int l = 0; l < 4; ++l) { main[l] = p.main[l]; mean[l] = p.mean[l]; }
+}
+
 // Value-only forward for the workspace-free entry point (noalloc.cu): bytes of scratch it needs
 // and the call itself on a caller-supplied scratch region.
-size_t value_forward_bytes(const DwArch* a, int precision, int B) {
+// Scratch bytes and call of the value-only forward with walker chunks sized against `budget`
+// bytes (the workspace-free entry point passes its fixed array, so a large batch runs in several
+// chunks instead of being refused). The FP64 form is not offered there.
+size_t value_forward_bytes(const DwArch* a, int precision, int B, size_t budget) {
     size_t out = 0;
-    with_act(precision, false, [&](auto tag) { out = plan_bytes<act_of<decltype(tag)>>(a, B, false); return 0; });
+    with_act(precision, false, [&](auto tag) {
+        using Act = act_of<decltype(tag)>;
+        if constexpr (!std::is_same<Act, double>::value) out = plan_bytes<Act>(a, B, false, budget);
+        return 0;
+    });
     return out;
 }
 int value_forward(const DwArch* a, int precision, const float* params, const void* prepared, const float* r, int B,
-                  const float* R, const int32_t* Z, float* lp, float* phase, void* ws, size_t wsb, cudaStream_t s) {
+                  const float* R, const int32_t* Z, float* lp, float* phase, void* ws, size_t wsb, size_t budget,
+                  cudaStream_t s) {
     return with_act(precision, true, [&](auto tag) {
         using Act = act_of<decltype(tag)>;
-        return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s);
+        if constexpr (std::is_same<Act, double>::value) return (int)DW_ERR_ARG;
+        else return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws,
+                                     wsb, s, nullptr, 1, budget);
     });
 }
 
@@ -466,7 +502,7 @@ int dw_prepare_params(const DwArch* a, int precision, const float* params, void*
     reset_launch_count();
     DW_CHECK(check_arch(a));
     if (!params || !prepared) return DW_ERR_ARG;
-    if (precision < DW_PRECISION_FP32 || precision > DW_PRECISION_BF16) return DW_ERR_ARG;
+    if (precision < DW_PRECISION_FP32 || precision > DW_PRECISION_FP64) return DW_ERR_ARG;
     return prepare(a, precision, params, prepared, bytes, (cudaStream_t)stream);
 }
 
@@ -485,7 +521,7 @@ int dw_log_psi_sqr(const DwArch* a, int precision, const float* params, const vo
     cudaStream_t s = (cudaStream_t)stream;
     return with_act(precision, true, [&](auto tag) {
         using Act = act_of<decltype(tag)>;
-        return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s);
+        return forward_any<Act>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s);
     });
 }
 
@@ -497,7 +533,7 @@ int dw_local_energy(const DwArch* a, int precision, const float* params, const v
     cudaStream_t s = (cudaStream_t)stream;
     return with_act(precision, true, [&](auto tag) {
         using Act = act_of<decltype(tag)>;
-        size_t pb = plan_bytes<Act>(a, B, true);
+        size_t pb = plan_bytes_any<Act>(a, B, true);
         float* lpo = lp;
         size_t fwd_bytes = wsb;
         if (!lpo) {   // log psi^2 output is optional; it then lives in the workspace tail
@@ -505,7 +541,7 @@ int dw_local_energy(const DwArch* a, int precision, const float* params, const v
             lpo = reinterpret_cast<float*>(static_cast<char*>(ws) + pb);
             fwd_bytes = pb;
         }
-        return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, fwd_bytes, s);
+        return forward_any<Act>(a, precision, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, fwd_bytes, s);
     });
 }
 
@@ -530,14 +566,14 @@ static int mcmc_impl(const DwArch* a, int precision, const float* params, const 
     return with_act(precision, true, [&](auto tag) {
         using Act = act_of<decltype(tag)>;
         if (wsb < ws_bytes_t<Act>(a, B, 2)) return (int)DW_ERR_WORKSPACE;
-        size_t fwd = plan_bytes<Act>(a, B, false);
+        size_t fwd = plan_bytes_any<Act>(a, B, false);
         Carver c(static_cast<char*>(ws) + fwd, wsb - fwd);
         float* r_prop = c.take<float>((size_t)B * a->n_el * 3);
         float* lp_prop = c.take<float>((size_t)B);
         int* counts = c.take<int>((size_t)mh_counts_needed(kMaxSeg));
         if (!c.ok()) return (int)DW_ERR_WORKSPACE;
         auto fwd_call = [&](const float* rr, float* out) {
-            return forward_all<Act>(a, precision, params, prepared, rr, B, R, Z, out, nullptr, nullptr, nullptr, false,
+            return forward_any<Act>(a, precision, params, prepared, rr, B, R, Z, out, nullptr, nullptr, nullptr, false,
                                     ws, fwd, s, seg, nseg);
         };
         int64_t launches = 0;
@@ -605,7 +641,7 @@ int dw_log_psi_sqr_packed(const DwArch* a, int precision, const float* params, c
     cudaStream_t s = (cudaStream_t)stream;
     return with_act(precision, true, [&](auto tag) {
         using Act = act_of<decltype(tag)>;
-        return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s,
+        return forward_any<Act>(a, precision, params, prepared, r, B, R, Z, lp, phase, nullptr, nullptr, false, ws, wsb, s,
                                 seg, nseg);
     });
 }
@@ -620,7 +656,7 @@ int dw_local_energy_packed(const DwArch* a, int precision, const float* params, 
     cudaStream_t s = (cudaStream_t)stream;
     return with_act(precision, true, [&](auto tag) {
         using Act = act_of<decltype(tag)>;
-        size_t pb = plan_bytes<Act>(a, B, true);
+        size_t pb = plan_bytes_any<Act>(a, B, true);
         float* lpo = lp;
         size_t fwd_bytes = wsb;
         if (!lpo) {
@@ -628,7 +664,7 @@ int dw_local_energy_packed(const DwArch* a, int precision, const float* params, 
             lpo = reinterpret_cast<float*>(static_cast<char*>(ws) + pb);
             fwd_bytes = pb;
         }
-        return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, fwd_bytes, s,
+        return forward_any<Act>(a, precision, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, fwd_bytes, s,
                                 seg, nseg);
     });
 }
@@ -639,6 +675,7 @@ int dw_log_psi_sqr_backward(const DwArch* a, int precision, const float* params,
     reset_launch_count();
     DW_CHECK(check_arch(a));
     if (!params || !prepared || !r || !R || !Z || !coeff || !grad || B <= 0) return DW_ERR_ARG;
+    if (precision == DW_PRECISION_FP64) return DW_ERR_UNSUPPORTED;   // the backward runs in FP32
     if (precision < DW_PRECISION_FP32 || precision > DW_PRECISION_BF16) return DW_ERR_ARG;
     Prepared pre = carve_prepared(a, precision, const_cast<void*>(prepared));
     const float* m4[4] = {pre.main[0], pre.main[1], pre.main[2], pre.main[3]};

@@ -1074,6 +1074,33 @@ __device__ double coulomb_walker(const float* rb, int n, const float* R, const i
     return warp_sum(e);
 }
 
+// The same sums with every difference, distance and quotient in FP64 (FP64 form).
+__device__ double coulomb_walker64(const float* rb, int n, const float* R, const int32_t* Z, int N, int lane) {
+    double e = 0.0;
+    for (int p = lane; p < n * n; p += 32) {
+        int i = p / n, j = p % n;
+        if (j <= i) continue;
+        const double dx = (double)rb[j * 3] - rb[i * 3], dy = (double)rb[j * 3 + 1] - rb[i * 3 + 1],
+                     dz = (double)rb[j * 3 + 2] - rb[i * 3 + 2];
+        e += 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    for (int p = lane; p < n * N; p += 32) {
+        int i = p / N, I = p % N;
+        if (Z[I] <= 0) continue;
+        const double dx = (double)rb[i * 3] - R[I * 3], dy = (double)rb[i * 3 + 1] - R[I * 3 + 1],
+                     dz = (double)rb[i * 3 + 2] - R[I * 3 + 2];
+        e -= (double)Z[I] / sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    for (int p = lane; p < N * N; p += 32) {
+        int I = p / N, J = p % N;
+        if (J <= I || Z[I] <= 0 || Z[J] <= 0) continue;
+        const double dx = (double)R[J * 3] - R[I * 3], dy = (double)R[J * 3 + 1] - R[I * 3 + 1],
+                     dz = (double)R[J * 3 + 2] - R[I * 3 + 2];
+        e += (double)(Z[I] * Z[J]) / sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    return warp_sum(e);
+}
+
 __global__ void k_coulomb(const float* __restrict__ r, int B, int n, const float* __restrict__ R,
                           const int32_t* __restrict__ Z, int N, float* __restrict__ E) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -1095,9 +1122,10 @@ __global__ void k_combine(const double* __restrict__ logdet, const double* __res
                           const double* __restrict__ g, const double* __restrict__ lapdet,
                           const double* __restrict__ jas, const float* __restrict__ r, const float* __restrict__ R,
                           const int32_t* __restrict__ Z, Dims d, int B, float* __restrict__ log_psi_sqr,
-                          float* __restrict__ phase, float* __restrict__ E_loc, float* __restrict__ grad_out) {
+                          float* __restrict__ phase, float* __restrict__ E_loc, float* __restrict__ grad_out,
+                          int coul64, const int* __restrict__ nvalid) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= B) return;
+    if (warp >= B || (nvalid && warp >= *nvalid)) return;
     const int b = warp, K = d.K, n3 = 3 * d.n;
     const double* ld = logdet + (int64_t)b * K;
     const double* sg = sign + (int64_t)b * K;
@@ -1152,15 +1180,19 @@ __global__ void k_combine(const double* __restrict__ logdet, const double* __res
     double lap = 2.0 * lapf + jb[d.lap];
     double ekin = -0.5 * (0.5 * lap + 0.25 * grad_sq);
     const int gs_ = seg_of(d, b);
-    double epot = coulomb_walker(r + (int64_t)b * d.n * 3, d.n, R + (size_t)gs_ * d.N * 3, Z + (size_t)gs_ * d.N, d.N, lane);
+    const float* rb = r + (int64_t)b * d.n * 3;
+    const float* Rg = R + (size_t)gs_ * d.N * 3;
+    const int32_t* Zg = Z + (size_t)gs_ * d.N;
+    double epot = coul64 ? coulomb_walker64(rb, d.n, Rg, Zg, d.N, lane) : coulomb_walker(rb, d.n, Rg, Zg, d.N, lane);
     if (lane == 0) E_loc[b] = (float)(ekin + epot);
 }
 
 void launch_combine(const double* logdet, const double* sign, const double* g, const double* lapdet, const double* jas,
                     const float* r, const float* R, const int32_t* Z, const Dims& d, int B,
-                    float* log_psi_sqr, float* phase, float* E_loc, float* grad_out, cudaStream_t s) {
+                    float* log_psi_sqr, float* phase, float* E_loc, float* grad_out, cudaStream_t s, int coul64,
+                    const int* nvalid) {
     k_combine<<<(B * 32 + 255) / 256, 256, 0, s>>>(logdet, sign, g, lapdet, jas, r, R, Z, d, B, log_psi_sqr, phase,
-                                                   E_loc, grad_out);
+                                                   E_loc, grad_out, coul64, nvalid);
     count_launch();
 }
 

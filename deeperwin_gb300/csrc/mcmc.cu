@@ -1,6 +1,7 @@
 // Metropolis-Hastings accept/propose kernel and FP64 cross-walker reductions.
 #include "net.cuh"
 #include "mcmc.cuh"
+#include <cooperative_groups.h>
 
 namespace dw {
 
@@ -143,30 +144,77 @@ __device__ Welford block_welford(Welford w) {
     return r;
 }
 
-// Single-block FP64 mean / variance / finite count of (optionally clipped) energies.
-__global__ void k_stats(const float* __restrict__ E, int n, int clip, double center, double width, double clip_by,
-                        float* __restrict__ E_clip, double* __restrict__ out) {
-    Welford w{0, 0, 0};
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+// FP64 mean / variance of (optionally clipped) energies with the reference's nanmean semantics
+// (loss_function.py:94-99): only NaN entries are dropped; an infinite entry makes the mean that
+// infinity and the variance infinite (NaN when both signs occur, or when no finite entry is left).
+// One thread-block cluster of kStatsBlocks CTAs on as many SMs (the FP64 tanh of the clipping and
+// the merges run on 8 SMs' FP64 pipes instead of one): each thread keeps counts and sums shifted by
+// its first finite value, blocks merge their threads by Welford, and block 0 merges the blocks'
+// partials through distributed shared memory in rank order, so the result is deterministic and no
+// global scratch is needed.
+constexpr int kStatsBlocks = 8, kStatsThreads = 512;
+struct StatPart { double n, mean, m2, npos, nneg, nnum; };
+
+__global__ void __cluster_dims__(kStatsBlocks, 1, 1) __launch_bounds__(kStatsThreads)
+k_stats(const float* __restrict__ E, int n, int clip, double center, double width, double clip_by,
+        float* __restrict__ E_clip, double* __restrict__ out) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int stride = kStatsBlocks * kStatsThreads;
+    double c0 = 0.0, s1 = 0.0, s2 = 0.0, cnt = 0.0, npos = 0.0, nneg = 0.0;
+    bool have = false;
+    for (int i = rank * kStatsThreads + threadIdx.x; i < n; i += stride) {
         double x = E[i];
         if (clip) {
             x = center + tanh((x - center) / width) * width;   // loss_function.py:49-51
             E_clip[i] = (float)x;
         }
-        if (isfinite(x)) w = wmerge(w, Welford{1.0, x, 0.0});
+        if (isnan(x)) continue;
+        if (isinf(x)) { if (x > 0) npos += 1.0; else nneg += 1.0; continue; }
+        if (!have) { c0 = x; have = true; }
+        const double dd = x - c0;
+        s1 += dd; s2 = fma(dd, dd, s2); cnt += 1.0;
     }
+    Welford w{cnt, cnt > 0 ? c0 + s1 / cnt : 0.0, cnt > 0 ? fmax(s2 - s1 * s1 / cnt, 0.0) : 0.0};
     Welford r = block_welford(w);
-    if (threadIdx.x == 0) {
-        double var = r.n > 0 ? r.m2 / r.n : NAN;
-        out[0] = r.n > 0 ? r.mean : NAN;
-        out[1] = var;
-        out[2] = r.n;
-        if (clip) { out[2] = r.mean; out[3] = sqrt(var) * clip_by; }
+    for (int o = 16; o > 0; o >>= 1) {
+        npos += __shfl_xor_sync(0xffffffffu, npos, o);
+        nneg += __shfl_xor_sync(0xffffffffu, nneg, o);
     }
+    __shared__ double inf_sh[2][kStatsThreads / 32];
+    __shared__ StatPart part;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { inf_sh[0][wid] = npos; inf_sh[1][wid] = nneg; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double p = 0.0, q = 0.0;
+        for (int k = 0; k < kStatsThreads / 32; ++k) { p += inf_sh[0][k]; q += inf_sh[1][k]; }
+        part = StatPart{r.n, r.mean, r.m2, p, q, 0.0};
+    }
+    cl.sync();
+    if (rank == 0 && threadIdx.x == 0) {
+        Welford t{0, 0, 0};
+        double p = 0.0, q = 0.0;
+        for (int b = 0; b < kStatsBlocks; ++b) {
+            const StatPart* o = cl.map_shared_rank(&part, b);
+            t = wmerge(t, Welford{o->n, o->mean, o->m2});
+            p += o->npos; q += o->nneg;
+        }
+        double mean = t.n > 0 ? t.mean : NAN, var = t.n > 0 ? t.m2 / t.n : NAN;
+        if (p > 0 && q > 0) { mean = NAN; var = NAN; }
+        else if (p > 0) { mean = INFINITY; var = t.n > 0 ? INFINITY : NAN; }
+        else if (q > 0) { mean = -INFINITY; var = t.n > 0 ? INFINITY : NAN; }
+        out[0] = mean;
+        out[1] = var;
+        out[2] = t.n + p + q;                  // entries that are not NaN
+        if (clip) { out[2] = mean; out[3] = sqrt(var) * clip_by; }
+    }
+    cl.sync();                                 // keep every block's partial alive until block 0 has read it
 }
 
 void launch_stats(const float* E, int n, int clip, double c, double w, double cb, float* Ec, double* out, cudaStream_t s) {
-    k_stats<<<1, 1024, 0, s>>>(E, n, clip, c, w, cb, Ec, out);
+    k_stats<<<kStatsBlocks, kStatsThreads, 0, s>>>(E, n, clip, c, w, cb, Ec, out);
     count_launch();
 }
 

@@ -119,15 +119,27 @@ void launch_det_tangents(const float* MO, const float* Ainv, const double* sign,
                          double* g, double* lapdet, cudaStream_t s);
 void launch_combine(const double* logdet, const double* sign, const double* g, const double* lapdet, const double* jas,
                     const float* r, const float* R, const int32_t* Z, const Dims& d, int B,
-                    float* log_psi_sqr, float* phase, float* E_loc, float* grad_out, cudaStream_t s);
+                    float* log_psi_sqr, float* phase, float* E_loc, float* grad_out, cudaStream_t s,
+                    int coul64 = 0, const int* nvalid = nullptr);
 void launch_coulomb(const float* r, int B, int n, const float* R, const int32_t* Z, int N, float* E, cudaStream_t s);
 // FP64 Gauss-Jordan log|det| and inverse of the value-channel Slater matrices (any Dims mode).
 void launch_slogdet_inv(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, cudaStream_t s);
 
-// api.cu: value-only forward on caller-provided scratch
-size_t value_forward_bytes(const DwArch* a, int precision, int B);
+// api.cu: value-only forward on caller-provided scratch, walker chunks sized against `budget` bytes
+size_t value_forward_bytes(const DwArch* a, int precision, int B, size_t budget);
 int value_forward(const DwArch* a, int precision, const float* params, const void* prepared, const float* r, int B,
-                  const float* R, const int32_t* Z, float* lp, float* phase, void* ws, size_t wsb, cudaStream_t s);
+                  const float* R, const int32_t* Z, float* lp, float* phase, void* ws, size_t wsb, size_t budget,
+                  cudaStream_t s);
+
+// api.cu: the FP32 row-gathered layer weights (Wmain, Wmean per iteration) of a prepared buffer
+void prepared_fp32_layers(const DwArch* a, const void* prepared, const float* main[4], const float* mean[4]);
+
+// fp64.cu: FP64 form (DW_PRECISION_FP64). nvalid (device int, may be null): walkers at or beyond
+// *nvalid are skipped; it requires the walkers to fit one chunk.
+size_t fp64_plan_bytes(const DwArch* a, int B, bool tang);
+int fp64_forward_all(const DwArch* a, const float* P, const void* prepared, const float* r, int B, const float* R,
+                     const int32_t* Z, float* lp, float* phase, float* E, float* grad, bool tang, void* ws,
+                     size_t ws_bytes, cudaStream_t s, const int32_t* seg, int nseg, const int* nvalid);
 
 // backward.cu
 size_t bwd_bytes(const DwArch* a, int B, int* chunk);

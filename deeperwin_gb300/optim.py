@@ -40,9 +40,9 @@ class InverseLRSchedule:
 @dataclasses.dataclass
 class ExponentialLRSchedule:
     """lr(t) = base exp(-(t + offset_time) / decay_time), at least `minimum`, linear warmup
-    (opt_utils.py:51-60)."""
+    (opt_utils.py:51-60); defaults of ExponentialLRSchedule (configuration.py:1065-1070)."""
 
-    decay_time: float = 6000.0
+    decay_time: float = 10000.0
     offset_time: float = 0.0
     warmup: int = 0
     minimum: float = 0.0

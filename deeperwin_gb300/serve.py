@@ -21,7 +21,7 @@ Design:
 * Admission is by an HBM budget: a request reserves its state plus the workspace of its walkers
   evaluated alone (an upper bound of its share of any packed launch) and is admitted when the sum
   of the active reservations stays within the budget (and a slot is free).
-* Every n_el group has a fixed CUDA stream and its own workspace; groups run concurrently.
+* Every (n_el, n_up) group has a fixed CUDA stream and its own workspace; groups run concurrently.
   Requests join their group's pack at the next scheduling quantum (``quantum`` MH steps), so
   arrivals are admitted while earlier requests are on the GPU. The host issues work
   asynchronously and learns about completions from CUDA events.
@@ -220,7 +220,7 @@ class ServingEngine:
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max(1, n_streams))]
         self.ws: List[Optional[torch.Tensor]] = [None] * len(self.streams)
         self.inflight: List[Deque[torch.cuda.Event]] = [collections.deque() for _ in self.streams]
-        self.groups: Dict[int, _Group] = {}
+        self.groups: Dict[Tuple[int, int], _Group] = {}     # keyed by (n_el, n_up)
         self.pending: Deque[Tuple[Request, float]] = collections.deque()    # (request, host arrival time)
         self.finishing: List[Tuple[torch.cuda.Event, List[_State], torch.Tensor, torch.Tensor]] = []
         self.results: Dict[int, Result] = {}
@@ -308,12 +308,13 @@ class ServingEngine:
             self.n_active += 1
 
     def _group(self, n_el: int, n_up: int) -> _Group:
-        g = self.groups.get(n_el)
+        # packed launches share one architecture, so a group holds one (n_el, n_up) spin state
+        g = self.groups.get((n_el, n_up))
         if g is None:
             si = len(self.groups) % len(self.streams)
             g = _Group(n_el, n_up, self.streams[si])
             g.si = si
-            self.groups[n_el] = g
+            self.groups[(n_el, n_up)] = g
         return g
 
     # ------------------------------------------------------------------ packed launches

@@ -59,7 +59,12 @@ enum DwPrecision {
     DW_PRECISION_FP32 = 0,  /* plain form: FP32 end to end (CUDA-core GEMMs, FP32 LU) */
     DW_PRECISION_MIXED = 1, /* tensor-core GEMMs on split-BF16 operands (hi + lo, three BF16 MMAs per
                                K step, FP32 accumulate) + FP64 LU / trace / reductions */
-    DW_PRECISION_BF16 = 2   /* single-pass BF16 tensor-core GEMMs + FP64 LU (fastest, least accurate) */
+    DW_PRECISION_BF16 = 2,  /* single-pass BF16 tensor-core GEMMs + FP64 LU (fastest, least accurate) */
+    DW_PRECISION_FP64 = 3   /* FP64 end to end: every GEMM, activation, envelope, LU, inverse, determinant
+                               tangent, Coulomb sum and reduction in double (the reference's
+                               float_precision: float64 mode, configuration.py:1893 and
+                               process_molecule.py:20-29); outputs are rounded to float32. Forward,
+                               local energy and MCMC only (no parameter gradient) */
 };
 
 /* Human-readable text for a status code (static storage). */
@@ -175,7 +180,10 @@ int dw_mcmc_steps_packed(const DwArch* arch, int precision, const float* params,
                          const DwMcmcConfig* cfg, void* workspace, size_t workspace_bytes, void* stream);
 
 /* FP64 cross-walker statistics of a float32 vector: out[0]=mean, out[1]=variance
- * (population), out[2]=count of finite entries. NaNs are skipped (nanmean, loss_function.py:94-95). */
+ * (population), out[2]=count of entries that are not NaN. Only NaNs are skipped, as jnp.nanmean
+ * does (loss_function.py:94-95): an infinite entry makes the mean that infinity and the variance
+ * infinite (NaN if both signs occur or no finite entry is left). Deterministic (fixed reduction
+ * order). */
 int dw_energy_stats(const float* E, int n, double* out_dev, void* stream);
 
 /* tanh clipping of local energies around (center, width) and the clipped statistics
@@ -196,12 +204,14 @@ int dw_log_psi_sqr_backward(const DwArch* arch, int precision, const float* para
  * allocation anywhere: scratch comes from a fixed static device array of
  * dw_noalloc_scratch_bytes() bytes (64 MiB) that every GPU loading the library reserves until
  * process exit. For callers that cannot allocate device memory at call time (a host framework
- * owning all device memory through its own pool, or a fixed-budget embedding). Calls that need
- * more scratch than the array (too many walkers for the architecture) return
- * DW_ERR_WORKSPACE. The first call on a device resolves the array's device address with
- * cudaGetSymbolAddress; make that first call before any stream capture. All calls share the
- * array and its contents persist between calls, so calls that overlap on the GPU (different
- * streams, or concurrent host threads) race; serialize them. No counterpart in the reference. */
+ * owning all device memory through its own pool, or a fixed-budget embedding). The walkers run
+ * in chunks sized to fit the array, so any walker count is accepted; an architecture whose
+ * single-walker scratch exceeded the array would return DW_ERR_WORKSPACE. FP32, mixed and BF16
+ * forms only (DW_PRECISION_FP64: DW_ERR_ARG). The first call on a device resolves the array's
+ * device address with cudaGetSymbolAddress (again after a cudaDeviceReset of that device); make
+ * that first call before any stream capture. All calls share the array and its contents persist
+ * between calls, so calls that overlap on the GPU (different streams, or concurrent host
+ * threads) race; serialize them. No counterpart in the reference. */
 int dw_log_psi_sqr_noalloc(const DwArch* arch, int precision, const float* params, const void* prepared,
                            const float* r, int n_walkers, const float* R, const int32_t* Z,
                            float* log_psi_sqr, float* phase, void* stream);

@@ -218,6 +218,43 @@ def local_energy(p, arch, r, R, Z):
     return e_kin + potential_energy(r, R, Z), lp, g, lap
 
 
+# --------------------------------------------------------------------------- batched, any dtype
+def log_psi_sqr_raw(p, arch, r, R, Z):
+    """``Wavefunction.__call__`` on tensors used as given (no float64 cast): the restatement in the
+    dtype of ``p`` and ``r`` (float32 for the reference's default precision, configuration.py:1893)."""
+    h_el, dist_ei = embedding(p, arch, r, R, Z)
+    mo = orbitals(p, arch, h_el, dist_ei)
+    phase, lp = sum_of_determinants(mo)
+    return phase, lp + jastrow(p, arch, h_el)
+
+
+def local_energy_batched(p, arch, r, R, Z):
+    """E_L of a batch of walkers in the dtype of ``p`` / ``r``: gradient and exact Laplacian of
+    log psi^2 by torch.func (Hessian diagonal of each walker, vmapped over the batch, like the
+    reference's batched_vmap over get_local_energy, hamiltonian.py:272-291), Coulomb energy in the
+    same dtype (hamiltonian.py:17-39)."""
+    B, n, _ = r.shape
+
+    def f(x):
+        return log_psi_sqr_raw(p, arch, x.reshape(1, n, 3), R, Z)[1][0]
+
+    x = r.reshape(B, 3 * n)
+    g = torch.func.vmap(torch.func.grad(f))(x)
+    H = torch.func.vmap(torch.func.jacfwd(torch.func.grad(f)))(x)
+    lap = torch.diagonal(H, dim1=-2, dim2=-1).sum(-1)
+    e_kin = -0.5 * (0.5 * lap + 0.25 * (g ** 2).sum(-1))
+    Zt = torch.as_tensor(np.asarray(Z), dtype=r.dtype)
+    d_ei = torch.linalg.norm(r[:, :, None, :] - R[None, None, :, :], dim=-1)
+    e_ei = -(Zt / d_ei).sum(dim=(-2, -1))
+    eye = torch.eye(n, dtype=r.dtype)
+    d_ee = torch.linalg.norm(r[:, :, None, :] - r[:, None, :, :], dim=-1)
+    e_ee = torch.triu(1.0 / (d_ee + eye), diagonal=1).sum(dim=(-2, -1))
+    N = R.shape[0]
+    d_ii = torch.linalg.norm(R[:, None, :] - R[None, :, :], dim=-1)
+    e_ii = torch.triu((Zt[:, None] * Zt[None, :]) / (d_ii + torch.eye(N, dtype=r.dtype)), diagonal=1).sum()
+    return e_kin + e_ee + e_ei + e_ii
+
+
 # --------------------------------------------------------------------------- MCMC
 def mh_step(p, arch, R, Z, r, lp, age, stepsize, noise, uniform, max_age):
     """One Metropolis-Hastings step with injected randomness

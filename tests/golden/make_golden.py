@@ -9,7 +9,7 @@ executed), and runs them in float64 on seeded weights and walkers.
 
 Run from the repository root with the reference checked out:
 
-    python tests/golden/make_golden.py /path/to/deeperwin
+    python tests/golden/make_golden.py /path/to/deeperwin [case ...]
 
 It writes ``tests/golden/*.npz``. The fixtures hold the walkers, nuclei, the seed and
 init settings of the weights (weights are regenerated by
@@ -297,18 +297,23 @@ def reference_forward(g: dict, arch: A.Arch, params: dict, r, R, Z, requested: d
 
 
 CASES = [
-    # name, molecule, n_dets, n_walkers, bias_std, envelope_jitter
-    ("lih_k8", A.lih, 8, 8, 0.1, 0.2),
-    ("h6_k4", lambda: A.h_chain(6), 4, 4, 0.1, 0.2),
-    ("c2h4_k2", A.c2h4_shaped, 2, 3, 0.1, 0.2),
-    ("h10_k16_plain_init", A.h_chain, 16, 3, 0.0, 0.0),
+    # name, molecule, n_dets, n_walkers, bias_std, envelope_jitter, walkers whose Slater matrices are kept
+    ("lih_k8", A.lih, 8, 8, 0.1, 0.2, None),
+    ("h6_k4", lambda: A.h_chain(6), 4, 4, 0.1, 0.2, None),
+    ("c2h4_k2", A.c2h4_shaped, 2, 3, 0.1, 0.2, None),
+    ("h10_k16_plain_init", A.h_chain, 16, 3, 0.0, 0.0, None),
+    # the contract shapes: C2H4-shaped with 32 determinants, the 40-electron molecule with 64
+    ("c2h4_k32", A.c2h4_shaped, 32, 16, 0.1, 0.2, 2),
+    ("scale40_k64", A.scale_molecule, 64, 4, 0.1, 0.2, 0),
 ]
 
 
-def main(ref_root: str, paths_only: bool = False):
+def main(ref_root: str, paths_only: bool = False, only=None):
     g = load_reference(Path(ref_root))
     out_dir = Path(__file__).resolve().parent
-    for name, mol_fn, K, B, bstd, jit in CASES:
+    for name, mol_fn, K, B, bstd, jit, n_slater in CASES:
+        if only and name not in only:
+            continue
         mol = mol_fn()
         arch = A.arch_for(mol, K)
         params = P.init_params(arch, seed=0, bias_std=bstd, envelope_jitter=jit)
@@ -338,12 +343,14 @@ def main(ref_root: str, paths_only: bool = False):
             packed_abs_sum=np.float64(np.abs(packed.astype(np.float64)).sum()),
             R=np.asarray(mol.R, np.float64), Z=np.asarray(mol.Z, np.int64), r=r,
             log_psi_sqr=np.asarray(lp, np.float64), phase=np.asarray(phase, np.float64),
-            slater=np.asarray(mo, np.float64), e_pot=np.asarray(e_pot, np.float64),
+            slater=np.asarray(mo, np.float64)[:n_slater], e_pot=np.asarray(e_pot, np.float64),
             clip_E=E, clip_in=np.array([-7.5, 3.0]), clip_out=np.asarray(clipped, np.float64),
             clip_state_out=np.array([c_new, w_new], np.float64))
         print(f"{name}: log_psi_sqr={np.asarray(lp)[:3]} e_pot={np.asarray(e_pot)[:3]}")
 
 
 if __name__ == "__main__":
-    args = [a for a in sys.argv[1:] if a != "--paths-only"]
-    main(args[0] if args else "/root/reference", paths_only="--paths-only" in sys.argv)
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if not args:
+        sys.exit("usage: make_golden.py <path of the reference checkout> [case ...] [--paths-only]")
+    main(args[0], paths_only="--paths-only" in sys.argv, only=set(args[1:]) or None)

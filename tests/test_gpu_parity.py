@@ -237,14 +237,46 @@ def test_potential_energy(cuda):
 
 
 def test_energy_stats(cuda):
-    x = torch.randn(10007, device="cuda") * 3 + 1
-    x[5] = float("nan")
-    out = api.energy_stats(x).cpu().numpy()
-    xn = x.cpu().double().numpy()
-    xn = xn[np.isfinite(xn)]
-    assert out[0] == pytest.approx(xn.mean(), rel=1e-12)
-    assert out[1] == pytest.approx(xn.var(), rel=1e-12)
-    assert out[2] == len(xn)
+    for n in (1, 31, 4096, 10007, 300001):
+        x = torch.randn(n, device="cuda") * 3 - 78
+        if n > 5:
+            x[5] = float("nan")
+        out = api.energy_stats(x).cpu().numpy()
+        xn = x.cpu().double().numpy()
+        xn = xn[~np.isnan(xn)]
+        assert out[0] == pytest.approx(xn.mean(), rel=1e-12)
+        assert out[1] == pytest.approx(xn.var(), rel=1e-10, abs=1e-12)
+        assert out[2] == len(xn)
+        # deterministic: the same input gives the same bits
+        assert np.array_equal(api.energy_stats(x).cpu().numpy(), out, equal_nan=True)
+
+
+def test_energy_stats_nanmean_semantics(cuda):
+    """Only NaN is dropped (jnp.nanmean, loss_function.py:94-99): one +inf walker makes the
+    mean +inf and the variance inf; +inf and -inf together give NaN; all-NaN gives NaN. Clipping
+    maps infinities to finite values (tanh saturates), so the clipped statistics stay finite."""
+    from deeperwin_gb300 import _lib
+    x = torch.randn(1000, device="cuda") - 40
+    x[3] = float("nan")
+    y = x.clone(); y[7] = float("inf")
+    out = api.energy_stats(y).cpu().numpy()
+    assert out[0] == np.inf and out[1] == np.inf and out[2] == 999
+    z = y.clone(); z[9] = -float("inf")
+    out = api.energy_stats(z).cpu().numpy()
+    assert np.isnan(out[0]) and np.isnan(out[1]) and out[2] == 999
+    out = api.energy_stats(torch.full((64,), float("nan"), device="cuda")).cpu().numpy()
+    assert np.isnan(out[0]) and np.isnan(out[1]) and out[2] == 0
+    Ec = torch.empty_like(y)
+    st = torch.empty(4, dtype=torch.float64, device="cuda")
+    _lib.check(_lib.lib().dw_clip_energies(api._ptr(y), 1000, -40.0, 5.0, 5.0, api._ptr(Ec), api._ptr(st),
+                                           api._stream()), "dw_clip_energies")
+    yc = y.cpu().double().numpy()
+    ref = -40.0 + np.tanh((yc + 40.0) / 5.0) * 5.0
+    np.testing.assert_allclose(Ec.cpu().numpy(), ref, rtol=1e-6, atol=1e-5)
+    r = ref[~np.isnan(ref)]
+    s = st.cpu().numpy()
+    assert np.isfinite(s).all()
+    assert s[2] == pytest.approx(r.mean(), rel=1e-12) and s[3] == pytest.approx(r.std() * 5.0, rel=1e-10)
 
 
 def _big_case(name):

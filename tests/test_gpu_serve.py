@@ -210,3 +210,32 @@ def test_opt_step_request_gradient(weights):
     torch.testing.assert_close(res.grad, g, rtol=1e-3, atol=1e-4 * g.abs().max().item())
     torch.testing.assert_close(res.new_params, prm.flat - 1e-2 * res.grad)
     assert res.loss == pytest.approx(float(Ec.mean()), rel=1e-6)
+
+
+def test_equal_electron_count_different_spin_states(weights):
+    """Requests with the same n_el but different n_up run in separate groups: each result equals
+    the request alone, and equals one_at_a_time's evaluation of its own spin state."""
+    h6 = _mols6()[0]
+    h6_open = Molecule(R=h6.R, Z=h6.Z, n_el=6, n_up=4, name="H6_triplet")
+    reqs = [serve.Request(0, h6, 48, n_steps=3, seed=7, keep_walkers=True),
+            serve.Request(1, h6_open, 40, n_steps=3, seed=9, keep_walkers=True)]
+    alone = {}
+    for q in reqs:
+        eng = serve.ServingEngine(weights, quantum=2, n_streams=1)
+        eng.submit(q)
+        eng.drain()
+        alone[q.rid] = eng.results[q.rid]
+    eng = serve.ServingEngine(weights, quantum=2, n_streams=1)
+    for q in reqs:
+        eng.submit(q)
+    eng.drain()
+    torch.cuda.synchronize()
+    assert sorted(eng.groups) == [(6, 3), (6, 4)]
+    for q in reqs:
+        a, b = alone[q.rid], eng.results[q.rid]
+        assert torch.equal(a.r, b.r) and torch.equal(a.E_loc, b.E_loc), q.rid
+    # the open-shell result is that of its own (n_up = 4) model
+    prm = weights.params(6, 4)
+    Rp, Zp = serve.padded_geometry(h6_open)
+    E = api.local_energy(prm, (4, 2), eng.results[1].r, Rp, Zp)
+    torch.testing.assert_close(E, eng.results[1].E_loc, rtol=1e-5, atol=1e-5)

@@ -30,8 +30,10 @@ def test_golden_forward(f):
     ph, lp = O.log_psi_sqr(tp, a, d["r"], d["R"], d["Z"])
     np.testing.assert_allclose(lp.numpy(), d["log_psi_sqr"], rtol=1e-11, atol=1e-10)
     np.testing.assert_array_equal(ph.numpy(), d["phase"])
-    mo = O.slater_matrices(tp, a, d["r"], d["R"], d["Z"])
-    np.testing.assert_allclose(mo.numpy(), d["slater"], rtol=1e-11, atol=1e-13)
+    ns = d["slater"].shape[0]           # the fixtures of the larger shapes keep the first walkers' matrices
+    if ns:
+        mo = O.slater_matrices(tp, a, d["r"][:ns], d["R"], d["Z"])
+        np.testing.assert_allclose(mo.numpy(), d["slater"], rtol=1e-11, atol=1e-13)
 
 
 @pytest.mark.parametrize("f", GOLDEN, ids=lambda f: f.split("/")[-1])

@@ -30,7 +30,12 @@ class DwMcmcConfig(ctypes.Structure):
     _fields_ = [("n_steps", ctypes.c_int32), ("max_age", ctypes.c_int32),
                 ("stepsize_update_interval", ctypes.c_int32), ("target_acceptance_rate", ctypes.c_float),
                 ("min_stepsize", ctypes.c_float), ("max_stepsize", ctypes.c_float), ("seed", ctypes.c_uint64),
-                ("reevaluate", ctypes.c_int32)]
+                ("reevaluate", ctypes.c_int32), ("proposal", ctypes.c_int32), ("r_min", ctypes.c_float),
+                ("r_max", ctypes.c_float), ("langevin_scale", ctypes.c_float), ("p_spin_swap", ctypes.c_float),
+                ("p_spin_flip", ctypes.c_float)]
+
+
+DW_PROPOSAL = {"normal": 0, "cauchy": 1, "langevin": 2, "local": 3, "normal_one_el": 4, "local_one_el": 5}
 
 
 SCALARS_BYTES = ctypes.sizeof(DwMcmcScalars)
@@ -60,6 +65,9 @@ _SIGS = {
                                             ctypes.c_int, _P, _P, _P, _P, _P, _P, ctypes.POINTER(DwMcmcConfig), _P,
                                             ctypes.c_size_t, _P]),
     "dw_energy_stats": (ctypes.c_int, [_P, ctypes.c_int, _P, _P]),
+    "dw_forces_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(DwArch), ctypes.c_int, ctypes.c_int]),
+    "dw_forces": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P, _P, _P,
+                                 ctypes.c_float, ctypes.c_float, ctypes.c_int, _P, _P, _P, ctypes.c_size_t, _P]),
     "dw_clip_energies": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P, _P,
                                         _P]),
     "dw_log_psi_sqr_backward": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P,
@@ -73,6 +81,10 @@ _SIGS = {
     "dw_debug_tc_error_flag": (ctypes.c_int, []),
     "dw_debug_slogdet_small": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                               _P, _P, _P, _P]),
+    "dw_debug_local_energy_scales": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P,
+                                                    _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
+    "dw_guard_stats": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                      ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
     "dw_timer_enable": (ctypes.c_int, [ctypes.c_int]),
     "dw_timer_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
                                      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),

@@ -158,6 +158,27 @@ def potential_energy(r, R, Z) -> torch.Tensor:
     return E
 
 
+def calculate_forces(params: Params, r, R, Z, log_psi_sqr: torch.Tensor, R_cut: float = 0.1, R_core: float = 0.5,
+                     use_antithetic_sampling: bool = False, per_walker: bool = False):
+    """Forces on the nuclei, [n_ions, 3] FP64 (hamiltonian.py:309-338; ForceEvaluationConfig defaults,
+    configuration.py:1225-1229). With per_walker, also the per-walker forces [B, n_ions, 3]."""
+    a = params.arch
+    dev = params.flat.device
+    r = _as_walkers(r, dev)
+    B = r.shape[0]
+    Rt, Zt = (R, Z) if torch.is_tensor(R) and R.is_cuda else _geometry(R, Z, dev)
+    F = torch.empty(a.n_ions, 3, dtype=torch.float64, device=dev)
+    pw = torch.empty(B, a.n_ions, 3, dtype=torch.float64, device=dev) if per_walker else None
+    L = _lib.lib()
+    nbytes = L.dw_forces_workspace_bytes(ctypes.byref(params.c_arch), params.prec, B)
+    ws = _WS.get("forces", nbytes, dev)
+    _lib.check(L.dw_forces(ctypes.byref(params.c_arch), params.prec, _ptr(params.flat), _ptr(params.prepared), _ptr(r),
+                           B, _ptr(Rt), _ptr(Zt), _ptr(log_psi_sqr.contiguous()), float(R_cut), float(R_core),
+                           1 if use_antithetic_sampling else 0, _ptr(F), _ptr(pw), _ptr(ws), nbytes, _stream()),
+               "dw_forces")
+    return (F, pw) if per_walker else F
+
+
 def build_log_psi_squared(mol: Molecule, n_dets: int, seed: int = 0, precision: str = "mixed",
                           z_min: int = 1, z_max: Optional[int] = None, device="cuda", **init_kw):
     """Seeded model for a molecule; returns (log_psi_sqr, params) like the reference's builder."""
@@ -181,7 +202,11 @@ def build_local_energy(log_psi_squared=None, is_complex=False, is_periodic=False
 # ---------------------------------------------------------------------------- MCMC
 @dataclasses.dataclass
 class MCMCConfig:
-    """Defaults of MCMCConfigOptimization (configuration.py:1030-1034) with the normal proposal."""
+    """Defaults of MCMCConfigOptimization (configuration.py:1030-1034). ``proposal`` names the
+    proposal rule (configuration.py:952-975, mcmc.py:328-342): "normal", "cauchy",
+    "normal_one_el", "local", "local_one_el" or "langevin"; r_min / r_max default to the rule's
+    config (local: 0.1 / 1.0, Langevin: 0.2 / 2.0); spin swaps and flips as p_spin_swap /
+    p_spin_flip (configuration.py:1024-1028)."""
 
     n_inter_steps: int = 20
     n_burn_in: int = 1000
@@ -191,6 +216,23 @@ class MCMCConfig:
     target_acceptance_rate: float = 0.5
     min_stepsize_scale: float = 1e-2
     max_stepsize_scale: float = 1.0
+    proposal: str = "normal"
+    r_min: Optional[float] = None
+    r_max: Optional[float] = None
+    langevin_scale: float = 1.0
+    p_spin_swap: float = 0.0
+    p_spin_flip: float = 0.0
+
+    def c_config(self, n_steps: int, seed: int, reevaluate: bool) -> "_lib.DwMcmcConfig":
+        if self.proposal not in _lib.DW_PROPOSAL:
+            raise ValueError(f"unknown MCMC proposal {self.proposal!r}")
+        lo, hi = (0.2, 2.0) if self.proposal == "langevin" else (0.1, 1.0)
+        return _lib.DwMcmcConfig(int(n_steps), int(self.max_age), int(self.stepsize_update_interval),
+                                 float(self.target_acceptance_rate), float(self.min_stepsize_scale),
+                                 float(self.max_stepsize_scale), ctypes.c_uint64(seed).value, 1 if reevaluate else 0,
+                                 _lib.DW_PROPOSAL[self.proposal], float(lo if self.r_min is None else self.r_min),
+                                 float(hi if self.r_max is None else self.r_max), float(self.langevin_scale),
+                                 float(self.p_spin_swap), float(self.p_spin_flip))
 
 
 class MCMCState:
@@ -260,10 +302,7 @@ class MetropolisHastingsMonteCarlo:
         a = params.arch
         if (n_up, n_dn) != (a.n_up, a.n_dn):
             raise ValueError("spin state does not match the model")
-        c = self.config
-        cfg = _lib.DwMcmcConfig(int(n_steps), int(c.max_age), int(c.stepsize_update_interval),
-                                float(c.target_acceptance_rate), float(c.min_stepsize_scale),
-                                float(c.max_stepsize_scale), ctypes.c_uint64(state.seed).value, 1 if reevaluate else 0)
+        cfg = self.config.c_config(n_steps, state.seed, reevaluate)
         B = state.r.shape[0]
         L = _lib.lib()
         nbytes = L.dw_workspace_bytes(ctypes.byref(params.c_arch), params.prec, B, 2)

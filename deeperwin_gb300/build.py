@@ -15,7 +15,7 @@ from pathlib import Path
 CSRC = Path(__file__).resolve().parent / "csrc"
 BUILD = CSRC / "_build"
 LIB = CSRC / "libdwgb.so"
-SOURCES = ["model.cu", "net.cu", "gemm_simt.cu", "gemm_tc.cu", "det.cu", "mcmc.cu", "api.cu", "backward.cu", "noalloc.cu", "fp64.cu"]
+SOURCES = ["model.cu", "net.cu", "gemm_simt.cu", "gemm_tc.cu", "det.cu", "mcmc.cu", "api.cu", "backward.cu", "noalloc.cu", "fp64.cu", "guard.cu", "forces.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -256,7 +256,7 @@ template <class Act> static inline int64_t act_off(int64_t row, int ld) { return
 template <class Act>
 static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, const ParamLayout& L,
                      const Prepared& pre, const float* r, const float* R, const int32_t* Z, const int32_t* seg,
-                     float* lp, float* phase, float* E_loc, float* grad, cudaStream_t s) {
+                     float* lp, float* phase, float* E_loc, float* grad, cudaStream_t s, float* esc = nullptr) {
     Dims d = p.d;
     d.seg = seg;          // walker -> geometry segment of this chunk (null: one geometry)
     const int rows = Bc * d.n * d.Tp;
@@ -367,7 +367,8 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
     }
     launch_jastrow_out<Act>(p.J2, d.J1, P + L.jas_w[2], d, Bc, p.jas, s);
     timer_end("jastrow", s, 0.0, 0.0);
-    DW_TIMED("combine", launch_combine(p.logdet, p.sign, p.g, p.lapdet, p.jas, r, R, Z, d, Bc, lp, phase, E_loc, grad, s));
+    DW_TIMED("combine", launch_combine(p.logdet, p.sign, p.g, p.lapdet, p.jas, r, R, Z, d, Bc, lp, phase, E_loc, grad, s,
+                                       0, nullptr, esc));
     DW_CHECK_CUDA(cudaGetLastError());
     return DW_OK;
 }
@@ -396,6 +397,12 @@ static size_t plan_bytes(const DwArch* a, int B, bool tang, size_t budget = kChu
     return (carve_plan<Act>(d, choose_chunk<Act>(d, std::max(B, 1), budget), nullptr).bytes + 4096 + 255) / 256 * 256;
 }
 
+// Mixed-form local energies: the forward's plan (or the tail re-evaluation, which reuses that
+// region once the forward is done) followed by the per-walker error scales.
+static size_t guarded_bytes(const DwArch* a, int B, size_t plan) {
+    return (std::max(plan, guard_bytes(a, B)) + 255) / 256 * 256 + (size_t)3 * B * sizeof(float) + 256;
+}
+
 // Workspace of one forward (value or tangent) and the forward itself, for every precision form.
 template <class Act>
 static size_t plan_bytes_any(const DwArch* a, int B, bool tang) {
@@ -410,10 +417,12 @@ static size_t ws_bytes_t(const DwArch* a, int n_walkers, int mode) {
         size_t b = plan_bytes_any<Act>(a, n_walkers, false);
         b += (size_t)n_walkers * a->n_el * 3 * sizeof(float) + 256;      // proposals
         b += (size_t)n_walkers * sizeof(float) + 256;                    // proposal log psi^2
+        b += (size_t)n_walkers * sizeof(float) + 256;                    // log proposal ratios
         b += (size_t)mh_counts_needed(kMaxSeg) * sizeof(int) + 256;
         return b;
     }
     size_t b = plan_bytes_any<Act>(a, n_walkers, mode == 1);
+    if (mode == 1 && std::is_same<Act, Split>::value) b = guarded_bytes(a, n_walkers, b);
     if (mode == 1) b += (size_t)n_walkers * sizeof(float) + 256;         // log psi^2 when not requested
     return b;
 }
@@ -422,7 +431,7 @@ template <class Act>
 static int forward_all(const DwArch* a, int precision, const float* P, const void* prepared, const float* r, int B,
                        const float* R, const int32_t* Z, float* lp, float* phase, float* E, float* grad, bool tang,
                        void* ws, size_t ws_bytes, cudaStream_t s, const int32_t* seg = nullptr, int nseg = 1,
-                       size_t budget = kChunkBudget) {
+                       size_t budget = kChunkBudget, float* esc = nullptr) {
     Dims d = make_dims(a, tang);
     if (nseg < 1 || nseg > kMaxSeg || (nseg > 1 && !seg)) return DW_ERR_ARG;
     // the fused forward-Laplacian epilogue keeps one electron's channels inside a 128-row tile
@@ -441,7 +450,7 @@ static int forward_all(const DwArch* a, int precision, const float* P, const voi
         DW_CHECK(run_chunk<Act>(p, nb, precision, P, L, pre, r + (int64_t)b0 * d.n * 3, R, Z, seg ? seg + b0 : nullptr,
                                 lp + b0,
                                 phase ? phase + b0 : nullptr, E ? E + b0 : nullptr,
-                                grad ? grad + (int64_t)b0 * 3 * d.n : nullptr, s));
+                                grad ? grad + (int64_t)b0 * 3 * d.n : nullptr, s, esc ? esc + 3 * (int64_t)b0 : nullptr));
     }
     return DW_OK;
 }
@@ -454,6 +463,39 @@ static int forward_any(const DwArch* a, int precision, const float* P, const voi
         return fp64_forward_all(a, P, prepared, r, B, R, Z, lp, phase, E, grad, tang, ws, ws_bytes, s, seg, nseg, nullptr);
     else
         return forward_any<Act>(a, precision, P, prepared, r, B, R, Z, lp, phase, E, grad, tang, ws, ws_bytes, s, seg, nseg);
+}
+
+// Local energies of one or several geometries. Workspace: [forward plan | log psi^2 when not
+// requested], and for the mixed form [plan or tail re-evaluation | log psi^2 | error scales]: the
+// mixed form's walkers whose predicted E_L error exceeds the tolerance are re-evaluated in FP64
+// (guard.cu).
+static int local_energy_impl(const DwArch* a, int precision, const float* params, const void* prepared, const float* r,
+                             int B, const float* R, const int32_t* Z, const int32_t* seg, int nseg, float* E, float* lp,
+                             float* grad, void* ws, size_t wsb, cudaStream_t s) {
+    return with_act(precision, true, [&](auto tag) {
+        using Act = act_of<decltype(tag)>;
+        const size_t pb = plan_bytes_any<Act>(a, B, true);
+        const bool guarded = std::is_same<Act, Split>::value && precision == DW_PRECISION_MIXED;
+        const size_t region = guarded ? (std::max(pb, guard_bytes(a, B)) + 255) / 256 * 256 : pb;
+        char* tail = static_cast<char*>(ws) + region;
+        float* lpo = lp;
+        if (!lpo) {   // log psi^2 output is optional; it then lives after the plan
+            lpo = reinterpret_cast<float*>(tail);
+            tail += ((size_t)B * sizeof(float) + 255) / 256 * 256;
+        }
+        float* esc = guarded ? reinterpret_cast<float*>(tail) : nullptr;
+        if (guarded) tail += (size_t)3 * B * sizeof(float);
+        if ((size_t)(tail - static_cast<char*>(ws)) > wsb) return (int)DW_ERR_WORKSPACE;
+        if constexpr (std::is_same<Act, double>::value) {
+            return fp64_forward_all(a, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, region, s, seg, nseg,
+                                    nullptr);
+        } else {
+            DW_CHECK(forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, region,
+                                      s, seg, nseg, kChunkBudget, esc));
+            if (!guarded) return (int)DW_OK;
+            return tail_guard(a, params, prepared, r, B, R, Z, seg, nseg, esc, E, lpo, grad, ws, region, s);
+        }
+    });
 }
 
 // FP32 row-gathered layer weights of a prepared buffer (the same offsets in every precision form).
@@ -531,18 +573,7 @@ int dw_local_energy(const DwArch* a, int precision, const float* params, const v
     DW_CHECK(check_arch(a));
     if (!params || !prepared || !r || !R || !Z || !E || B <= 0) return DW_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    return with_act(precision, true, [&](auto tag) {
-        using Act = act_of<decltype(tag)>;
-        size_t pb = plan_bytes_any<Act>(a, B, true);
-        float* lpo = lp;
-        size_t fwd_bytes = wsb;
-        if (!lpo) {   // log psi^2 output is optional; it then lives in the workspace tail
-            if (pb + (size_t)B * sizeof(float) > wsb) return (int)DW_ERR_WORKSPACE;
-            lpo = reinterpret_cast<float*>(static_cast<char*>(ws) + pb);
-            fwd_bytes = pb;
-        }
-        return forward_any<Act>(a, precision, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, fwd_bytes, s);
-    });
+    return local_energy_impl(a, precision, params, prepared, r, B, R, Z, nullptr, 1, E, lp, grad, ws, wsb, s);
 }
 
 int dw_potential_energy(const float* r, int B, int n, const float* R, const int32_t* Z, int N, float* E, void* stream) {
@@ -557,6 +588,15 @@ int dw_potential_energy(const float* r, int B, int n, const float* R, const int3
 
 namespace dw {
 
+// Proposal rule and its parameters within their domains.
+static bool mcmc_config_ok(const DwMcmcConfig* c) {
+    if (c->proposal < DW_PROPOSAL_NORMAL || c->proposal > DW_PROPOSAL_LOCAL_ONE_EL) return false;
+    const bool local = c->proposal == DW_PROPOSAL_LANGEVIN || c->proposal == DW_PROPOSAL_LOCAL ||
+                       c->proposal == DW_PROPOSAL_LOCAL_ONE_EL;
+    if (local && !(c->r_min > 0.f && c->r_max >= c->r_min)) return false;
+    return c->p_spin_swap >= 0.f && c->p_spin_swap <= 1.f && c->p_spin_flip >= 0.f && c->p_spin_flip <= 1.f;
+}
+
 // Metropolis-Hastings chains (mcmc.py:390-396 run_mcmc_steps): optional re-evaluation of log psi^2
 // at the current walkers, then n_steps x (forward at the proposals, accept / propose).
 static int mcmc_impl(const DwArch* a, int precision, const float* params, const void* prepared, float* r, int B,
@@ -570,6 +610,7 @@ static int mcmc_impl(const DwArch* a, int precision, const float* params, const 
         Carver c(static_cast<char*>(ws) + fwd, wsb - fwd);
         float* r_prop = c.take<float>((size_t)B * a->n_el * 3);
         float* lp_prop = c.take<float>((size_t)B);
+        float* lq = c.take<float>((size_t)B);
         int* counts = c.take<int>((size_t)mh_counts_needed(kMaxSeg));
         if (!c.ok()) return (int)DW_ERR_WORKSPACE;
         auto fwd_call = [&](const float* rr, float* out) {
@@ -586,6 +627,13 @@ static int mcmc_impl(const DwArch* a, int precision, const float* params, const 
         m.interval = cfg->stepsize_update_interval; m.target = cfg->target_acceptance_rate;
         m.min_step = cfg->min_stepsize; m.max_step = cfg->max_stepsize; m.seed = cfg->seed;
         m.seg = seg; m.widx = widx; m.seeds = seeds; m.nseg = nseg;
+        m.proposal = cfg->proposal;
+        m.r_min = cfg->r_min; m.r_max = cfg->r_max; m.langevin_scale = cfg->langevin_scale;
+        m.p_swap = cfg->p_spin_swap; m.p_flip = cfg->p_spin_flip;
+        const bool asym = cfg->proposal == DW_PROPOSAL_LANGEVIN || cfg->proposal == DW_PROPOSAL_LOCAL ||
+                          cfg->proposal == DW_PROPOSAL_LOCAL_ONE_EL;
+        m.lq = asym ? lq : nullptr;
+        m.R = R; m.Z = Z; m.N = a->n_ions;
         reset_launch_count();
         DW_TIMED("mh", launch_mh(m, 0, s));
         launches += launch_count();
@@ -612,7 +660,7 @@ int dw_mcmc_steps(const DwArch* a, int precision, const float* params, const voi
     reset_launch_count();
     DW_CHECK(check_arch(a));
     if (!params || !prepared || !r || !R || !Z || !lp || !age || !scalars || !cfg || B <= 0) return DW_ERR_ARG;
-    if (cfg->n_steps < 0) return DW_ERR_ARG;
+    if (cfg->n_steps < 0 || !mcmc_config_ok(cfg)) return DW_ERR_ARG;
     return mcmc_impl(a, precision, params, prepared, r, B, R, Z, 1, nullptr, nullptr, nullptr, lp, age, scalars, cfg,
                      ws, wsb, (cudaStream_t)stream);
 }
@@ -626,7 +674,7 @@ int dw_mcmc_steps_packed(const DwArch* a, int precision, const float* params, co
     if (!params || !prepared || !r || !R || !Z || !seg || !walker_index || !seeds || !lp || !age || !scalars || !cfg ||
         B <= 0)
         return DW_ERR_ARG;
-    if (cfg->n_steps < 0 || nseg < 1 || nseg > kMaxSeg) return DW_ERR_ARG;
+    if (cfg->n_steps < 0 || nseg < 1 || nseg > kMaxSeg || !mcmc_config_ok(cfg)) return DW_ERR_ARG;
     return mcmc_impl(a, precision, params, prepared, r, B, R, Z, nseg, seg, walker_index, seeds, lp, age, scalars, cfg,
                      ws, wsb, (cudaStream_t)stream);
 }
@@ -654,19 +702,7 @@ int dw_local_energy_packed(const DwArch* a, int precision, const float* params, 
     if (!params || !prepared || !r || !R || !Z || !seg || !E || B <= 0 || nseg < 1 || nseg > kMaxSeg)
         return DW_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    return with_act(precision, true, [&](auto tag) {
-        using Act = act_of<decltype(tag)>;
-        size_t pb = plan_bytes_any<Act>(a, B, true);
-        float* lpo = lp;
-        size_t fwd_bytes = wsb;
-        if (!lpo) {
-            if (pb + (size_t)B * sizeof(float) > wsb) return (int)DW_ERR_WORKSPACE;
-            lpo = reinterpret_cast<float*>(static_cast<char*>(ws) + pb);
-            fwd_bytes = pb;
-        }
-        return forward_any<Act>(a, precision, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, fwd_bytes, s,
-                                seg, nseg);
-    });
+    return local_energy_impl(a, precision, params, prepared, r, B, R, Z, seg, nseg, E, lp, grad, ws, wsb, s);
 }
 
 int dw_log_psi_sqr_backward(const DwArch* a, int precision, const float* params, const void* prepared, const float* r,
@@ -690,6 +726,25 @@ int dw_energy_stats(const float* E, int n, double* out, void* stream) {
     launch_stats(E, n, 0, 0.0, 1.0, 1.0, nullptr, out, (cudaStream_t)stream);
     DW_CHECK_CUDA(cudaGetLastError());
     return DW_OK;
+}
+
+// Instrumentation: the local energy of dw_local_energy plus three per-walker error scales
+// (scales[3 b .. 3 b + 2]: the magnitude S of the terms summed into E_L, the magnitude of the
+// determinant terms summed into the Laplacian of log|sum of determinants|, and 1 / (|psi~| + 1e-8)
+// with psi~ the determinant sum relative to its largest term). FP32, mixed and BF16 forms.
+int dw_debug_local_energy_scales(const DwArch* a, int precision, const float* params, const void* prepared,
+                                 const float* r, int B, const float* R, const int32_t* Z, float* E, float* lp,
+                                 float* scales, void* ws, size_t wsb, void* stream) {
+    reset_launch_count();
+    DW_CHECK(check_arch(a));
+    if (!params || !prepared || !r || !R || !Z || !E || !lp || !scales || B <= 0) return DW_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    return with_act(precision, true, [&](auto tag) {
+        using Act = act_of<decltype(tag)>;
+        if constexpr (std::is_same<Act, double>::value) return (int)DW_ERR_ARG;
+        else return forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lp, nullptr, E, nullptr, true, ws, wsb,
+                                     s, nullptr, 1, kChunkBudget, scales);
+    });
 }
 
 int dw_clip_energies(const float* E, int n, double center, double width, double clip_by, float* E_clip, double* out,

@@ -1123,7 +1123,7 @@ __global__ void k_combine(const double* __restrict__ logdet, const double* __res
                           const double* __restrict__ jas, const float* __restrict__ r, const float* __restrict__ R,
                           const int32_t* __restrict__ Z, Dims d, int B, float* __restrict__ log_psi_sqr,
                           float* __restrict__ phase, float* __restrict__ E_loc, float* __restrict__ grad_out,
-                          int coul64, const int* __restrict__ nvalid) {
+                          int coul64, const int* __restrict__ nvalid, float* __restrict__ esc) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= B || (nvalid && warp >= *nvalid)) return;
     const int b = warp, K = d.K, n3 = 3 * d.n;
@@ -1169,13 +1169,16 @@ __global__ void k_combine(const double* __restrict__ logdet, const double* __res
         if (grad_out) grad_out[(int64_t)b * n3 + t] = (float)gl;
     }
     // Laplacian of psi~
-    double lp = 0.0;
+    double lp = 0.0, lpa = 0.0;
     for (int k = lane; k < K; k += 32) {
         double dg2 = 0.0;
         for (int t = 0; t < n3; ++t) { double dd = gb[(int64_t)k * n3 + t] - gs[t]; dg2 += dd * dd; }
-        lp += ak[k] * ((lapdet[(int64_t)b * K + k] - lapdet[(int64_t)b * K + ks]) + dg2);
+        const double dl = lapdet[(int64_t)b * K + k] - lapdet[(int64_t)b * K + ks];
+        lp += ak[k] * (dl + dg2);
+        lpa += fabs(ak[k]) * (fabs(dl) + dg2);
     }
     grad_sq = warp_sum(grad_sq); gpsi_sq = warp_sum(gpsi_sq); lp = warp_sum(lp);
+    if (esc) lpa = warp_sum(lpa);
     double lapf = sgn * lp / (u + eps) - gpsi_sq / ((u + eps) * (u + eps)) + lapdet[(int64_t)b * K + ks];
     double lap = 2.0 * lapf + jb[d.lap];
     double ekin = -0.5 * (0.5 * lap + 0.25 * grad_sq);
@@ -1185,14 +1188,23 @@ __global__ void k_combine(const double* __restrict__ logdet, const double* __res
     const int32_t* Zg = Z + (size_t)gs_ * d.N;
     double epot = coul64 ? coulomb_walker64(rb, d.n, Rg, Zg, d.N, lane) : coulomb_walker(rb, d.n, Rg, Zg, d.N, lane);
     if (lane == 0) E_loc[b] = (float)(ekin + epot);
+    if (esc && lane == 0) {
+        // error scales of this walker: the magnitude S of the terms summed into E_L, the magnitude
+        // of the determinant terms summed into Lap log|psi~| (cancellation across determinants),
+        // and 1 / (|psi~| + eps) (closeness to a node of the determinant sum)
+        const double ue = u + eps;
+        esc[3 * (int64_t)b] = (float)(0.25 * fabs(lap) + 0.125 * grad_sq + fabs(epot));
+        esc[3 * (int64_t)b + 1] = (float)(lpa / ue + gpsi_sq / (ue * ue) + fabs(lapdet[(int64_t)b * K + ks]));
+        esc[3 * (int64_t)b + 2] = (float)(1.0 / ue);
+    }
 }
 
 void launch_combine(const double* logdet, const double* sign, const double* g, const double* lapdet, const double* jas,
                     const float* r, const float* R, const int32_t* Z, const Dims& d, int B,
                     float* log_psi_sqr, float* phase, float* E_loc, float* grad_out, cudaStream_t s, int coul64,
-                    const int* nvalid) {
+                    const int* nvalid, float* esc) {
     k_combine<<<(B * 32 + 255) / 256, 256, 0, s>>>(logdet, sign, g, lapdet, jas, r, R, Z, d, B, log_psi_sqr, phase,
-                                                   E_loc, grad_out, coul64, nvalid);
+                                                   E_loc, grad_out, coul64, nvalid, esc);
     count_launch();
 }
 

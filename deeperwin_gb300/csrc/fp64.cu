@@ -117,7 +117,9 @@ k64_gemm(const double* __restrict__ A, int lda, int64_t sA, const float* __restr
 static void gemm64(const double* A, int lda, int64_t sA, const float* W, int ldw, double* C, int ldc, int64_t sC,
                    int M, int N, int K, const Epi64& e, int batch, const Run64& q, cudaStream_t s) {
     dim3 grid((N + 63) / 64, (M + 63) / 64, batch);
+    timer_begin("fp64_gemm", s);
     k64_gemm<<<grid, 256, 0, s>>>(A, lda, sA, W, ldw, C, ldc, sC, M, N, K, e, q);
+    timer_end("fp64_gemm", s, 2.0 * M * N * K * batch, 0.0);
     count_launch();
 }
 
@@ -149,7 +151,9 @@ __global__ void k64_jet_tanh(const double* __restrict__ Z, int ldz, int ncols, R
 
 static void jet_tanh(const double* Z, int ldz, int ncols, const Run64& q, double* Y, int ldy, cudaStream_t s) {
     const int64_t n = (int64_t)q.B * q.d.n * ncols;
+    timer_begin("fp64_tanh", s);
     k64_jet_tanh<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(Z, ldz, ncols, q, Y, ldy);
+    timer_end("fp64_tanh", s, 0.0, 0.0);
     count_launch();
 }
 
@@ -686,12 +690,14 @@ static int run_chunk64(const Plan64& p, const Dims& d0, int Bc, const float* P, 
     const bool tang = C > 1;
     const int w0 = d.hw[0] + d.E + d.eiw[0];
     // layer-0 input [features | conv_ee | conv_ei] in XB (free until layer 1 writes it)
+    timer_begin("fp64_streams", s);
     k64_features<<<blocks_for(rows * d.N, 256), 256, 0, s>>>(r, R, Z, q, p.XB, w0);
     count_launch();
     k64_pair_streams<<<blocks_for((int64_t)Bc * n * n * 32, 256), 256, 0, s>>>(r, P, L, q, p.WP);
     count_launch();
     k64_ei_streams<<<blocks_for((int64_t)Bc * n * 32, 256), 256, 0, s>>>(r, R, Z, P, L, p.him, q, p.CE);
     count_launch();
+    timer_end("fp64_streams", s, 0.0, 0.0);
     double* xin = p.XB;
     int ldin = w0;
     for (int l = 0; l < 4; ++l) {
@@ -702,8 +708,10 @@ static int run_chunk64(const Plan64& p, const Dims& d0, int Bc, const float* P, 
         gemm64(xin, ldin, 0, P + L.h_map_w[l], d.E, p.Zt, d.E, 0, (int)rows, d.E, hw, em, 1, q, s);
         jet_tanh(p.Zt, d.E, d.E, q, p.HM, 32, s);
         // convolutions into columns [hw, hw + E + eiw)
+        timer_begin("fp64_conv", s);
         k64_conv_ee<<<(unsigned)((int64_t)Bc * n), 128, 0, s>>>(r, p.WP + (int64_t)l * Bc * n * n * 96, p.HM, q, xin,
                                                                  ldin, hw);
+        timer_end("fp64_conv", s, 0.0, 0.0);
         count_launch();
         k64_conv_ei<<<blocks_for(rows * d.eiw[l], 256), 256, 0, s>>>(p.CE + (int64_t)l * Bc * n * 5 * 32, q, d.eiw[l],
                                                                       xin, ldin, hw + d.E);
@@ -729,17 +737,23 @@ static int run_chunk64(const Plan64& p, const Dims& d0, int Bc, const float* P, 
         gemm64(H + (int64_t)i0 * C * kXW64, kXW64, (int64_t)n * C * kXW64, P + (spin == 0 ? L.bf_up : L.bf_dn), d.KN,
                p.BF + (int64_t)i0 * C * d.KN, d.KN, (int64_t)n * C * d.KN, ns * C, d.KN, d.D, e0, Bc, q, s);
     }
+    timer_begin("fp64_envelope", s);
     k64_envelope_mo<<<blocks_for((int64_t)Bc * d.K * n * n, 128), 128, 0, s>>>(r, R, Z, P, L, q, p.BF, d.KN, p.MO);
+    timer_end("fp64_envelope", s, 0.0, 0.0);
     count_launch();
     const int nmat = Bc * d.K;
     const size_t sm_lu = ((size_t)n * (2 * n + 1) + n) * sizeof(double);
     if (sm_lu > 48 * 1024) cudaFuncSetAttribute(k64_slogdet_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_lu);
+    timer_begin("fp64_lu", s);
     k64_slogdet_inv<<<nmat, 128, sm_lu, s>>>(p.MO, q, p.logdet, p.sign, tang ? p.Ainv : nullptr);
+    timer_end("fp64_lu", s, 0.0, 0.0);
     count_launch();
     if (tang) {
         const size_t sm_t = (size_t)3 * n * n * sizeof(double);
         if (sm_t > 48 * 1024) cudaFuncSetAttribute(k64_det_tangents, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_t);
+        timer_begin("fp64_det_tangents", s);
         k64_det_tangents<<<nmat, 128, sm_t, s>>>(p.MO, p.Ainv, p.sign, q, p.g, p.lapdet);
+        timer_end("fp64_det_tangents", s, 0.0, 0.0);
         count_launch();
     }
     // Jastrow MLP([64, 64, 1]) on the final embedding (wavefunction.py:42-60)
@@ -757,6 +771,12 @@ static int run_chunk64(const Plan64& p, const Dims& d0, int Bc, const float* P, 
     launch_combine(p.logdet, p.sign, p.g, p.lapdet, p.jas, r, R, Z, dc, Bc, lp, phase, E, grad, s, 1, nvalid);
     DW_CHECK_CUDA(cudaGetLastError());
     return DW_OK;
+}
+
+int fp64_max_chunk(const DwArch* a, bool tang) {
+    Dims d = make_dims(a, tang);
+    const int C = tang ? 3 * d.n + 2 : 1;
+    return choose_chunk64(d, C, 1 << 30, kChunkBudget64);
 }
 
 size_t fp64_plan_bytes(const DwArch* a, int B, bool tang) {

@@ -1,0 +1,177 @@
+// FP64 re-evaluation of the ill-conditioned tail of the mixed form's local energies.
+//
+// The split-BF16 GEMMs of the mixed form carry about 2^-16 relative error per Slater-matrix entry;
+// the forward Laplacian turns entry errors into E_L errors amplified by the cancellations of the
+// kinetic term (|grad log psi|^2 against Lap log psi near the nodes, and between the determinants
+// of the sum). For nearly all walkers that stays below a mHa; for the walkers near a node of the
+// wavefunction it reaches Hartrees and dominates the mean energy. The combine kernel reports per
+// walker the magnitude of the terms it cancels; walkers whose predicted error (that magnitude
+// times the form's relative entry accuracy) exceeds a threshold are gathered, re-evaluated by the
+// FP64 form (fp64.cu) in one launch sequence sized by a device-side count (no host
+// synchronisation: kernels skip the unused capacity), and their E_L, log psi^2 and gradient are
+// scattered back. The selection depends only on each walker's own scales, so a walker gets the
+// same result in any batch as long as the flagged walkers fit the capacity.
+#include "net.cuh"
+#include <algorithm>
+
+namespace dw {
+
+__device__ unsigned long long g_guard_walkers = 0, g_guard_flagged = 0, g_guard_overflow = 0;
+
+// Relative accuracy of the split-BF16 entries as it shows in E_L, and the tolerated predicted
+// error per walker (Hartree).
+constexpr float kGuardRel = 1.0e-5f;
+constexpr float kGuardTol = 2.0e-2f;
+
+// Predicted absolute E_L error of a walker of the mixed form from its scales (see k_combine):
+// the relative accuracy of split-BF16 entries times the largest cancelled magnitude.
+__device__ __forceinline__ bool guard_flag(const float* sc, float rel, float tol) {
+    const float m = fmaxf(sc[0], sc[1]);
+    return !(m * rel <= tol);          // NaN scales are flagged too
+}
+
+// Deterministic compaction (one block, walkers in order): idx[0 .. min(count, cap)) = the flagged
+// walkers, counts[0] = min(count, cap) (the FP64 pass's valid walkers), counts[1] = count.
+__global__ void __launch_bounds__(1024)
+k_guard_select(const float* __restrict__ esc, int B, float rel, float tol, int cap, int* __restrict__ idx,
+               int* __restrict__ counts) {
+    __shared__ int warp_tot[32];
+    __shared__ int base;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    for (int b0 = 0; b0 < B; b0 += blockDim.x) {
+        const int b = b0 + threadIdx.x;
+        const bool f = b < B && guard_flag(esc + 3 * (int64_t)b, rel, tol);
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) warp_tot[wid] = __popc(m);
+        __syncthreads();
+        int off = base;
+        for (int w = 0; w < wid; ++w) off += warp_tot[w];
+        const int pos = off + __popc(m & ((1u << lane) - 1u));
+        if (f && pos < cap) idx[pos] = b;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int t = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += warp_tot[w];
+            base += t;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        counts[0] = min(base, cap);
+        counts[1] = base;
+        atomicAdd(&g_guard_walkers, (unsigned long long)B);
+        atomicAdd(&g_guard_flagged, (unsigned long long)base);
+        if (base > cap) atomicAdd(&g_guard_overflow, (unsigned long long)(base - cap));
+    }
+}
+
+__global__ void k_guard_gather(const float* __restrict__ r, const int32_t* __restrict__ seg, const int* __restrict__ idx,
+                               const int* __restrict__ counts, int n3, float* __restrict__ r_sub,
+                               int32_t* __restrict__ seg_sub, int cap) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = (int)(e / n3), c = (int)(e % n3);
+    if (k >= cap || k >= counts[0]) return;
+    const int b = idx[k];
+    r_sub[(int64_t)k * n3 + c] = r[(int64_t)b * n3 + c];
+    if (seg && c == 0) seg_sub[k] = seg[b];
+}
+
+__global__ void k_guard_scatter(const float* __restrict__ E_sub, const float* __restrict__ lp_sub,
+                                const float* __restrict__ g_sub, const int* __restrict__ idx,
+                                const int* __restrict__ counts, int n3, int cap, float* __restrict__ E,
+                                float* __restrict__ lp, float* __restrict__ grad) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = (int)(e / n3), c = (int)(e % n3);
+    if (k >= cap || k >= counts[0]) return;
+    const int b = idx[k];
+    if (c == 0) {
+        E[b] = E_sub[k];
+        if (lp) lp[b] = lp_sub[k];
+    }
+    if (grad) grad[(int64_t)b * n3 + c] = g_sub[(int64_t)k * n3 + c];
+}
+
+int guard_capacity(const DwArch* a, int B) {
+    // up to 1 / 32 of the batch (at least 16), limited to one chunk of the FP64 form (the
+    // device-side walker count needs the flagged walkers in one launch sequence)
+    const int want = std::min(B, std::max(16, (B + 31) / 32));
+    return std::max(1, std::min(want, fp64_max_chunk(a, true)));
+}
+
+struct GuardPlan {
+    int cap;
+    int* idx; int* counts; float* r_sub; int32_t* seg_sub; float* E_sub; float* lp_sub; float* g_sub;
+    void* fp64_ws; size_t fp64_bytes;
+    size_t bytes;
+};
+
+static GuardPlan carve_guard(const DwArch* a, int B, void* ws) {
+    GuardPlan g;
+    const int n3 = 3 * a->n_el;
+    g.cap = guard_capacity(a, B);
+    Carver c(ws, (size_t)-1);
+    g.idx = c.take<int>((size_t)g.cap);
+    g.counts = c.take<int>(2);
+    g.r_sub = c.take<float>((size_t)g.cap * n3);
+    g.seg_sub = c.take<int32_t>((size_t)g.cap);
+    g.E_sub = c.take<float>((size_t)g.cap);
+    g.lp_sub = c.take<float>((size_t)g.cap);
+    g.g_sub = c.take<float>((size_t)g.cap * n3);
+    g.fp64_bytes = fp64_plan_bytes(a, g.cap, true);
+    g.fp64_ws = c.take<unsigned char>(g.fp64_bytes);
+    g.bytes = c.used + 256;
+    return g;
+}
+
+size_t guard_bytes(const DwArch* a, int B) { return carve_guard(a, B, nullptr).bytes; }
+
+int tail_guard(const DwArch* a, const float* P, const void* prepared, const float* r, int B, const float* R,
+               const int32_t* Z, const int32_t* seg, int nseg, const float* esc, float* E, float* lp, float* grad,
+               void* ws, size_t wsb, cudaStream_t s) {
+    GuardPlan g = carve_guard(a, B, ws);
+    if (g.bytes > wsb) return DW_ERR_WORKSPACE;
+    const int n3 = 3 * a->n_el;
+    k_guard_select<<<1, 1024, 0, s>>>(esc, B, kGuardRel, kGuardTol, g.cap, g.idx, g.counts);
+    count_launch();
+    const int64_t ne = (int64_t)g.cap * n3;
+    k_guard_gather<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(r, seg, g.idx, g.counts, n3, g.r_sub,
+                                                                 seg ? g.seg_sub : nullptr, g.cap);
+    count_launch();
+    DW_CHECK(fp64_forward_all(a, P, prepared, g.r_sub, g.cap, R, Z, g.lp_sub, nullptr, g.E_sub, grad ? g.g_sub : nullptr,
+                              true, g.fp64_ws, g.fp64_bytes, s, seg ? g.seg_sub : nullptr, nseg, g.counts));
+    k_guard_scatter<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(g.E_sub, g.lp_sub, g.g_sub, g.idx, g.counts, n3, g.cap,
+                                                                  E, lp, grad);
+    count_launch();
+    DW_CHECK_CUDA(cudaGetLastError());
+    return DW_OK;
+}
+
+}  // namespace dw
+
+extern "C" {
+
+// Cumulative counts of the tail re-evaluation since the last reset: walkers seen, walkers
+// flagged, flagged walkers beyond the capacity (kept at their mixed-form values). Synchronizes
+// the device. No counterpart in the reference.
+int dw_guard_stats(int64_t* walkers, int64_t* flagged, int64_t* overflow, int reset) {
+    unsigned long long v[3] = {0, 0, 0};
+    if (cudaDeviceSynchronize() != cudaSuccess) return DW_ERR_CUDA;
+    if (cudaMemcpyFromSymbol(&v[0], dw::g_guard_walkers, sizeof(v[0])) != cudaSuccess ||
+        cudaMemcpyFromSymbol(&v[1], dw::g_guard_flagged, sizeof(v[1])) != cudaSuccess ||
+        cudaMemcpyFromSymbol(&v[2], dw::g_guard_overflow, sizeof(v[2])) != cudaSuccess)
+        return DW_ERR_CUDA;
+    if (walkers) *walkers = (int64_t)v[0];
+    if (flagged) *flagged = (int64_t)v[1];
+    if (overflow) *overflow = (int64_t)v[2];
+    if (reset) {
+        unsigned long long z = 0;
+        cudaMemcpyToSymbol(dw::g_guard_walkers, &z, sizeof(z));
+        cudaMemcpyToSymbol(dw::g_guard_flagged, &z, sizeof(z));
+        cudaMemcpyToSymbol(dw::g_guard_overflow, &z, sizeof(z));
+    }
+    return DW_OK;
+}
+
+}  // extern "C"

@@ -17,6 +17,127 @@ __device__ __forceinline__ float uniform1(uint64_t seed, uint32_t walker, uint32
     Philox4 x = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
     return u32_to_unit(x.x);
 }
+// Four uniforms in (0, 1) for (walker, step, group, tag).
+__device__ __forceinline__ void uniforms4(uint64_t seed, uint32_t walker, uint32_t step, uint32_t group, uint32_t tag,
+                                          float (&o)[4]) {
+    Philox4 x = philox4x32_10(Philox4{walker, step, group, tag}, (uint32_t)seed, (uint32_t)(seed >> 32));
+    o[0] = u32_to_unit(x.x); o[1] = u32_to_unit(x.y); o[2] = u32_to_unit(x.z); o[3] = u32_to_unit(x.w);
+}
+constexpr uint32_t kTagCauchy = 0xC4A3B1E7u, kTagSpin = 0x5F1A9C3Du;
+
+// Standard normal for coordinate q of a walker's proposal at counter `step`.
+__device__ __forceinline__ float normal_q(uint64_t key, uint32_t wk, uint32_t step, int q) {
+    float z[4];
+    normals4(key, wk, step, (uint32_t)(q >> 2), z);
+    return z[q & 3];
+}
+
+// Local step size and Langevin drift of one electron (mcmc.py:204-215): s = stepsize
+// clip(d_closest_ion, r_min, r_max), g = -scale sum_I Z_I (r - R_I) / |r - R_I|.
+__device__ __forceinline__ void local_step(const float* x, const float* R, const int32_t* Z, int N, float stepsize,
+                                           const MhArgs& a, float& s, float (&g)[3]) {
+    float dmin = 3.4e38f;
+    g[0] = g[1] = g[2] = 0.f;
+    for (int I = 0; I < N; ++I) {
+        if (Z[I] <= 0) continue;                 // padding ion of a packed geometry
+        const float dx = x[0] - R[3 * I], dy = x[1] - R[3 * I + 1], dz = x[2] - R[3 * I + 2];
+        const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+        dmin = fminf(dmin, d);
+        const float w = -a.langevin_scale * (float)Z[I] / d;
+        g[0] += w * dx; g[1] += w * dy; g[2] += w * dz;
+    }
+    s = stepsize * fminf(fmaxf(dmin, a.r_min), a.r_max);
+}
+
+// Proposal of one walker (warp): writes pw and returns the log proposal ratio (lane 0).
+__device__ float propose_walker(const MhArgs& a, const float* rw, float* pw, float step, int nr, uint64_t key,
+                                uint32_t wk, int sg, int lane) {
+    const int n = a.n, n3 = 3 * n;
+    const int kind = a.proposal;
+    float lq = 0.f;
+    if (kind == DW_PROPOSAL_NORMAL || kind == DW_PROPOSAL_NORMAL_ONE_EL) {
+        const int one = kind == DW_PROPOSAL_NORMAL_ONE_EL ? nr % n : -1;
+        for (int g = lane; g * 4 < n3; g += 32) {
+            float z[4];
+            normals4(key, wk, (uint32_t)nr, (uint32_t)g, z);
+            #pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int q = g * 4 + c;
+                if (q < n3) pw[q] = (one < 0 || q / 3 == one) ? rw[q] + step * z[c] : rw[q];   // mcmc.py:178-179, 190-192
+            }
+        }
+    } else if (kind == DW_PROPOSAL_CAUCHY) {
+        for (int g = lane; g * 4 < n3; g += 32) {
+            float u[4];
+            uniforms4(key, wk, (uint32_t)nr, (uint32_t)g, kTagCauchy, u);
+            #pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int q = g * 4 + c;
+                float sn, cs;
+                sincospif(u[c] - 0.5f, &sn, &cs);                   // Cauchy = tan(pi (u - 1/2))
+                if (q < n3) pw[q] = rw[q] + step * (sn / cs);       // mcmc.py:199-200
+            }
+        }
+    } else {
+        // local step sizes (all electrons, or electron nr mod n) and the Langevin drift
+        const float* R = a.R + (size_t)sg * a.N * 3;
+        const int32_t* Z = a.Z + (size_t)sg * a.N;
+        const int one = kind == DW_PROPOSAL_LOCAL_ONE_EL ? nr % n : -1;
+        const bool lang = kind == DW_PROPOSAL_LANGEVIN;
+        for (int i = lane; i < n; i += 32) {
+            const float* x = rw + 3 * i;
+            float* y = pw + 3 * i;
+            if (one >= 0 && i != one) { y[0] = x[0]; y[1] = x[1]; y[2] = x[2]; continue; }
+            float s, g[3], s2, g2[3];
+            local_step(x, R, Z, a.N, step, a, s, g);
+            float d_fwd = 0.f;
+            for (int c = 0; c < 3; ++c) {
+                const float z = normal_q(key, wk, (uint32_t)nr, 3 * i + c);
+                const float drift = lang ? g[c] * s * s : 0.f;
+                y[c] = x[c] + z * s + drift;                         // mcmc.py:227, :270
+                const float e = y[c] - x[c] - drift;
+                d_fwd += e * e;
+            }
+            local_step(y, R, Z, a.N, step, a, s2, g2);
+            float d_rev = 0.f;
+            for (int c = 0; c < 3; ++c) {
+                const float e = x[c] - y[c] - (lang ? g2[c] * s2 * s2 : 0.f);
+                d_rev += e * e;
+            }
+            // 3 (log s - log s') + (|fwd|^2 / s^2 - |rev|^2 / s'^2) / 2 (mcmc.py:230-233, :280-285)
+            lq += 3.f * (logf(s) - logf(s2)) + 0.5f * (d_fwd / (s * s) - d_rev / (s2 * s2));
+        }
+        lq = warp_sum(lq);
+    }
+    // spin swap / flip of the proposal (mcmc.py:346-356). The swap exchanges an electron of the
+    // first n_el // 2 with one of the others, the split the reference uses (mcmc.py:350).
+    if (a.p_swap > 0.f || a.p_flip > 0.f) {
+        __syncwarp();
+        float u[4];
+        uniforms4(key, wk, (uint32_t)nr, 0u, kTagSpin, u);
+        const int nh = n / 2;
+        if (a.p_swap > 0.f && u[0] < a.p_swap && nh > 0) {
+            const int iu = min((int)(u[1] * nh), nh - 1);
+            const int id = nh + min((int)(u[2] * (n - nh)), n - nh - 1);
+            if (lane < 3) {
+                const float t = pw[3 * iu + lane];
+                pw[3 * iu + lane] = pw[3 * id + lane];
+                pw[3 * id + lane] = t;
+            }
+            __syncwarp();
+        }
+        if (a.p_flip > 0.f && u[3] < a.p_flip) {
+            for (int q = lane; q < 3 * nh; q += 32) {
+                const int i = q / 3, c = q % 3;
+                const float t = pw[3 * i + c];
+                pw[3 * i + c] = pw[3 * (n - 1 - i) + c];
+                pw[3 * (n - 1 - i) + c] = t;
+            }
+            __syncwarp();
+        }
+    }
+    return lq;
+}
 
 // Step-size rule (mcmc.py:370-387): on steps where step_nr % interval == 0, divide by 1.05
 // if the previous running acceptance is below target, else multiply; clip.
@@ -50,8 +171,9 @@ __global__ void k_mh(MhArgs a, int phase) {
         int nr_prop = step_nr;
         if (phase >= 1) {
             float lp = a.lp[w], lpn = a.lp_prop[w];
+            const float lq = a.lq ? a.lq[w] : 0.f;
             float U = uniform1(key, wk, (uint32_t)step_nr);
-            bool acc = expf(lpn - lp) > U;          // mcmc.py:359-362
+            bool acc = expf(lpn - lp + lq) > U;     // mcmc.py:358-362
             int age = a.age[w];
             acc = acc || (age >= a.max_age);        // mcmc.py:363
             if (acc) for (int q = lane; q < n3; q += 32) rw[q] = pw[q];
@@ -65,15 +187,8 @@ __global__ void k_mh(MhArgs a, int phase) {
             __syncwarp();
         }
         if (phase <= 1) {
-            for (int g = lane; g * 4 < n3; g += 32) {
-                float z[4];
-                normals4(key, wk, (uint32_t)nr_prop, (uint32_t)g, z);
-                #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    int q = g * 4 + c;
-                    if (q < n3) pw[q] = rw[q] + s_prop * z[c];   // mcmc.py:178-179
-                }
-            }
+            const float lq = propose_walker(a, rw, pw, s_prop, nr_prop, key, wk, sg, lane);
+            if (a.lq && lane == 0) a.lq[w] = lq;
         }
     }
     if (phase == 0) return;

@@ -21,6 +21,14 @@ struct MhArgs {
     const int32_t* widx;
     const uint64_t* seeds;
     int nseg;
+    // Proposal rule (DwProposal) and its parameters; lq[B] holds the log proposal ratio of the
+    // pending proposals (asymmetric rules). R / Z / N: nuclei of each segment (local, Langevin).
+    int proposal;
+    float r_min, r_max, langevin_scale, p_swap, p_flip;
+    float* lq;
+    const float* R;
+    const int32_t* Z;
+    int N;
 };
 
 void launch_mh(const MhArgs& a, int phase, cudaStream_t s);

@@ -120,7 +120,7 @@ void launch_det_tangents(const float* MO, const float* Ainv, const double* sign,
 void launch_combine(const double* logdet, const double* sign, const double* g, const double* lapdet, const double* jas,
                     const float* r, const float* R, const int32_t* Z, const Dims& d, int B,
                     float* log_psi_sqr, float* phase, float* E_loc, float* grad_out, cudaStream_t s,
-                    int coul64 = 0, const int* nvalid = nullptr);
+                    int coul64 = 0, const int* nvalid = nullptr, float* esc = nullptr);
 void launch_coulomb(const float* r, int B, int n, const float* R, const int32_t* Z, int N, float* E, cudaStream_t s);
 // FP64 Gauss-Jordan log|det| and inverse of the value-channel Slater matrices (any Dims mode).
 void launch_slogdet_inv(const float* MO, const Dims& d, int B, double* logdet, double* sign, float* Ainv, cudaStream_t s);
@@ -137,9 +137,18 @@ void prepared_fp32_layers(const DwArch* a, const void* prepared, const float* ma
 // fp64.cu: FP64 form (DW_PRECISION_FP64). nvalid (device int, may be null): walkers at or beyond
 // *nvalid are skipped; it requires the walkers to fit one chunk.
 size_t fp64_plan_bytes(const DwArch* a, int B, bool tang);
+int fp64_max_chunk(const DwArch* a, bool tang);     // walkers of one FP64 chunk
 int fp64_forward_all(const DwArch* a, const float* P, const void* prepared, const float* r, int B, const float* R,
                      const int32_t* Z, float* lp, float* phase, float* E, float* grad, bool tang, void* ws,
                      size_t ws_bytes, cudaStream_t s, const int32_t* seg, int nseg, const int* nvalid);
+
+// guard.cu: FP64 re-evaluation of the mixed form's flagged walkers (esc: per-walker error scales
+// written by the combine kernel, 3 floats per walker)
+int guard_capacity(const DwArch* a, int B);
+size_t guard_bytes(const DwArch* a, int B);
+int tail_guard(const DwArch* a, const float* P, const void* prepared, const float* r, int B, const float* R,
+               const int32_t* Z, const int32_t* seg, int nseg, const float* esc, float* E, float* lp, float* grad,
+               void* ws, size_t wsb, cudaStream_t s);
 
 // backward.cu
 size_t bwd_bytes(const DwArch* a, int B, int* chunk);

@@ -41,6 +41,20 @@ def pmean_(t: torch.Tensor, group=None) -> torch.Tensor:
     return t
 
 
+def pmean_array(x, group=None, device=None):
+    """pmean of a small host array (e.g. the force metrics), returned as float64 numpy; the
+    exchange runs on `device` (the backend's device: CUDA under NCCL, CPU under gloo)."""
+    import numpy as np
+    a = np.asarray(x, dtype=np.float64)
+    if world(group) == 1:
+        return a
+    if device is None:
+        device = "cuda" if torch.distributed.get_backend(group) == "nccl" else "cpu"
+    t = torch.as_tensor(a, device=device).clone()
+    pmean_(t, group)
+    return t.cpu().numpy()
+
+
 def combine_moments(mean: torch.Tensor, var: torch.Tensor, group=None) -> Tuple[torch.Tensor, torch.Tensor]:
     """Global (pmean of means, pmean of nanmean((x - global mean)^2)) from each rank's nanmean and
     population variance, as ``E_mean = pmean(nanmean(E))``,

@@ -12,6 +12,7 @@ threshold).
 """
 from __future__ import annotations
 
+import dataclasses
 from typing import Dict, Iterable, Optional
 
 import numpy as np
@@ -58,12 +59,33 @@ def summarize(history: Dict[str, Iterable]) -> Dict[str, float]:
     return out
 
 
+@dataclasses.dataclass
+class ForceEvaluationConfig:
+    """ForceEvaluationConfig (configuration.py:1225-1229)."""
+
+    use: bool = True
+    R_cut: float = 0.1
+    R_core: float = 0.5
+    use_antithetic_sampling: bool = False
+
+
+def force_metrics(forces: np.ndarray) -> Dict[str, np.ndarray]:
+    """The force observables of get_observables (evaluation.py:152-157): calculate_forces returns
+    the [n_ions, 3] batch mean, and the metrics are its nanmean and nan-variance over axis 0."""
+    f = np.asarray(forces, dtype=np.float64)
+    mean = np.nanmean(f, axis=0)
+    return {"forces_mean": mean, "forces_var": np.nanmean((f - mean) ** 2, axis=0)}
+
+
 def evaluate_wavefunction(params, state, mcmc, n_epochs: int, n_burn_in: Optional[int] = None,
-                          n_inter_steps: Optional[int] = None, group=None):
+                          n_inter_steps: Optional[int] = None, group=None,
+                          forces: Optional[ForceEvaluationConfig] = None):
     """Burn-in, then `n_epochs` x (inter-steps, local energies); returns (history, summary, state).
 
     history: per epoch ``E_mean`` (FP64 mean of the walkers' local energies) and ``E_var``; with
-    several ranks both are combined as the reference's pmean (evaluation.py:148-151)."""
+    several ranks both are combined as the reference's pmean (evaluation.py:148-151). With a
+    force configuration also ``forces_mean`` / ``forces_var`` (evaluation.py:152-157) from
+    dw_forces at the chain's current log psi^2, averaged over ranks."""
     from . import api, dist
     a = params.arch
     spin = (a.n_up, a.n_dn)
@@ -72,6 +94,8 @@ def evaluate_wavefunction(params, state, mcmc, n_epochs: int, n_burn_in: Optiona
     if burn > 0:
         mcmc.run_mcmc_steps(None, state, params, a.n_up, a.n_dn, None, n_steps=burn, reevaluate=True, group=group)
     hist: Dict[str, list] = {"E_mean": [], "E_var": []}
+    if forces is not None and forces.use:
+        hist["forces_mean"], hist["forces_var"] = [], []
     for _ in range(n_epochs):
         mcmc.run_mcmc_steps(None, state, params, a.n_up, a.n_dn, None, n_steps=inter, reevaluate=True, group=group)
         E = api.local_energy(params, spin, state.r, state.R, state.Z)
@@ -79,4 +103,10 @@ def evaluate_wavefunction(params, state, mcmc, n_epochs: int, n_burn_in: Optiona
         m, v = dist.combine_moments(st[0], st[1], group)
         hist["E_mean"].append(float(m))
         hist["E_var"].append(float(v))
+        if "forces_mean" in hist:
+            F = api.calculate_forces(params, state.r, state.R, state.Z, state.log_psi_sqr, forces.R_cut, forces.R_core,
+                                     forces.use_antithetic_sampling)
+            fm = force_metrics(F.cpu().numpy())
+            hist["forces_mean"].append(dist.pmean_array(fm["forces_mean"], group))
+            hist["forces_var"].append(dist.pmean_array(fm["forces_var"], group))
     return hist, summarize(hist), state

@@ -365,10 +365,7 @@ class ServingEngine:
 
     def _mh(self, g: _Group, p, prm: Params, n_steps: int) -> None:
         B = p["B"]
-        c = self.mcmc
-        cfg = _lib.DwMcmcConfig(int(n_steps), int(c.max_age), int(c.stepsize_update_interval),
-                                float(c.target_acceptance_rate), float(c.min_stepsize_scale),
-                                float(c.max_stepsize_scale), 0, 0)
+        cfg = self.mcmc.c_config(n_steps, 0, False)
         nbytes = self._ws_bytes(g.n_el, g.n_up, B, 2)
         ws = self._workspace(g.si, nbytes)
         _lib.check(_lib.lib().dw_mcmc_steps_packed(

@@ -128,6 +128,18 @@ typedef struct DwMcmcScalars {
     int32_t error;        /* internal */
 } DwMcmcScalars;
 
+/* Proposal rules of MetropolisHastingsMonteCarlo._build_proposal_function (mcmc.py:328-342). */
+enum DwProposal {
+    DW_PROPOSAL_NORMAL = 0,        /* r + s N(0, 1) (mcmc.py:175-180) */
+    DW_PROPOSAL_CAUCHY = 1,        /* r + s Cauchy (mcmc.py:196-201) */
+    DW_PROPOSAL_LANGEVIN = 2,      /* local step size + nuclear-attraction drift, with the proposal ratio
+                                      (mcmc.py:204-215, :260-288) */
+    DW_PROPOSAL_LOCAL = 3,         /* step size s clip(d_closest_ion, r_min, r_max) per electron, with the
+                                      proposal ratio (mcmc.py:218-234) */
+    DW_PROPOSAL_NORMAL_ONE_EL = 4, /* one electron (step_nr mod n_el) per step (mcmc.py:183-193) */
+    DW_PROPOSAL_LOCAL_ONE_EL = 5   /* local step size, one electron per step (mcmc.py:237-257) */
+};
+
 typedef struct DwMcmcConfig {
     int32_t n_steps;
     int32_t max_age;
@@ -137,13 +149,21 @@ typedef struct DwMcmcConfig {
     float max_stepsize;
     uint64_t seed;
     int32_t reevaluate;   /* 1: recompute log psi^2 of the current walkers first (mcmc.py:396) */
+    int32_t proposal;     /* DwProposal */
+    float r_min;          /* local / Langevin proposals: clip range of the closest-nucleus distance */
+    float r_max;
+    float langevin_scale; /* Langevin proposal: scale of the nuclear-attraction drift */
+    float p_spin_swap;    /* probability of exchanging an electron of the first n_el / 2 with one of the
+                             others after the proposal (mcmc.py:291-302, 349-354) */
+    float p_spin_flip;    /* probability of reversing the electron order (mcmc.py:305-310, 355-356) */
 } DwMcmcConfig;
 
-/* n_steps all-walker Metropolis-Hastings steps with Gaussian proposals.
+/* n_steps all-walker Metropolis-Hastings steps with the proposal rule cfg->proposal and the
+ * optional spin swaps / flips; acceptance exp(log psi^2' - log psi^2 + log q-ratio) > U.
  * r, log_psi_sqr, age (int32) and the device scalars are updated in place.
  * Random numbers: Philox-4x32-10 keyed by (seed, walker), counter = step number.
- * Replaces MetropolisHastingsMonteCarlo.run_mcmc_steps (mcmc.py:325-327, :389-406) with
- * the normal proposal (mcmc.py:175-180) and make_mcmc_step (mcmc.py:345-387). */
+ * Replaces MetropolisHastingsMonteCarlo.run_mcmc_steps (mcmc.py:325-327, :389-406) with its
+ * proposal functions (mcmc.py:175-310) and make_mcmc_step (mcmc.py:345-387). */
 int dw_mcmc_steps(const DwArch* arch, int precision, const float* params, const void* prepared,
                   float* r, int n_walkers, const float* R, const int32_t* Z,
                   float* log_psi_sqr, int32_t* age, DwMcmcScalars* scalars_dev,
@@ -178,6 +198,19 @@ int dw_mcmc_steps_packed(const DwArch* arch, int precision, const float* params,
                          const int32_t* seg, const int32_t* walker_index, const uint64_t* seeds,
                          float* log_psi_sqr, int32_t* age, DwMcmcScalars* scalars_dev,
                          const DwMcmcConfig* cfg, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Forces on the nuclei (hamiltonian.py:309-338 calculate_forces): forces[I][c] = mean over walkers of
+ * sum_i Z_I (r_i - R_I)_c / d'^3, d' = d / tanh(d / R_cut), plus the nucleus-nucleus repulsion
+ * (hamiltonian.py:298-306). antithetic = 1: each walker is averaged with its mirror image (electrons
+ * within R_core of their closest nucleus reflected through it) weighted by psi^2(mirror) / psi^2,
+ * which evaluates log psi^2 at the mirrored walkers in the given precision form. log_psi_sqr: the
+ * walkers' current log psi^2. forces [n_ions * 3] FP64; per_walker ([n_walkers, n_ions, 3] FP64,
+ * electrons summed) may be NULL. Workspace: dw_forces_workspace_bytes. */
+size_t dw_forces_workspace_bytes(const DwArch* arch, int precision, int n_walkers);
+int dw_forces(const DwArch* arch, int precision, const float* params, const void* prepared,
+              const float* r, int n_walkers, const float* R, const int32_t* Z, const float* log_psi_sqr,
+              float R_cut, float R_core, int antithetic, double* forces, double* per_walker,
+              void* workspace, size_t workspace_bytes, void* stream);
 
 /* FP64 cross-walker statistics of a float32 vector: out[0]=mean, out[1]=variance
  * (population), out[2]=count of entries that are not NaN. Only NaNs are skipped, as jnp.nanmean
@@ -217,6 +250,14 @@ int dw_log_psi_sqr_noalloc(const DwArch* arch, int precision, const float* param
                            float* log_psi_sqr, float* phase, void* stream);
 /* Size in bytes of the static scratch array used by dw_log_psi_sqr_noalloc. */
 size_t dw_noalloc_scratch_bytes(void);
+
+/* Instrumentation of the mixed form's local energy: walkers whose predicted E_L error (the
+ * magnitude of the terms the forward Laplacian cancels, times the split-BF16 entry accuracy) is
+ * above the tolerance are re-evaluated in FP64 inside dw_local_energy / dw_local_energy_packed.
+ * Returns the cumulative counts since the last reset: walkers seen, walkers flagged, flagged
+ * walkers beyond the per-call capacity (those keep their mixed-form values). Synchronizes the
+ * device. No reference counterpart. */
+int dw_guard_stats(int64_t* walkers, int64_t* flagged, int64_t* overflow, int reset);
 
 /* Number of kernel launches issued by the last call on this host thread (instrumentation). */
 int64_t dw_last_launch_count(void);

@@ -255,6 +255,32 @@ def local_energy_batched(p, arch, r, R, Z):
     return e_kin + e_ee + e_ei + e_ii
 
 
+def forces(p, arch, r, R, Z, log_psi_sqr, R_cut=0.1, R_core=0.5, antithetic=False):
+    """``calculate_forces`` (hamiltonian.py:293-338): [N, 3] batch mean of the per-walker
+    electron-nucleus forces with the tanh cut-off, optionally antithetic, plus the ion-ion term."""
+    r, R = _t(r), _t(R)
+    Zt = _t(np.asarray(Z, np.float64))
+
+    def direct(x):
+        diff, d = el_ion(x, R)                                       # diff = r_i - R_I
+        d = d / torch.tanh(d / R_cut)
+        return Zt[:, None] * diff / d[..., None] ** 3                 # [B, n, N, 3]
+    f = direct(r)
+    if antithetic:
+        diff, d = el_ion(r, R)
+        idx = d.argmin(dim=-1)
+        dmin = d.min(dim=-1, keepdim=True).values
+        to_closest = torch.gather(diff, 2, idx[..., None, None].expand(-1, -1, 1, 3))[:, :, 0]
+        rm = torch.where(dmin < R_core, r - 2 * to_closest, r)
+        w = torch.exp(log_psi_sqr_raw(p, arch, rm, R, Z)[1] - _t(log_psi_sqr))
+        f = (f + direct(rm) * w[:, None, None, None]) * 0.5
+    force = f.sum(1).mean(0)
+    diffR = R[:, None, :] - R[None, :, :]
+    dist = torch.linalg.norm(diffR, dim=-1, keepdim=True)
+    Zm = Zt[:, None] * Zt[None, :] - torch.diag(Zt ** 2)
+    return force + (diffR * Zm[..., None] / (dist + 1e-8) ** 3).sum(1)
+
+
 # --------------------------------------------------------------------------- MCMC
 def mh_step(p, arch, R, Z, r, lp, age, stepsize, noise, uniform, max_age):
     """One Metropolis-Hastings step with injected randomness
@@ -270,6 +296,84 @@ def mh_step(p, arch, R, Z, r, lp, age, stepsize, noise, uniform, max_age):
     lp_out = torch.where(acc, lp_new, lp)
     r_out = torch.where(acc[:, None, None], r_new, r)
     return r_out, lp_out, age_new, acc
+
+
+def _closest_ion_dist(r, R):
+    return torch.linalg.norm(r[..., :, None, :] - R[None, None, :, :], dim=-1).min(dim=-1).values   # [B, n]
+
+
+def propose(kind, r, R, Z, stepsize, step_nr, noise, cauchy_u=None, r_min=None, r_max=None, langevin_scale=1.0):
+    """Proposal functions of mcmc.py:175-288 with injected randomness; returns (r_new, log_q_ratio).
+    noise: standard normals [B, n, 3]; cauchy_u: uniforms in (0, 1) [B, n, 3] for the Cauchy proposal."""
+    r, R = _t(r), _t(R)
+    z = _t(noise)
+    B, n, _ = r.shape
+    zero = torch.zeros(B, dtype=T)
+    if kind == "normal":                                                 # mcmc.py:175-180
+        return r + z * stepsize, zero
+    if kind == "cauchy":                                                 # mcmc.py:196-201
+        return r + torch.tan(math.pi * (_t(cauchy_u) - 0.5)) * stepsize, zero
+    if kind in ("normal_one_el", "local_one_el"):
+        idx = step_nr % n                                                # mcmc.py:185, :240
+        r_new = r.clone()
+        if kind == "normal_one_el":                                      # mcmc.py:183-193
+            r_new[:, idx] += z[:, idx] * stepsize
+            return r_new, zero
+        s = stepsize * torch.clamp(_closest_ion_dist(r, R)[:, idx], r_min, r_max)      # mcmc.py:237-245
+        r_new[:, idx] += z[:, idx] * s[:, None]
+        s_new = stepsize * torch.clamp(_closest_ion_dist(r_new, R)[:, idx], r_min, r_max)
+        d2 = ((r_new[:, idx] - r[:, idx]) ** 2).sum(-1)
+        return r_new, 3 * (torch.log(s) - torch.log(s_new)) + 0.5 * d2 * (1 / s ** 2 - 1 / s_new ** 2)
+    if kind == "local":                                                  # mcmc.py:218-234
+        s = stepsize * torch.clamp(_closest_ion_dist(r, R), r_min, r_max)
+        r_new = r + z * s[..., None]
+        s_new = stepsize * torch.clamp(_closest_ion_dist(r_new, R), r_min, r_max)
+        d2 = ((r_new - r) ** 2).sum(-1)
+        lq = 3 * (torch.log(s) - torch.log(s_new)) + 0.5 * d2 * (1 / s ** 2 - 1 / s_new ** 2)
+        return r_new, lq.sum(-1)
+    if kind == "langevin":                                               # mcmc.py:204-215, :260-288
+        Zt = _t(np.asarray(Z, np.float64))
+
+        def bias(x):
+            diff = x[..., :, None, :] - R[None, None, :, :]
+            dist = torch.linalg.norm(diff, dim=-1)
+            s_ = stepsize * torch.clamp(dist.min(dim=-1, keepdim=True).values, r_min, r_max)
+            g_ = -langevin_scale * (diff * Zt[:, None] / dist[..., None]).sum(-2)
+            return s_, g_
+        s, g = bias(r)
+        r_new = r + z * s + g * s ** 2
+        s_new, g_new = bias(r_new)
+        d_fwd = ((r_new - r - g * s ** 2) ** 2).sum(-1)
+        d_rev = ((r - r_new - g_new * s_new ** 2) ** 2).sum(-1)
+        s, s_new = s[..., 0], s_new[..., 0]
+        lq = 3 * (torch.log(s) - torch.log(s_new)) + 0.5 * (d_fwd / s ** 2 - d_rev / s_new ** 2)
+        return r_new, lq.sum(-1)
+    raise ValueError(kind)
+
+
+def spin_swap(r, n_up, p_swap, u_select, ind_up, ind_dn):
+    """``spin_swap`` (mcmc.py:291-302) with injected draws: ind_up in [0, n_up), ind_dn in
+    [n_up, n_el); with probability p_swap the two electrons exchange positions."""
+    r = _t(r).clone()
+    for b in range(r.shape[0]):
+        if u_select[b] < p_swap:
+            i, j = int(ind_up[b]), int(ind_dn[b])
+            r[b, [i, j]] = r[b, [j, i]]
+    return r
+
+
+def spin_flip(r, p_flip, u):
+    """``spin_flip`` (mcmc.py:305-310): with probability p_flip the electron order is reversed."""
+    r = _t(r)
+    return torch.where(_t(u)[:, None, None] < p_flip, r.flip(-2), r)
+
+
+def mh_accept(lp, lp_new, log_q, age, uniform, max_age):
+    """Acceptance of ``make_mcmc_step`` (mcmc.py:357-366) with the proposal ratio."""
+    lp, lp_new = _t(lp), _t(lp_new)
+    acc = torch.exp(lp_new - lp + _t(log_q)) > _t(uniform)
+    age = torch.as_tensor(age)
+    return acc | (age >= max_age)
 
 
 def adjust_stepsize(step_nr, stepsize, acc_rate_prev, interval, target=0.5, lo=1e-2, hi=1.0):

@@ -48,3 +48,23 @@ def accept_uniform(seed, n_walkers, step):
     w = np.arange(n_walkers, dtype=np.uint64)
     x = philox4x32_10(w, np.full_like(w, step), np.zeros_like(w), np.full_like(w, 0x63D83595), seed)
     return _unit(x[0])
+
+
+def uniforms4(seed, n_walkers, step, group, tag):
+    """Four uniforms per walker for Philox counter {walker, step, group, tag}: [n_walkers, 4]."""
+    w = np.arange(n_walkers, dtype=np.uint64)
+    x = philox4x32_10(w, np.full_like(w, step), np.full_like(w, group), np.full_like(w, tag), seed)
+    return np.stack([_unit(v) for v in x], -1)
+
+
+def cauchy_uniforms(seed, n_walkers, n_el, step):
+    """The uniforms behind the Cauchy proposal of each coordinate: [n_walkers, n_el, 3]."""
+    n3 = 3 * n_el
+    groups = (n3 + 3) // 4
+    u = np.stack([uniforms4(seed, n_walkers, step, g, 0xC4A3B1E7) for g in range(groups)], 1)
+    return u.reshape(n_walkers, groups * 4)[:, :n3].reshape(n_walkers, n_el, 3)
+
+
+def spin_uniforms(seed, n_walkers, step):
+    """(select, up index, down index, flip) uniforms of the spin swap / flip: [n_walkers, 4]."""
+    return uniforms4(seed, n_walkers, step, 0, 0x5F1A9C3D)

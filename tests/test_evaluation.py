@@ -81,3 +81,37 @@ def test_evaluation_loop_order(monkeypatch):
     np.testing.assert_allclose(hist["E_mean"], [2.0, 2.0, 3.0])
     np.testing.assert_allclose(hist["E_var"], [2.0 / 3.0, 0.0, 14.0 / 3.0])
     assert summ["E_mean"] == pytest.approx(7.0 / 3.0)
+
+
+def test_force_metrics_and_loop(monkeypatch):
+    """Force observables as get_observables forms them (evaluation.py:152-157): nanmean and
+    nan-variance over axis 0 of calculate_forces' [n_ions, 3] result, once per epoch after the
+    energies."""
+    from deeperwin_gb300 import api
+    F = np.array([[1.0, 2.0, 3.0], [3.0, np.nan, -1.0]])
+    m = EV.force_metrics(F)
+    np.testing.assert_allclose(m["forces_mean"], [2.0, 2.0, 1.0])
+    np.testing.assert_allclose(m["forces_var"], [1.0, 0.0, 4.0])
+    calls = []
+
+    class MH:
+        config = types.SimpleNamespace(n_burn_in=0, n_inter_steps=2)
+
+        def run_mcmc_steps(self, func, state, params, n_up, n_dn, fixed, n_steps, reevaluate, group=None):
+            calls.append("mcmc")
+            return state
+
+    monkeypatch.setattr(api, "local_energy", lambda *a, **k: (calls.append("E"), torch.tensor([1.0, 3.0]))[1])
+    monkeypatch.setattr(api, "energy_stats", lambda E: torch.tensor([2.0, 1.0, 2.0], dtype=torch.float64))
+
+    def fake_forces(params, r, R, Z, lp, R_cut, R_core, anti):
+        calls.append(("F", R_cut, R_core, anti))
+        return torch.as_tensor(F)
+    monkeypatch.setattr(api, "calculate_forces", fake_forces)
+    params = types.SimpleNamespace(arch=types.SimpleNamespace(n_up=1, n_dn=1))
+    state = types.SimpleNamespace(r=None, R=None, Z=None, log_psi_sqr=None)
+    cfg = EV.ForceEvaluationConfig(R_cut=0.2, use_antithetic_sampling=True)
+    hist, summ, _ = EV.evaluate_wavefunction(params, state, MH(), n_epochs=2, forces=cfg)
+    assert calls == ["mcmc", "E", ("F", 0.2, 0.5, True), "mcmc", "E", ("F", 0.2, 0.5, True)]
+    np.testing.assert_allclose(summ["forces_mean"], [2.0, 2.0, 1.0])
+    assert summ["forces_mean_sigma"].shape == (3,)

@@ -269,7 +269,8 @@ def run_ours(args, rank, world, dev):
             ridge = pk["bf16_tflops"] * 1e12 / (pk["hbm_gbs"] * 1e9)
             # ncu traffic of one captured layer-1 launch, scaled to the average launch by the ratio of
             # algorithmic bytes (DRAM traffic grows in proportion to the rows and K of a launch)
-            cap_traffic, cap_alg = profile_traffic("layer_gemm_h10.txt") if w.name.startswith("h10") else (None, None)
+            prof_file = {"h10": "layer_gemm_h10.txt", "c2h4": "layer_gemm_c2h4.txt"}.get(w.name.split("_")[0])
+            cap_traffic, cap_alg = profile_traffic(prof_file) if prof_file else (None, None)
             traffic = (round(cap_traffic / cap_alg * kt["bytes"] / kt["launches"])
                        if cap_traffic and cap_alg else None)
             if intensity < ridge:
@@ -279,7 +280,7 @@ def run_ours(args, rank, world, dev):
                 roof = {"kernel": kname, "bound": "hbm",
                         "achieved": round(gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                         "frac": round(gbs / pk["hbm_gbs"], 4), "traffic": traffic,
-                        "traffic_source": ("ncu dram read+write of the h_el layer-1 launch (profiles/layer_gemm_h10.txt), "
+                        "traffic_source": (f"ncu dram read+write of an h_el layer launch of this workload (profiles/{prof_file}), "
                                            "scaled to the average launch by algorithmic bytes") if traffic else None,
                         "algorithmic_bytes_per_launch": kt["bytes"] / kt["launches"],
                         "avg_launch_ms": t_launch * 1e3, "tflops": round(tfs, 2),
@@ -390,7 +391,8 @@ def accuracy_vs_fp64(a, mol, state, params, n_fp64, p_dict):
                      "rel_err_quantiles": {q: float(np.quantile(rel, float(q) / 100)) for q in ("50", "99", "99.9")},
                      "frac_walkers_rel_err_le_1e-5": round(float((rel <= 1e-5).mean()), 5)}
     idx = np.argsort(-np.abs(errs["mixed"]))[:3]
-    E_o = O.local_energy(O.tparams(p_dict), a, r[idx].double().cpu().numpy(), mol.R, mol.Z)[0].numpy()
+    R32 = np.asarray(mol.R, np.float32).astype(np.float64)          # the nuclei as the library holds them
+    E_o = O.local_energy(O.tparams(p_dict), a, r[idx].double().cpu().numpy(), R32, mol.Z)[0].numpy()
     out["fp64_form_vs_cpu_oracle_max_abs_mHa"] = float(np.abs(E64.cpu().numpy()[idx] - E_o).max() * 1e3)
     out["fp64_form_vs_cpu_oracle_walkers"] = "the 3 walkers with the largest |E_mixed - E_fp64|"
     return out

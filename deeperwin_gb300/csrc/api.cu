@@ -462,7 +462,7 @@ static int forward_any(const DwArch* a, int precision, const float* P, const voi
     if constexpr (std::is_same<Act, double>::value)
         return fp64_forward_all(a, P, prepared, r, B, R, Z, lp, phase, E, grad, tang, ws, ws_bytes, s, seg, nseg, nullptr);
     else
-        return forward_any<Act>(a, precision, P, prepared, r, B, R, Z, lp, phase, E, grad, tang, ws, ws_bytes, s, seg, nseg);
+        return forward_all<Act>(a, precision, P, prepared, r, B, R, Z, lp, phase, E, grad, tang, ws, ws_bytes, s, seg, nseg);
 }
 
 // Local energies of one or several geometries. Workspace: [forward plan | log psi^2 when not

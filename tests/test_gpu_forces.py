@@ -17,7 +17,8 @@ pytestmark = pytest.mark.gpu
 def test_forces_match_oracle(cuda, mol_fn, K, antithetic):
     mol = mol_fn()
     a = A.arch_for(mol, K)
-    p = P.init_params(a, 2, bias_std=0.1, envelope_jitter=0.1)
+    p = {k: v.astype(np.float32).astype(np.float64) for k, v in P.init_params(a, 2, bias_std=0.1,
+                                                                             envelope_jitter=0.1).items()}
     params = api.Params.from_dict(a, p, "fp64")
     r = A.init_walkers(mol, 64, seed=3).astype(np.float32)
     _, lp = api.log_psi_sqr(params, a.n_up, a.n_dn, r, mol.R, mol.Z)

@@ -22,6 +22,13 @@ pytestmark = pytest.mark.gpu
 GOLDEN = sorted(glob.glob(str(Path(__file__).parent / "golden" / "*.npz")))
 
 
+def _r32(x):
+    """Values as the library holds them: weights, walkers and nuclei are float32."""
+    if isinstance(x, dict):
+        return {k: _r32(v) for k, v in x.items()}
+    return np.asarray(x, np.float64).astype(np.float32).astype(np.float64)
+
+
 def _fixture(f):
     d = np.load(f)
     a = A.Arch(n_el=int(d["n_el"]), n_up=int(d["n_up"]), n_ions=len(d["Z"]), n_dets=int(d["n_dets"]),
@@ -43,18 +50,17 @@ def _scale(r, mol, g, lap):
 
 @pytest.mark.parametrize("f", GOLDEN, ids=lambda f: f.split("/")[-1])
 def test_fp64_forward_matches_reference_golden(cuda, f):
-    """The library takes float32 walkers: against the oracle (pinned to the golden vectors to
-    1e-11) at the float32-rounded positions the FP64 form agrees to float32 rounding of its
-    output; against the golden values at the float64 positions the input rounding adds
-    |grad log psi^2| |dr| (a few 1e-7 relative)."""
+    """The library holds weights, walkers and nuclei in float32: against the oracle (pinned to the
+    golden vectors to 1e-11) on the float32-rounded inputs the FP64 form agrees to float32
+    rounding of its output; against the golden values on the float64 inputs the input rounding
+    adds about 1e-6 relative."""
     d, a, p = _fixture(f)
     params = api.Params.from_dict(a, p, "fp64")
     ph, lp = api.log_psi_sqr(params, a.n_up, a.n_dn, d["r"], d["R"], d["Z"])
     lp = lp.cpu().numpy().astype(np.float64)
-    r32 = d["r"].astype(np.float32).astype(np.float64)
-    ref32 = O.log_psi_sqr(O.tparams(p), a, r32, d["R"], d["Z"])[1].numpy()
+    ref32 = O.log_psi_sqr(O.tparams(_r32(p)), a, _r32(d["r"]), _r32(d["R"]), d["Z"])[1].numpy()
     np.testing.assert_allclose(lp, ref32, rtol=1.2e-7, atol=1e-6)
-    np.testing.assert_allclose(lp, d["log_psi_sqr"], rtol=2e-6, atol=1e-5)
+    np.testing.assert_allclose(lp, d["log_psi_sqr"], rtol=1e-5, atol=1e-5)
     np.testing.assert_array_equal(ph.cpu().numpy(), d["phase"].astype(np.float32))
 
 
@@ -78,8 +84,9 @@ def _molecule(name):
 def test_fp64_local_energy_matches_oracle(cuda, name):
     mol, K, B = _molecule(name)
     a = A.arch_for(mol, K)
-    p = P.init_params(a, 3, bias_std=0.1, envelope_jitter=0.2)
-    r = A.init_walkers(mol, B, seed=21).astype(np.float32).astype(np.float64)     # the library's input precision
+    p = _r32(P.init_params(a, 3, bias_std=0.1, envelope_jitter=0.2))     # the library's input precision
+    r = _r32(A.init_walkers(mol, B, seed=21))
+    mol = A.Molecule(R=_r32(mol.R), Z=mol.Z, n_el=mol.n_el, n_up=mol.n_up, name=mol.name)
     E_ref, lp_ref, g_ref, lap = [x.numpy() for x in O.local_energy(O.tparams(p), a, r, mol.R, mol.Z)]
     S = _scale(r, mol, g_ref, lap)
     kappa = _kappa(p, a, r, mol)
@@ -109,7 +116,7 @@ def test_fp64_mcmc_step_matches_oracle(cuda):
     from tests import philox_ref
     mol = A.lih()
     a = A.arch_for(mol, 8)
-    p = P.init_params(a, 0, bias_std=0.1, envelope_jitter=0.1)
+    p = _r32(P.init_params(a, 0, bias_std=0.1, envelope_jitter=0.1))
     params = api.Params.from_dict(a, p, "fp64")
     state = api.MCMCState.initialize_around_nuclei(64, mol, seed=0)
     r0 = state.r.cpu().numpy().astype(np.float64)

@@ -26,7 +26,8 @@ SEED = 4321
 def test_proposal_step_matches_oracle(cuda, kind, swap, flip):
     mol = A.lih()
     a = A.arch_for(mol, 4)
-    p = P.init_params(a, 0, bias_std=0.1, envelope_jitter=0.1)
+    p = {k: v.astype(np.float32).astype(np.float64) for k, v in P.init_params(a, 0, bias_std=0.1,
+                                                                             envelope_jitter=0.1).items()}
     params = api.Params.from_dict(a, p, "fp64")
     B, step0, stepsize = 128, 3, 0.15
     state = api.MCMCState.initialize_around_nuclei(B, mol, seed=5)

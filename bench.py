@@ -210,7 +210,14 @@ def run_ours(args, rank, world, dev):
             ms = float(t.item())
         return ms, E, clocks, kt, launches[0]
 
+    def guard_stats(reset):
+        v = [ctypes.c_int64() for _ in range(3)]
+        _lib.check(L.dw_guard_stats(*[ctypes.byref(x) for x in v], int(reset)), "dw_guard_stats")
+        return {"walkers": v[0].value, "flagged": v[1].value, "over_capacity": v[2].value}
+
+    guard_stats(True)
     ms, E_mixed, clocks, kt, n_launch = timed(params, args.steps, args.warmup, sample_clocks=True, instrument=True)
+    gs = guard_stats(True)
     value = world * B / (ms / 1e3)
 
     # end to end through the public API with host buffers: H2D of the walkers, D2H of E_L
@@ -301,6 +308,11 @@ def run_ours(args, rank, world, dev):
         }
         if plain:
             out["plain_fp32"] = plain
+        if w.precision == "mixed":
+            # walkers of the local energies (warm-up and timed steps) whose predicted E_L error was
+            # above the tolerance and which were re-evaluated in FP64 inside the mixed form
+            gs["fraction"] = round(gs["flagged"] / max(gs["walkers"], 1), 6)
+            out["tail_reevaluation_fp64"] = gs
     return out, (state, params, a, mol, w)
 
 

@@ -79,6 +79,7 @@ _SIGS = {
     "dw_debug_gemm_bf16": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_int, _P]),
     "dw_debug_tc_error_flag": (ctypes.c_int, []),
+    "dw_debug_set_gemm_bk": (ctypes.c_int, [ctypes.c_int]),
     "dw_debug_slogdet_small": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                               _P, _P, _P, _P]),
     "dw_debug_local_energy_scales": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P,

@@ -200,8 +200,10 @@ static int choose_chunk(const Dims& d, int B, size_t budget = kChunkBudget) {
     const size_t per = std::max<size_t>(two > one ? two - one : one, 1);
     const size_t fixed = one > per ? one - per : 0;
     const size_t avail = budget > fixed ? budget - fixed : per;
-    int bc = (int)std::max<size_t>(1, avail / per);
-    return std::min(bc, B);
+    int bc = std::min((int)std::max<size_t>(1, avail / per), B);
+    // buffers below the 256-byte carve granularity grow unseen in the two-walker estimate
+    while (bc > 1 && carve_plan<Act>(d, bc, nullptr).bytes > budget) bc -= std::max(1, bc / 32);
+    return bc;
 }
 
 // ------------------------------------------------------------------ GEMM dispatch by activation type

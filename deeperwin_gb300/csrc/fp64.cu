@@ -671,8 +671,9 @@ static int choose_chunk64(const Dims& d, int C, int B, size_t budget) {
     const size_t fixed = one > per ? one - per : 0;
     const size_t avail = budget > fixed ? budget - fixed : per;
     // batched GEMMs put the walker on grid.z (at most 65535)
-    const int bc = (int)std::min<size_t>(std::max<size_t>(1, avail / per), 32768);
-    return std::min(bc, B);
+    int bc = std::min((int)std::min<size_t>(std::max<size_t>(1, avail / per), 32768), B);
+    while (bc > 1 && carve64(d, C, bc, nullptr).bytes > budget) bc -= std::max(1, bc / 32);
+    return bc;
 }
 
 static inline unsigned blocks_for(int64_t n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }

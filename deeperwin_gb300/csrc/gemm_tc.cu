@@ -29,7 +29,7 @@ __device__ int g_tc_error = 0;
 
 namespace {
 
-constexpr int BM = 128, BK = 64;
+constexpr int BM = 128;
 constexpr int kEpiWarps = 8;                         // two per TMEM lane quarter
 constexpr int kThreads = 64 + 32 * kEpiWarps;        // producer warp, MMA warp, epilogue warps
 constexpr int CW = 32;                               // columns per epilogue chunk / staged store box
@@ -89,6 +89,15 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(const void* p) {
     uint64_t addr = smem_u32(p);
     return ((addr & 0x3FFFFull) >> 4) | (1ull << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) | (2ull << 61);
 }
+// K-major, 64-byte swizzle (32 BF16 per row), 8-row groups 512 B apart.
+__device__ __forceinline__ uint64_t smem_desc_sw64(const void* p) {
+    uint64_t addr = smem_u32(p);
+    return ((addr & 0x3FFFFull) >> 4) | (1ull << 16) | ((uint64_t)(512 >> 4) << 32) | (1ull << 46) | (4ull << 61);
+}
+// Operand tiles of BK K-columns: 64 -> 128-byte rows, 32 -> 64-byte rows.
+template <int BK> __device__ __forceinline__ uint64_t smem_desc(const void* p) {
+    return BK == 64 ? smem_desc_sw128(p) : smem_desc_sw64(p);
+}
 // Instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, M=128, N.
 __host__ __device__ constexpr uint32_t idesc_bf16(int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
@@ -143,8 +152,8 @@ struct TcArgs {
     int nrb;
 };
 
-// OUT: 0 = fp32 C, 1 = bf16 C, 2 = split-BF16 C.
-template <int NP, int OUT>
+// OUT: 0 = fp32 C, 1 = bf16 C, 2 = split-BF16 C. BK: K-columns per pipeline stage (64 or 32).
+template <int NP, int OUT, int BK>
 __global__ void __launch_bounds__(kThreads, 1)
 k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
           const __grid_constant__ CUtensorMap tmB0, const __grid_constant__ CUtensorMap tmB1,
@@ -236,8 +245,8 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUte
                     const int s = cnt % S;
                     if (!mbar_wait(&full[s], (cnt / S) & 1)) { err = true; break; }
                     tc_fence_after();
-                    const uint64_t a0 = smem_desc_sw128(sA(s, 0)), b0 = smem_desc_sw128(sB(s, 0));
-                    const uint64_t a1 = smem_desc_sw128(sA(s, NP - 1)), b1 = smem_desc_sw128(sB(s, NP - 1));
+                    const uint64_t a0 = smem_desc<BK>(sA(s, 0)), b0 = smem_desc<BK>(sB(s, 0));
+                    const uint64_t a1 = smem_desc<BK>(sA(s, NP - 1)), b1 = smem_desc<BK>(sB(s, NP - 1));
                     #pragma unroll
                     for (int kk = 0; kk < BK / 16; ++kk) {
                         const uint64_t o = (uint64_t)(kk * 2);
@@ -575,7 +584,10 @@ int num_sms() {
 // A: NP parts of a logical [M, lda] activation (NP = 2: [hi | lo] rows of width 2 lda).
 // W0/W1: [N, round_up(K, 64)] K-major weight parts. C: logical [M, ldc].
 // wb != nullptr: walker-block mode (FP32 output, plain epilogue); M is then ignored.
-template <int NP, int OUT>
+// K-columns per stage of the split-BF16 GEMMs (instrumentation: dw_debug_set_gemm_bk).
+int g_split_bk = 64;
+
+template <int NP, int OUT, int BK>
 int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __nv_bfloat16* W1, void* C, int ldc,
               int M, int N, int K, const GemmEpi& epi, int fl, int n3, cudaStream_t s, const WalkerBlocks* wb = nullptr) {
     if (wb) {
@@ -591,16 +603,16 @@ int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __
     const int Kp = round_up(K, 64);
     CUtensorMap ma0, ma1, mb0, mb1, mc0, mc1;
     if (wb) {
-        DW_CHECK(make_map3(&ma0, A, wb->nw, wb->rows, K, (int64_t)NP * lda, wb->a_wstride, 64, 32, 4, false));
-        if (NP == 2) DW_CHECK(make_map3(&ma1, A + lda, wb->nw, wb->rows, K, (int64_t)NP * lda, wb->a_wstride, 64, 32, 4, false));
+        DW_CHECK(make_map3(&ma0, A, wb->nw, wb->rows, K, (int64_t)NP * lda, wb->a_wstride, BK, 32, 4, false));
+        if (NP == 2) DW_CHECK(make_map3(&ma1, A + lda, wb->nw, wb->rows, K, (int64_t)NP * lda, wb->a_wstride, BK, 32, 4, false));
         else ma1 = ma0;
     } else {
-        DW_CHECK(make_map(&ma0, A, M, K, (int64_t)NP * lda, 64, BM, false));
-        if (NP == 2) DW_CHECK(make_map(&ma1, A + lda, M, K, (int64_t)NP * lda, 64, BM, false));
+        DW_CHECK(make_map(&ma0, A, M, K, (int64_t)NP * lda, BK, BM, false));
+        if (NP == 2) DW_CHECK(make_map(&ma1, A + lda, M, K, (int64_t)NP * lda, BK, BM, false));
         else ma1 = ma0;
     }
-    DW_CHECK(make_map(&mb0, W0, N, K, Kp, 64, BN, false));
-    if (NP == 2) DW_CHECK(make_map(&mb1, W1, N, K, Kp, 64, BN, false));
+    DW_CHECK(make_map(&mb0, W0, N, K, Kp, BK, BN, false));
+    if (NP == 2) DW_CHECK(make_map(&mb1, W1, N, K, Kp, BK, BN, false));
     else mb1 = mb0;
     if (wb) {
         DW_CHECK(make_map3(&mc0, C, wb->nw, wb->rows, N, ldc, wb->c_wstride, 32, 32, 1, true));
@@ -628,7 +640,7 @@ int launch_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W0, const __
     a.n_tiles_n = ntn;
     a.n_tiles = mt * ntn;
     size_t smem = (size_t)fixed + (size_t)a.stages * stage_bytes;
-    auto kern = k_gemm_tc<NP, OUT>;
+    auto kern = k_gemm_tc<NP, OUT, BK>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int grid = std::min(a.n_tiles, num_sms());
     kern<<<grid, kThreads, smem, s>>>(ma0, ma1, mb0, mb1, mc0, mc1, a);
@@ -656,18 +668,23 @@ int gemm_tc_wb(int np, const void* A, int lda, const __nv_bfloat16* W0, const __
                const WalkerBlocks& wb, int N, int K, cudaStream_t s) {
     const __nv_bfloat16* a = reinterpret_cast<const __nv_bfloat16*>(A);
     GemmEpi e;
-    if (np == 1) return launch_tc<1, 0>(a, lda, W0, W1, C, ldc, 0, N, K, e, 0, 0, s, &wb);
-    if (np == 2) return launch_tc<2, 0>(a, lda, W0, W1, C, ldc, 0, N, K, e, 0, 0, s, &wb);
+    if (np == 1) return launch_tc<1, 0, 64>(a, lda, W0, W1, C, ldc, 0, N, K, e, 0, 0, s, &wb);
+    if (np == 2 && g_split_bk == 32) return launch_tc<2, 0, 32>(a, lda, W0, W1, C, ldc, 0, N, K, e, 0, 0, s, &wb);
+    if (np == 2) return launch_tc<2, 0, 64>(a, lda, W0, W1, C, ldc, 0, N, K, e, 0, 0, s, &wb);
     return DW_ERR_ARG;
 }
 
 int gemm_tc(int np, int out, const void* A, int lda, const __nv_bfloat16* W0, const __nv_bfloat16* W1, void* C, int ldc,
             int M, int N, int K, const GemmEpi& epi, int fl, int n3, cudaStream_t s) {
     const __nv_bfloat16* a = reinterpret_cast<const __nv_bfloat16*>(A);
-    if (np == 1 && out == 0) return launch_tc<1, 0>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
-    if (np == 1 && out == 1) return launch_tc<1, 1>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
-    if (np == 2 && out == 0) return launch_tc<2, 0>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
-    if (np == 2 && out == 2) return launch_tc<2, 2>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
+    if (np == 1 && out == 0) return launch_tc<1, 0, 64>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
+    if (np == 1 && out == 1) return launch_tc<1, 1, 64>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
+    if (g_split_bk == 32) {
+        if (np == 2 && out == 0) return launch_tc<2, 0, 32>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
+        if (np == 2 && out == 2) return launch_tc<2, 2, 32>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
+    }
+    if (np == 2 && out == 0) return launch_tc<2, 0, 64>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
+    if (np == 2 && out == 2) return launch_tc<2, 2, 64>(a, lda, W0, W1, C, ldc, M, N, K, epi, fl, n3, s);
     return DW_ERR_ARG;
 }
 
@@ -683,6 +700,14 @@ int dw_debug_gemm_bf16(const void* A, int lda, const void* Wt, const void* Wt_lo
     dw::GemmEpi e;
     return dw::gemm_tc(Wt_lo ? 2 : 1, 0, A, lda, (const __nv_bfloat16*)Wt, (const __nv_bfloat16*)Wt_lo, C, ldc, M, N, K,
                        e, 0, 0, (cudaStream_t)stream);
+}
+
+// Instrumentation: K-columns per pipeline stage of the split-BF16 GEMMs (64: two stages of 64 KB at
+// N tiles of 128; 32: four stages of 32 KB). Returns the previous value; other values are ignored.
+int dw_debug_set_gemm_bk(int bk) {
+    const int prev = dw::g_split_bk;
+    if (bk == 32 || bk == 64) dw::g_split_bk = bk;
+    return prev;
 }
 
 // Reads and clears the device-side error flag of the tensor-core kernels (1 = a bounded wait timed out).

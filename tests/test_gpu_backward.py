@@ -68,12 +68,14 @@ def test_backward_matches_oracle_autograd(cuda, case):
         assert err.max() <= 1e-4 * scale, worst
 
 
-def test_backward_matches_central_finite_differences(cuda):
-    """64 random parameters, central differences with h = 1e-3 on the FP64 oracle forward."""
-    mol = A.lih()
-    a = A.arch_for(mol, 4)
+@pytest.mark.parametrize("case", ["lih_k4", "c2h4_k32"])
+def test_backward_matches_central_finite_differences(cuda, case):
+    """64 random parameters, central differences with h = 1e-3 on the FP64 oracle forward; the
+    C2H4-shaped case is the differentiation form's own shape (16 electrons, 32 determinants)."""
+    mol, K = (A.lih(), 4) if case == "lih_k4" else (A.c2h4_shaped(), 32)
+    a = A.arch_for(mol, K)
     p = P.init_params(a, 5, bias_std=0.1, envelope_jitter=0.2)
-    r = A.init_walkers(mol, 4, seed=8)
+    r = A.init_walkers(mol, 4, seed=8).astype(np.float32).astype(np.float64)
     coeff = np.array([0.7, -1.1, 0.4, 0.25])
     params = api.Params.from_dict(a, p, "mixed")
     g = vmc.log_psi_sqr_backward(params, torch.tensor(r, dtype=torch.float32), mol.R, mol.Z,

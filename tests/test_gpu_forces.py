@@ -27,7 +27,10 @@ def test_forces_match_oracle(cuda, mol_fn, K, antithetic):
     ref = O.forces(O.tparams(p), a, r.astype(np.float64), mol.R.astype(np.float32).astype(np.float64), mol.Z,
                    lp.double().cpu().numpy(), 0.1, 0.5, antithetic).numpy()
     scale = np.abs(pw.cpu().numpy()).max()
-    np.testing.assert_allclose(F.cpu().numpy(), ref, rtol=1e-6, atol=1e-9 * scale + 1e-9)
+    # antithetic: the mirror images are formed in float32 and their weights exp(log psi^2(mirror) -
+    # log psi^2) inherit the float32 rounding of both log psi^2 values (about 5e-6 at |log psi^2| ~ 80)
+    rtol, atol = (1e-4, 1e-5 * scale) if antithetic else (1e-6, 1e-9 * scale + 1e-9)
+    np.testing.assert_allclose(F.cpu().numpy(), ref, rtol=rtol, atol=atol)
     # F minus the batch mean of the per-walker forces is the nucleus-nucleus repulsion
     R64 = mol.R.astype(np.float32).astype(np.float64)
     Z = np.asarray(mol.Z, np.float64)

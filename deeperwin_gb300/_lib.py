@@ -11,7 +11,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "csrc" / "libdwgb.so"
 
-DW_PRECISION = {"fp32": 0, "plain": 0, "mixed": 1, "bf16": 2, "fp64": 3}
+DW_PRECISION = {"fp32": 0, "plain": 0, "mixed": 1, "bf16": 2, "fp64": 3, "fp32_det64": 4}
 
 
 class DwArch(ctypes.Structure):

@@ -306,11 +306,14 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         GemmEpi e3; e3.rowbias = p.WB; e3.ldrb = d.D; e3.Tp = d.Tp; e3.rows_per_walker = d.n * d.Tp; e3.act = tang ? 0 : 1;
         WRef wm = wref(pre.main[l], d.D, &pre.main_bf[0][0], l);
         if (tang) {
-            // algorithmic work of this launch: 2 M N K with the unpadded K, A and C streamed once
+            // algorithmic work of this launch: 2 M N K over the T = 3n + 2 channel rows of each
+            // electron (not the Tp - T zero padding rows the launch also moves) and the unpadded K,
+            // A and C streamed once
             const double kreal = hw + d.E + d.eiw[l];
-            const double flops = 2.0 * rows * d.D * kreal;
+            const double rows_alg = (double)Bc * d.n * d.T;
+            const double flops = 2.0 * rows_alg * d.D * kreal;
             const double esz = (double)sizeof(Act) * ActIO<Act>::kParts;
-            const double bytes = (double)rows * (kreal + d.D) * esz + kreal * d.D * esz;
+            const double bytes = rows_alg * (kreal + d.D) * esz + kreal * d.D * esz;
             timer_begin("layer_gemm", s);
             DW_CHECK(MM<Act>::mm_fl(xin, ldin, wm, xout, kXW, rows, d.D, d.kw[l], e3, d, p.Zb, s));
             timer_end("layer_gemm", s, flops, bytes);
@@ -352,9 +355,18 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         DW_TIMED("backflow_gemm", DW_CHECK(MM<Act>::mm(H, kXW, wb, p.BF, ldbf, rows, 2 * d.KN, d.D, e0, s)));
     }
     DW_TIMED("envelope", launch_envelope(r, R, Z, P, L, pre.sp_alpha, d, Bc, p.BF, ldbf, spin_cols, p.MO, s));
-    if (precision == DW_PRECISION_FP32) DW_TIMED("slogdet", launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
-    else DW_TIMED("slogdet", launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
-    if (tang) DW_TIMED("det_tangents", launch_det_tangents(p.MO, p.Ainv, p.sign, d, Bc, p.g, p.lapdet, s));
+    if (precision == DW_PRECISION_FP32_DET64 && tang) {
+        // FP64 LU, inverse and tangent traces of the FP32 Slater channels; the widened channels use
+        // the backflow buffer (consumed by the envelope kernel, at least twice the Slater channels'
+        // size) and the inverses the layer buffer XA (the embedding H is in XB)
+        DW_TIMED("det_tangents", DW_CHECK(fp64_dets_from_f32(p.MO, d, Bc, reinterpret_cast<double*>(p.BF),
+                                                             reinterpret_cast<double*>(p.XA), p.logdet, p.sign, p.g,
+                                                             p.lapdet, s)));
+    } else {
+        if (precision == DW_PRECISION_FP32) DW_TIMED("slogdet", launch_slogdet<float>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
+        else DW_TIMED("slogdet", launch_slogdet<double>(p.MO, d, Bc, p.logdet, p.sign, p.Ainv, s));
+        if (tang) DW_TIMED("det_tangents", launch_det_tangents(p.MO, p.Ainv, p.sign, d, Bc, p.g, p.lapdet, s));
+    }
     // Jastrow MLP([64, 64, 1]) on the final embedding
     GemmEpi j0; j0.bias = P + L.jas_b[0]; j0.Tp = d.Tp; j0.rows_per_walker = d.n * d.Tp; j0.act = tang ? 0 : 1;
     GemmEpi j1 = j0; j1.bias = P + L.jas_b[1];
@@ -381,6 +393,7 @@ template <class F>
 static int with_act(int precision, bool need_device, F&& f) {
     switch (precision) {
         case DW_PRECISION_FP32: return f((float*)nullptr);
+        case DW_PRECISION_FP32_DET64: return f((float*)nullptr);
         case DW_PRECISION_FP64: return f((double*)nullptr);
         case DW_PRECISION_MIXED:
             if (need_device && !tc_available()) return DW_ERR_UNSUPPORTED;
@@ -500,6 +513,16 @@ static int local_energy_impl(const DwArch* a, int precision, const float* params
     });
 }
 
+// Local energy of the plain FP32 network with FP64 determinant algebra (DW_PRECISION_FP32_DET64)
+// on a caller region: the mixed form's re-evaluation of flagged walkers (guard.cu).
+size_t det64_plan_bytes(const DwArch* a, int B) { return plan_bytes<float>(a, B, true); }
+int det64_local_energy(const DwArch* a, const float* P, const void* prepared, const float* r, int B, const float* R,
+                       const int32_t* Z, const int32_t* seg, int nseg, float* E, float* lp, float* grad, void* ws,
+                       size_t wsb, cudaStream_t s) {
+    return forward_all<float>(a, DW_PRECISION_FP32_DET64, P, prepared, r, B, R, Z, lp, nullptr, E, grad, true, ws, wsb,
+                              s, seg, nseg);
+}
+
 // FP32 row-gathered layer weights of a prepared buffer (the same offsets in every precision form).
 void prepared_fp32_layers(const DwArch* a, const void* prepared, const float* main[4], const float* mean[4]) {
     Prepared p = carve_prepared(a, DW_PRECISION_FP32, const_cast<void*>(prepared));
@@ -546,7 +569,7 @@ int dw_prepare_params(const DwArch* a, int precision, const float* params, void*
     reset_launch_count();
     DW_CHECK(check_arch(a));
     if (!params || !prepared) return DW_ERR_ARG;
-    if (precision < DW_PRECISION_FP32 || precision > DW_PRECISION_FP64) return DW_ERR_ARG;
+    if (precision < DW_PRECISION_FP32 || precision > DW_PRECISION_FP32_DET64) return DW_ERR_ARG;
     return prepare(a, precision, params, prepared, bytes, (cudaStream_t)stream);
 }
 

@@ -774,6 +774,38 @@ static int run_chunk64(const Plan64& p, const Dims& d0, int Bc, const float* P, 
     return DW_OK;
 }
 
+// FP64 determinant algebra on float32 Slater-matrix channels MO[b][k][t][i][o] (t < d.T): the
+// channels are widened to FP64 in MO64, then the FP64 LU / Gauss-Jordan inverse and the FP64
+// determinant tangents of this file give log|det|, sign, the gradient traces and the Laplacian
+// term. Used by the plain form's FP64-determinant variant.
+__global__ void k64_widen(const float* __restrict__ x, int64_t n, double* __restrict__ y) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = (double)x[i];
+}
+
+int fp64_dets_from_f32(const float* MO, const Dims& d, int Bc, double* MO64, double* Ainv64, double* logdet,
+                       double* sign, double* g, double* lapdet, cudaStream_t s) {
+    Run64 q;
+    q.d = d; q.C = d.T; q.B = Bc; q.nvalid = nullptr;
+    const int n = d.n, nmat = Bc * d.K;
+    const int64_t ne = (int64_t)nmat * d.T * n * n;
+    k64_widen<<<(unsigned)std::min<int64_t>((ne + 255) / 256, 152 * 32), 256, 0, s>>>(MO, ne, MO64);
+    count_launch();
+    const bool tang = d.T > 1;
+    const size_t sm_lu = ((size_t)n * (2 * n + 1) + n) * sizeof(double);
+    if (sm_lu > 48 * 1024) cudaFuncSetAttribute(k64_slogdet_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_lu);
+    k64_slogdet_inv<<<nmat, 128, sm_lu, s>>>(MO64, q, logdet, sign, tang ? Ainv64 : nullptr);
+    count_launch();
+    if (tang) {
+        const size_t sm_t = (size_t)3 * n * n * sizeof(double);
+        if (sm_t > 48 * 1024) cudaFuncSetAttribute(k64_det_tangents, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_t);
+        k64_det_tangents<<<nmat, 128, sm_t, s>>>(MO64, Ainv64, sign, q, g, lapdet);
+        count_launch();
+    }
+    DW_CHECK_CUDA(cudaGetLastError());
+    return DW_OK;
+}
+
 int fp64_max_chunk(const DwArch* a, bool tang) {
     Dims d = make_dims(a, tang);
     const int C = tang ? 3 * d.n + 2 : 1;

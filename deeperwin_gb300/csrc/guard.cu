@@ -1,4 +1,4 @@
-// FP64 re-evaluation of the ill-conditioned tail of the mixed form's local energies.
+// Re-evaluation of the ill-conditioned tail of the mixed form's local energies.
 //
 // The split-BF16 GEMMs of the mixed form carry about 2^-16 relative error per Slater-matrix entry;
 // the forward Laplacian turns entry errors into E_L errors amplified by the cancellations of the
@@ -6,10 +6,9 @@
 // of the sum). For nearly all walkers that stays below a mHa; for the walkers near a node of the
 // wavefunction it reaches Hartrees and dominates the mean energy. The combine kernel reports per
 // walker the magnitude of the terms it cancels; walkers whose predicted error (that magnitude
-// times the form's relative entry accuracy) exceeds a threshold are gathered, re-evaluated by the
-// FP64 form (fp64.cu) in one launch sequence sized by a device-side count (no host
-// synchronisation: kernels skip the unused capacity), and their E_L, log psi^2 and gradient are
-// scattered back. The selection depends only on each walker's own scales, so a walker gets the
+// times the form's relative entry accuracy) exceeds a threshold are gathered into a fixed-capacity
+// sub-batch (no host synchronisation), re-evaluated with FP64 determinant algebra, and their E_L,
+// log psi^2 and gradient are scattered back. The selection depends only on each walker's own scales, so a walker gets the
 // same result in any batch as long as the flagged walkers fit the capacity; beyond it the walkers
 // with the largest predicted errors are taken.
 #include "net.cuh"
@@ -22,11 +21,17 @@ __device__ unsigned long long g_guard_walkers = 0, g_guard_flagged = 0, g_guard_
 // Predicted E_L error of a mixed-form walker: kGuardRel times the largest magnitude the combine
 // kernel cancels (the determinant terms of the Laplacian of log|psi~|, or the terms of E_L). On
 // C2H4-shaped walkers (16 electrons, 32 determinants) the measured |E_mixed - E_FP64| / that
-// magnitude has median 1.7e-6 and 99th percentile 1.5e-5; walkers predicted above kGuardTol are
-// re-evaluated. With these values about 0.5 % of equilibrated walkers are flagged and the mean
-// E_L over 2,048 walkers moves from +1.37 mHa to within 0.03 mHa of the FP64 form.
+// magnitude has median 1.7e-6 and 99th percentile 1.5e-5 (2e-5 to 5e-5 after optimisation steps).
+// Walkers predicted above kGuardTol (magnitude above 2,000 Ha) are re-evaluated, those of the
+// largest magnitudes first when more than the capacity (1 / 32 of the batch) are flagged.
 constexpr float kGuardRel = 1.5e-5f;
-constexpr float kGuardTol = 0.5f;
+constexpr float kGuardTol = 0.03f;
+// Re-evaluation form: the plain FP32 network with FP64 determinant algebra (LU, inverse, tangent
+// traces). The catastrophic errors of ill-conditioned walkers come from the determinant algebra:
+// on 4,096 C2H4-shaped walkers near the initial weights the plain FP32 form is off by up to 14 Ha,
+// the same network with FP64 determinants by at most 95 mHa (mean 0.03 mHa), at about 1.5x the
+// plain form's cost per walker. The FP64 form (fp64.cu) would cost about 15x more per walker.
+constexpr bool kGuardFp64 = false;
 
 // Sort key of a walker (larger = re-evaluate first); NaN scales rank first.
 __device__ __forceinline__ float guard_key(const float* sc) {
@@ -97,13 +102,15 @@ k_guard_select(const float* __restrict__ esc, int B, float rel, float tol, int c
     }
 }
 
+// Flagged walkers into the sub-batch; with fill = 1 the unused slots get a copy of walker 0 (a
+// valid configuration for passes that run over the whole capacity).
 __global__ void k_guard_gather(const float* __restrict__ r, const int32_t* __restrict__ seg, const int* __restrict__ idx,
                                const int* __restrict__ counts, int n3, float* __restrict__ r_sub,
-                               int32_t* __restrict__ seg_sub, int cap) {
+                               int32_t* __restrict__ seg_sub, int cap, int fill) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int k = (int)(e / n3), c = (int)(e % n3);
-    if (k >= cap || k >= counts[0]) return;
-    const int b = idx[k];
+    if (k >= cap || (!fill && k >= counts[0])) return;
+    const int b = k < counts[0] ? idx[k] : 0;
     r_sub[(int64_t)k * n3 + c] = r[(int64_t)b * n3 + c];
     if (seg && c == 0) seg_sub[k] = seg[b];
 }
@@ -124,10 +131,11 @@ __global__ void k_guard_scatter(const float* __restrict__ E_sub, const float* __
 }
 
 int guard_capacity(const DwArch* a, int B) {
-    // up to 1 / 64 of the batch (at least 16), limited to one chunk of the FP64 form (the
-    // device-side walker count needs the flagged walkers in one launch sequence)
-    const int want = std::min(B, std::max(16, (B + 63) / 64));
-    return std::max(1, std::min(want, fp64_max_chunk(a, true)));
+    // up to 1 / 32 of the batch (at least 16); the FP64 form needs the flagged walkers in one chunk
+    // (its kernels skip the unused capacity through the device-side count), the FP32 network with
+    // FP64 determinants runs over the whole capacity (unused slots hold a copy of walker 0)
+    const int want = std::min(B, std::max(16, (B + 31) / 32));
+    return kGuardFp64 ? std::max(1, std::min(want, fp64_max_chunk(a, true))) : want;
 }
 
 struct GuardPlan {
@@ -149,7 +157,7 @@ static GuardPlan carve_guard(const DwArch* a, int B, void* ws) {
     g.E_sub = c.take<float>((size_t)g.cap);
     g.lp_sub = c.take<float>((size_t)g.cap);
     g.g_sub = c.take<float>((size_t)g.cap * n3);
-    g.fp64_bytes = fp64_plan_bytes(a, g.cap, true);
+    g.fp64_bytes = kGuardFp64 ? fp64_plan_bytes(a, g.cap, true) : det64_plan_bytes(a, g.cap);
     g.fp64_ws = c.take<unsigned char>(g.fp64_bytes);
     g.bytes = c.used + 256;
     return g;
@@ -167,10 +175,15 @@ int tail_guard(const DwArch* a, const float* P, const void* prepared, const floa
     count_launch();
     const int64_t ne = (int64_t)g.cap * n3;
     k_guard_gather<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(r, seg, g.idx, g.counts, n3, g.r_sub,
-                                                                 seg ? g.seg_sub : nullptr, g.cap);
+                                                                 seg ? g.seg_sub : nullptr, g.cap, kGuardFp64 ? 0 : 1);
     count_launch();
-    DW_CHECK(fp64_forward_all(a, P, prepared, g.r_sub, g.cap, R, Z, g.lp_sub, nullptr, g.E_sub, grad ? g.g_sub : nullptr,
-                              true, g.fp64_ws, g.fp64_bytes, s, seg ? g.seg_sub : nullptr, nseg, g.counts));
+    if (kGuardFp64)
+        DW_CHECK(fp64_forward_all(a, P, prepared, g.r_sub, g.cap, R, Z, g.lp_sub, nullptr, g.E_sub,
+                                  grad ? g.g_sub : nullptr, true, g.fp64_ws, g.fp64_bytes, s, seg ? g.seg_sub : nullptr,
+                                  nseg, g.counts));
+    else
+        DW_CHECK(det64_local_energy(a, P, prepared, g.r_sub, g.cap, R, Z, seg ? g.seg_sub : nullptr, nseg, g.E_sub,
+                                    g.lp_sub, grad ? g.g_sub : nullptr, g.fp64_ws, g.fp64_bytes, s));
     k_guard_scatter<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(g.E_sub, g.lp_sub, g.g_sub, g.idx, g.counts, n3, g.cap,
                                                                   E, lp, grad);
     count_launch();

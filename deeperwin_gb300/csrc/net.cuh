@@ -138,9 +138,19 @@ void prepared_fp32_layers(const DwArch* a, const void* prepared, const float* ma
 // *nvalid are skipped; it requires the walkers to fit one chunk.
 size_t fp64_plan_bytes(const DwArch* a, int B, bool tang);
 int fp64_max_chunk(const DwArch* a, bool tang);     // walkers of one FP64 chunk
+// FP64 LU, inverse and determinant tangents of float32 Slater channels (MO layout of the forward
+// plans, d.T channels); MO64 holds Bc K T n^2 doubles, Ainv64 Bc K n^2.
+int fp64_dets_from_f32(const float* MO, const Dims& d, int Bc, double* MO64, double* Ainv64, double* logdet,
+                       double* sign, double* g, double* lapdet, cudaStream_t s);
 int fp64_forward_all(const DwArch* a, const float* P, const void* prepared, const float* r, int B, const float* R,
                      const int32_t* Z, float* lp, float* phase, float* E, float* grad, bool tang, void* ws,
                      size_t ws_bytes, cudaStream_t s, const int32_t* seg, int nseg, const int* nvalid);
+
+// api.cu: the plain network with FP64 determinant algebra on a caller region
+size_t det64_plan_bytes(const DwArch* a, int B);
+int det64_local_energy(const DwArch* a, const float* P, const void* prepared, const float* r, int B, const float* R,
+                       const int32_t* Z, const int32_t* seg, int nseg, float* E, float* lp, float* grad, void* ws,
+                       size_t wsb, cudaStream_t s);
 
 // guard.cu: FP64 re-evaluation of the mixed form's flagged walkers (esc: per-walker error scales
 // written by the combine kernel, 3 floats per walker)

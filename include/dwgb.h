@@ -60,11 +60,14 @@ enum DwPrecision {
     DW_PRECISION_MIXED = 1, /* tensor-core GEMMs on split-BF16 operands (hi + lo, three BF16 MMAs per
                                K step, FP32 accumulate) + FP64 LU / trace / reductions */
     DW_PRECISION_BF16 = 2,  /* single-pass BF16 tensor-core GEMMs + FP64 LU (fastest, least accurate) */
-    DW_PRECISION_FP64 = 3   /* FP64 end to end: every GEMM, activation, envelope, LU, inverse, determinant
+    DW_PRECISION_FP64 = 3,  /* FP64 end to end: every GEMM, activation, envelope, LU, inverse, determinant
                                tangent, Coulomb sum and reduction in double (the reference's
                                float_precision: float64 mode, configuration.py:1893 and
                                process_molecule.py:20-29); outputs are rounded to float32. Forward,
                                local energy and MCMC only (no parameter gradient) */
+    DW_PRECISION_FP32_DET64 = 4 /* plain FP32 network (CUDA-core GEMMs) with the determinant algebra in
+                                   FP64: LU, Gauss-Jordan inverse and tangent traces of the FP32 Slater
+                                   channels. Forward, local energy and MCMC (no parameter gradient) */
 };
 
 /* Human-readable text for a status code (static storage). */

@@ -424,3 +424,16 @@ def test_split_gemm_stage_depths_agree_on_local_energy(cuda, le_cases):
             L.dw_debug_set_gemm_bk(prev)
         out[bk] = E.cpu().numpy().astype(np.float64)
     assert np.all(np.abs(out[32] - out[64]) <= 1e-6 * S + 1e-5), (out[32], out[64])
+
+
+@pytest.mark.parametrize("name", ["lih", "h6", "h10"])
+def test_local_energy_fp32_network_fp64_determinants(cuda, le_cases, name):
+    """DW_PRECISION_FP32_DET64 (the mixed form's re-evaluation of flagged walkers): the plain FP32
+    network with FP64 LU, inverse and tangent traces, held to the plain form's tolerance."""
+    mol, a, p, r, E_ref, lp_ref, g_ref, S = le_cases[name]
+    params = api.Params.from_dict(a, p, "fp32_det64")
+    E, lp, g = api.local_energy(params, (a.n_up, a.n_dn), r, mol.R, mol.Z, return_grad=True)
+    E = E.cpu().numpy().astype(np.float64)
+    np.testing.assert_allclose(lp.cpu().numpy(), lp_ref, rtol=1e-5, atol=1e-4)
+    np.testing.assert_allclose(g.cpu().numpy(), g_ref, rtol=1e-4, atol=1e-3 * np.abs(g_ref).max())
+    assert np.all(np.abs(E - E_ref) <= 5e-5 * S), (E, E_ref, S)

@@ -244,6 +244,8 @@ def run_ours(args, rank, world, dev):
     e2e = {"value": world * B / (ms_e2e / 1e3), "unit": "walker-evals/s",
            "h2d_bytes_per_step": int(r_host.numel() * 4), "d2h_bytes_per_step": int(B * 4)}
 
+    # walkers of the mixed chain at its current weights (the plain leg below moves the shared chain)
+    r_mixed = state.r.clone()
     plain = None
     if not args.no_plain and w.precision != "fp32":
         # with parameter updates the plain form optimises its own copy of the weights
@@ -253,8 +255,8 @@ def run_ours(args, rank, world, dev):
         # same walkers and weights through both forms: accuracy of the mixed form against plain
         # FP32 on the full batch
         pcmp = params.with_precision("fp32") if w.backward else pparams
-        E_m = api.local_energy(params, spin, state.r, state.R, state.Z).double()
-        E_p = api.local_energy(pcmp, spin, state.r, state.R, state.Z).double()
+        E_m = api.local_energy(params, spin, r_mixed, state.R, state.Z).double()
+        E_p = api.local_energy(pcmp, spin, r_mixed, state.R, state.Z).double()
         d = (E_m - E_p)
         ad = d.abs().cpu().numpy() * 1e3
         plain = {"value": world * B / (ms_p / 1e3), "ms_per_step": ms_p,
@@ -313,7 +315,7 @@ def run_ours(args, rank, world, dev):
             # above the tolerance and which were re-evaluated in FP64 inside the mixed form
             gs["fraction"] = round(gs["flagged"] / max(gs["walkers"], 1), 6)
             out["tail_reevaluation_fp64"] = gs
-    return out, (state, params, a, mol, w)
+    return out, (state, params, a, mol, w, r_mixed)
 
 
 def ours_config(w, mol, a, B, world):
@@ -373,15 +375,15 @@ def cpu_baseline(args, a, mol, r_sample, backward, p_dict=None):
                       f"{dt:.1f} s"}
 
 
-def accuracy_vs_fp64(a, mol, state, params, n_fp64, p_dict):
+def accuracy_vs_fp64(a, mol, r_all, state, params, n_fp64, p_dict):
     """Both production forms against the FP64 form on the GPU over the whole batch (or its first
-    n_fp64 walkers), at the weights the run ends with; the FP64 form itself is checked against
-    the CPU FP64 oracle on the walkers where the mixed form is furthest from it."""
+    n_fp64 walkers) of the mixed chain, at the weights the run ends with; the FP64 form itself is
+    checked against the CPU FP64 oracle on the walkers where the mixed form is furthest from it."""
     import torch
     from deeperwin_gb300 import api
     from oracle import dpe4 as O
     spin = (a.n_up, a.n_dn)
-    r = state.r[:n_fp64].contiguous()
+    r = r_all[:n_fp64].contiguous()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     E64 = api.local_energy(params.with_precision("fp64"), spin, r, state.R, state.Z).double()
@@ -466,12 +468,12 @@ def main():
     out, ctx = run_ours(args, rank, world, dev)
     if rank == 0:
         from deeperwin_gb300 import params as P
-        state, params, a, mol, w = ctx
+        state, params, a, mol, w, r_mixed = ctx
         # the checks evaluate the weights the GPU holds now (updated ones after optimisation steps)
         p_now = P.unpack(a, params.flat.detach().cpu().numpy())
         if w.precision != "fp32" and not args.no_plain:
             n64 = args.fp64_walkers or (1024 if a.n_el > 30 else state.r.shape[0])
-            out["accuracy_vs_fp64"] = accuracy_vs_fp64(a, mol, state, params, min(n64, state.r.shape[0]), p_now)
+            out["accuracy_vs_fp64"] = accuracy_vs_fp64(a, mol, r_mixed, state, params, min(n64, state.r.shape[0]), p_now)
         if not args.no_cpu_baseline:
             r_sample = state.r[:32].double().cpu().numpy()
             out["cpu_baseline"] = cpu_baseline(args, a, mol, r_sample, w.backward, p_now)

@@ -40,9 +40,11 @@ __device__ __forceinline__ float guard_key(const float* sc) {
 }
 
 // Flagged walkers into idx[0 .. min(count, cap)), in walker order (one block, deterministic).
-// When more than cap are flagged, the cap walkers with the largest keys are taken: the smallest
-// key threshold t (float bit pattern, binary search) with #{key >= t} <= cap. counts[0] = walkers
-// to re-evaluate, counts[1] = walkers flagged.
+// When more than cap are flagged, the walkers with the largest keys are taken: t is the smallest key
+// (float bit pattern, binary search) with #{key >= t} <= cap; the walkers with key >= t come first
+// and walkers whose key equals the next lower bit pattern (ties, including NaN scales ranked as
+// infinity) fill the remaining slots in walker order. counts[0] = walkers to re-evaluate,
+// counts[1] = walkers flagged.
 __global__ void __launch_bounds__(1024)
 k_guard_select(const float* __restrict__ esc, int B, float rel, float tol, int cap, int* __restrict__ idx,
                int* __restrict__ counts) {
@@ -50,10 +52,11 @@ k_guard_select(const float* __restrict__ esc, int B, float rel, float tol, int c
     __shared__ int base;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint32_t thr_flag = __float_as_uint(tol / rel);
+    auto key_bits = [&](int b) { return __float_as_uint(guard_key(esc + 3 * (int64_t)b)); };
     // block-wide count of walkers whose key bits are >= t
     auto count_ge = [&](uint32_t t) {
         int c = 0;
-        for (int b = threadIdx.x; b < B; b += blockDim.x) c += __float_as_uint(guard_key(esc + 3 * (int64_t)b)) >= t;
+        for (int b = threadIdx.x; b < B; b += blockDim.x) c += key_bits(b) >= t;
         c = __reduce_add_sync(0xffffffffu, c);
         __syncthreads();
         if (lane == 0) warp_tot[wid] = c;
@@ -62,48 +65,57 @@ k_guard_select(const float* __restrict__ esc, int B, float rel, float tol, int c
         for (int w = 0; w < nw; ++w) tot += warp_tot[w];
         return tot;
     };
+    // appends the walkers selected by `pick` in walker order while slots are left
+    auto compact = [&](auto pick) {
+        for (int b0 = 0; b0 < B; b0 += blockDim.x) {
+            const int b = b0 + threadIdx.x;
+            const bool f = b < B && pick(b);
+            const unsigned m = __ballot_sync(0xffffffffu, f);
+            if (lane == 0) warp_tot[wid] = __popc(m);
+            __syncthreads();
+            int off = base;
+            for (int w = 0; w < wid; ++w) off += warp_tot[w];
+            const int pos = off + __popc(m & ((1u << lane) - 1u));
+            if (f && pos < cap) idx[pos] = b;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int tt = 0;
+                for (int w = 0; w < nw; ++w) tt += warp_tot[w];
+                base += tt;
+            }
+            __syncthreads();
+        }
+    };
     // keys are non-negative floats: their bit patterns order as the values
     uint32_t t = thr_flag + 1u;                       // key > tol / rel
     const int flagged = count_ge(t);
+    bool fill = false;
     if (flagged > cap) {
         uint32_t lo = t, hi = 0x7F800001u;            // count_ge(hi) = 0 <= cap
         while (lo < hi) {
             const uint32_t mid = lo + (hi - lo) / 2;
             if (count_ge(mid) <= cap) hi = mid; else lo = mid + 1;
         }
+        fill = lo > t;                                // count_ge(lo - 1) > cap: ties at lo - 1
         t = lo;
     }
     if (threadIdx.x == 0) base = 0;
     __syncthreads();
-    for (int b0 = 0; b0 < B; b0 += blockDim.x) {
-        const int b = b0 + threadIdx.x;
-        const bool f = b < B && __float_as_uint(guard_key(esc + 3 * (int64_t)b)) >= t;
-        const unsigned m = __ballot_sync(0xffffffffu, f);
-        if (lane == 0) warp_tot[wid] = __popc(m);
-        __syncthreads();
-        int off = base;
-        for (int w = 0; w < wid; ++w) off += warp_tot[w];
-        const int pos = off + __popc(m & ((1u << lane) - 1u));
-        if (f && pos < cap) idx[pos] = b;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int tt = 0;
-            for (int w = 0; w < nw; ++w) tt += warp_tot[w];
-            base += tt;
-        }
-        __syncthreads();
+    compact([&](int b) { return key_bits(b) >= t; });
+    if (fill) {
+        const uint32_t tie = t - 1u;
+        compact([&](int b) { return key_bits(b) == tie; });
     }
     if (threadIdx.x == 0) {
-        counts[0] = min(base, cap);
+        const int sel = min(base, cap);
+        counts[0] = sel;
         counts[1] = flagged;
         atomicAdd(&g_guard_walkers, (unsigned long long)B);
         atomicAdd(&g_guard_flagged, (unsigned long long)flagged);
-        if (flagged > cap) atomicAdd(&g_guard_overflow, (unsigned long long)(flagged - min(base, cap)));
+        if (flagged > sel) atomicAdd(&g_guard_overflow, (unsigned long long)(flagged - sel));
     }
 }
 
-// Flagged walkers into the sub-batch; with fill = 1 the unused slots get a copy of walker 0 (a
-// valid configuration for passes that run over the whole capacity).
 __global__ void k_guard_gather(const float* __restrict__ r, const int32_t* __restrict__ seg, const int* __restrict__ idx,
                                const int* __restrict__ counts, int n3, float* __restrict__ r_sub,
                                int32_t* __restrict__ seg_sub, int cap, int fill) {

@@ -3,7 +3,8 @@
 A request asks for an energy estimate (``kind="energy"``: ``n_steps`` Metropolis-Hastings steps of
 ``n_walkers`` walkers initialised around the nuclei, then E_L of every walker and its FP64 mean and
 variance) or one optimisation step (``kind="opt_step"``: the same, then the clipped VMC gradient of
-the request's own copy of the weights and an SGD update of that copy). It is the per-geometry work
+the request's own copy of the weights and the first Adam update of that copy, from a fresh optimiser
+state, as the VMC optimisation step makes it). It is the per-geometry work
 of the reference's optimisation / evaluation loops (optimization/variational_optimization.py:139-186,
 optimization/evaluation.py:143-201: MCMC inter-steps, get_local_energy, value_and_grad), served for
 many geometries at once, which the reference does not do.
@@ -41,7 +42,7 @@ from typing import Deque, Dict, List, Optional, Sequence, Tuple
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, optim
 from .api import MCMCConfig, Params, _ptr
 from .arch import Arch, Molecule, init_walkers, random_molecule
 from .params import init_params, pack, slice_shared
@@ -60,7 +61,7 @@ class Request:
     kind: str = "energy"          # "energy" | "opt_step"
     arrival: float = 0.0          # seconds after the start of the stream
     seed: int = 0
-    lr: float = 1e-3              # SGD step of kind="opt_step"
+    lr: float = 1e-3              # Adam learning rate of kind="opt_step" (a fresh optimiser state)
     keep_walkers: bool = False    # keep the final walkers and E_L on the device in the result
 
 
@@ -386,7 +387,7 @@ class ServingEngine:
         self.launches += int(_lib.lib().dw_last_launch_count())
 
     def _opt_step(self, g: _Group, m: _State, E: torch.Tensor) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
-        """Clipped VMC gradient of the request's own (unpadded) weight copy and its SGD update
+        """Clipped VMC gradient of the request's own (unpadded) weight copy and its Adam update
         (loss_function.py:75-156 with tanh clipping, center = mean, width = clip_by * std of this batch)."""
         L = _lib.lib()
         mol = m.req.mol
@@ -414,7 +415,9 @@ class ServingEngine:
                                              _ptr(r), nw, _ptr(Rt), _ptr(Zt), _ptr(coeff), _ptr(grad), _ptr(ws),
                                              nbytes, ctypes.c_void_p(g.stream.cuda_stream)),
                    "dw_log_psi_sqr_backward")
-        new = prm.flat - m.req.lr * grad
+        # optax.adam of the VMC step (opt_utils.py:73-76), first update, on a copy of the weights
+        new = prm.flat.clone()
+        optim.Adam(new, learning_rate=m.req.lr).update_(new, grad)
         return grad, new, cs[0]
 
     def _issue(self, g: _Group) -> bool:

@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--walkers", type=int, default=0, help="override walker count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--breakdown", action="store_true",
+                    help="after the measurements, time two more steps by phase and by library timer tag")
     return ap.parse_args()
 
 
@@ -148,11 +150,20 @@ def run_ours(args, rank, world, dev):
     clip_state = [vmc.init_clipping_state()]
     optimizers = {}
 
-    def step(prm):
+    def mark(marks):
+        if marks is not None:
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record()
+            marks.append(ev)
+
+    def step(prm, marks=None):
+        mark(marks)
         mh.run_mcmc_steps(None, state, prm, a.n_up, a.n_dn, None, n_steps=n_mh, reevaluate=True)
         launches[0] += api.last_launch_count()
+        mark(marks)
         E = api.local_energy(prm, spin, state.r, state.R, state.Z)
         launches[0] += api.last_launch_count()
+        mark(marks)
         if w.backward:
             # clipped VMC gradient (loss_function.py:75-156): tanh clipping with the previous
             # step's (center, width), coefficients (E_clip - mean) / B, hand-written backward
@@ -161,6 +172,7 @@ def run_ours(args, rank, world, dev):
             coeff = ((Ec.double() - cs[0]) / B).float()
             g = vmc.log_psi_sqr_backward(prm, state.r, state.R, state.Z, coeff)
             launches[0] += api.last_launch_count()
+            mark(marks)
             # Adam update of the packed weights (optax.adam on the inverse schedule,
             # optimization/opt_utils.py:73-76) and the rebuilt derived weight copies
             opt = optimizers.get(id(prm))
@@ -170,7 +182,34 @@ def run_ours(args, rank, world, dev):
             launches[0] += api.last_launch_count()
             c = cs[2:4].cpu()
             clip_state[0] = (float(c[0]), max(float(c[1]), 1e-12))
+            mark(marks)
         return E
+
+    def breakdown(n=2):
+        """Milliseconds per step by phase (CUDA events on the current stream) and by library
+        timer tag, over n steps after the measured ones."""
+        tags = ["mh", "features", "streams", "conv", "spin_means", "mean_gemm", "map_gemm", "layer_gemm_value",
+                "layer_gemm", "backflow_gemm", "envelope", "slogdet", "det_tangents", "jastrow", "combine",
+                "guard", "guard_layer_gemm", "fp64_gemm", "fp64_tanh", "fp64_streams", "fp64_conv", "fp64_envelope", "fp64_lu",
+                "fp64_det_tangents", "backward"]
+        names = ["mcmc (11 forwards)", "local_energy", "backward", "adam"]
+        tot = [0.0] * len(names)
+        torch.cuda.synchronize()
+        L.dw_timer_enable(1)
+        for _ in range(n):
+            marks = []
+            step(params, marks)
+            torch.cuda.synchronize()
+            for i in range(len(marks) - 1):
+                tot[i] += marks[i].elapsed_time(marks[i + 1]) / n
+        out = {"phases_ms": {k: round(v, 3) for k, v in zip(names, tot) if v}, "tags_ms": {}}
+        for t in tags:
+            vals = [ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()]
+            L.dw_timer_read(t.encode(), *[ctypes.byref(x) for x in vals])
+            if vals[1].value:
+                out["tags_ms"][t] = {"ms_per_step": round(vals[0].value / n, 3), "launches": vals[1].value // n}
+        L.dw_timer_enable(0)
+        return out
 
     def barrier():
         if world > 1:
@@ -315,7 +354,7 @@ def run_ours(args, rank, world, dev):
             # above the tolerance and which were re-evaluated in FP64 inside the mixed form
             gs["fraction"] = round(gs["flagged"] / max(gs["walkers"], 1), 6)
             out["tail_reevaluation_fp64"] = gs
-    return out, (state, params, a, mol, w, r_mixed)
+    return out, (state, params, a, mol, w, r_mixed, breakdown)
 
 
 def ours_config(w, mol, a, B, world):
@@ -468,7 +507,7 @@ def main():
     out, ctx = run_ours(args, rank, world, dev)
     if rank == 0:
         from deeperwin_gb300 import params as P
-        state, params, a, mol, w, r_mixed = ctx
+        state, params, a, mol, w, r_mixed, breakdown = ctx
         # the checks evaluate the weights the GPU holds now (updated ones after optimisation steps)
         p_now = P.unpack(a, params.flat.detach().cpu().numpy())
         if w.precision != "fp32" and not args.no_plain:
@@ -477,6 +516,8 @@ def main():
         if not args.no_cpu_baseline:
             r_sample = state.r[:32].double().cpu().numpy()
             out["cpu_baseline"] = cpu_baseline(args, a, mol, r_sample, w.backward, p_now)
+        if args.breakdown:
+            out["breakdown"] = breakdown()
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.barrier()

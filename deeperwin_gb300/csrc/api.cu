@@ -314,9 +314,11 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
             const double flops = 2.0 * rows_alg * d.D * kreal;
             const double esz = (double)sizeof(Act) * ActIO<Act>::kParts;
             const double bytes = rows_alg * (kreal + d.D) * esz + kreal * d.D * esz;
-            timer_begin("layer_gemm", s);
+            // the tail re-evaluation's FP32 layers are timed apart from the production form's
+            const char* tag = precision == DW_PRECISION_FP32_DET64 ? "guard_layer_gemm" : "layer_gemm";
+            timer_begin(tag, s);
             DW_CHECK(MM<Act>::mm_fl(xin, ldin, wm, xout, kXW, rows, d.D, d.kw[l], e3, d, p.Zb, s));
-            timer_end("layer_gemm", s, flops, bytes);
+            timer_end(tag, s, flops, bytes);
         } else {
             DW_TIMED("layer_gemm_value", DW_CHECK(MM<Act>::mm(xin, ldin, wm, xout, kXW, rows, d.D, d.kw[l], e3, s)));
         }
@@ -508,7 +510,10 @@ static int local_energy_impl(const DwArch* a, int precision, const float* params
             DW_CHECK(forward_all<Act>(a, precision, params, prepared, r, B, R, Z, lpo, nullptr, E, grad, true, ws, region,
                                       s, seg, nseg, kChunkBudget, esc));
             if (!guarded) return (int)DW_OK;
-            return tail_guard(a, params, prepared, r, B, R, Z, seg, nseg, esc, E, lpo, grad, ws, region, s);
+            timer_begin("guard", s);
+            const int st = tail_guard(a, params, prepared, r, B, R, Z, seg, nseg, esc, E, lpo, grad, ws, region, s);
+            timer_end("guard", s, 0.0, 0.0);
+            return st;
         }
     });
 }
@@ -741,8 +746,11 @@ int dw_log_psi_sqr_backward(const DwArch* a, int precision, const float* params,
     Prepared pre = carve_prepared(a, precision, const_cast<void*>(prepared));
     const float* m4[4] = {pre.main[0], pre.main[1], pre.main[2], pre.main[3]};
     const float* n4[4] = {pre.mean[0], pre.mean[1], pre.mean[2], pre.mean[3]};
-    return backward_all(a, params, m4, n4, pre.bf_cat, pre.sp_alpha, r, B, R, Z, coeff, grad, ws, wsb,
-                        (cudaStream_t)stream);
+    timer_begin("backward", (cudaStream_t)stream);
+    const int st = backward_all(a, params, m4, n4, pre.bf_cat, pre.sp_alpha, r, B, R, Z, coeff, grad, ws, wsb,
+                                (cudaStream_t)stream);
+    timer_end("backward", (cudaStream_t)stream, 0.0, 0.0);
+    return st;
 }
 
 int dw_energy_stats(const float* E, int n, double* out, void* stream) {

@@ -266,7 +266,10 @@ int dw_guard_stats(int64_t* walkers, int64_t* flagged, int64_t* overflow, int re
 int64_t dw_last_launch_count(void);
 
 /* Instrumentation: per-tag CUDA-event timing of selected kernels on their launch stream
- * ("layer_gemm" = the widened forward-Laplacian layer GEMMs). dw_timer_enable clears the
+ * ("layer_gemm" = the widened forward-Laplacian layer GEMMs of the production form,
+ * "guard_layer_gemm" = those of the tail re-evaluation, "guard" = the whole tail re-evaluation,
+ * "backward" = dw_log_psi_sqr_backward, "mh" = the Metropolis-Hastings kernel; the other tags
+ * name the stages of the forward). dw_timer_enable clears the
  * accumulators; dw_timer_read synchronizes the recorded events and returns the total time (ms),
  * launch count, and the algorithmic FLOPs and bytes of those launches. No reference counterpart. */
 int dw_timer_enable(int on);

@@ -190,7 +190,7 @@ def run_ours(args, rank, world, dev):
         timer tag, over n steps after the measured ones."""
         tags = ["mh", "features", "streams", "conv", "spin_means", "mean_gemm", "map_gemm", "layer_gemm_value",
                 "layer_gemm", "backflow_gemm", "envelope", "slogdet", "det_tangents", "jastrow", "combine",
-                "guard", "guard_layer_gemm", "fp64_gemm", "fp64_tanh", "fp64_streams", "fp64_conv", "fp64_envelope", "fp64_lu",
+                "guard", "guard_layer_gemm", "guard_fp64", "fp64_gemm", "fp64_tanh", "fp64_streams", "fp64_conv", "fp64_envelope", "fp64_lu",
                 "fp64_det_tangents", "backward"]
         names = ["mcmc (11 forwards)", "local_energy", "backward", "adam"]
         tot = [0.0] * len(names)
@@ -250,9 +250,13 @@ def run_ours(args, rank, world, dev):
         return ms, E, clocks, kt, launches[0]
 
     def guard_stats(reset):
-        v = [ctypes.c_int64() for _ in range(3)]
-        _lib.check(L.dw_guard_stats(*[ctypes.byref(x) for x in v], int(reset)), "dw_guard_stats")
-        return {"walkers": v[0].value, "flagged": v[1].value, "over_capacity": v[2].value}
+        out = {}
+        for tier, name in ((0, "fp64_determinants"), (1, "fp64_form")):
+            v = [ctypes.c_int64() for _ in range(3)]
+            _lib.check(L.dw_guard_tier_stats(tier, *[ctypes.byref(x) for x in v], int(reset)), "dw_guard_tier_stats")
+            out[name] = {"walkers": v[0].value, "flagged": v[1].value, "over_capacity": v[2].value,
+                         "fraction": round(v[1].value / max(v[0].value, 1), 6)}
+        return out
 
     guard_stats(True)
     ms, E_mixed, clocks, kt, n_launch = timed(params, args.steps, args.warmup, sample_clocks=True, instrument=True)
@@ -351,9 +355,9 @@ def run_ours(args, rank, world, dev):
             out["plain_fp32"] = plain
         if w.precision == "mixed":
             # walkers of the local energies (warm-up and timed steps) whose predicted E_L error was
-            # above the tolerance and which were re-evaluated in FP64 inside the mixed form
-            gs["fraction"] = round(gs["flagged"] / max(gs["walkers"], 1), 6)
-            out["tail_reevaluation_fp64"] = gs
+            # above the tolerance and which were re-evaluated inside the mixed form: with FP64
+            # determinant algebra, and (cancelled magnitude above 1e5 Ha) by the FP64 form
+            out["tail_reevaluation"] = gs
     return out, (state, params, a, mol, w, r_mixed, breakdown)
 
 
@@ -507,12 +511,27 @@ def main():
     out, ctx = run_ours(args, rank, world, dev)
     if rank == 0:
         from deeperwin_gb300 import params as P
+        from deeperwin_gb300 import api
         state, params, a, mol, w, r_mixed, breakdown = ctx
         # the checks evaluate the weights the GPU holds now (updated ones after optimisation steps)
         p_now = P.unpack(a, params.flat.detach().cpu().numpy())
         if w.precision != "fp32" and not args.no_plain:
             n64 = args.fp64_walkers or (1024 if a.n_el > 30 else state.r.shape[0])
             out["accuracy_vs_fp64"] = accuracy_vs_fp64(a, mol, r_mixed, state, params, min(n64, state.r.shape[0]), p_now)
+            out["accuracy_vs_fp64"]["state"] = ("the mixed chain's walkers and weights at the end of the run "
+                                                "(after the warm-up, timed and end-to-end optimisation steps)")
+            # the same comparison at the random-init weights, on a chain equilibrated by 30 steps
+            p0 = P.init_params(a, seed=0)
+            params0 = api.Params.from_dict(a, p0, w.precision)
+            st0 = api.MCMCState.initialize_around_nuclei(state.r.shape[0], mol, seed=1)
+            st0.scalars[:] = torch.frombuffer(bytearray(bytes(_lib.DwMcmcScalars(0.0, 0.0, w.step_size, 0, 0, 0))),
+                                              dtype=torch.uint8).cuda()
+            api.MetropolisHastingsMonteCarlo(api.MCMCConfig(stepsize_update_interval=100)).run_mcmc_steps(
+                None, st0, params0, a.n_up, a.n_dn, None, n_steps=30)
+            out["accuracy_vs_fp64_initial_weights"] = accuracy_vs_fp64(a, mol, st0.r, st0, params0,
+                                                                       min(n64, st0.r.shape[0]), p0)
+            out["accuracy_vs_fp64_initial_weights"]["state"] = ("random-init weights (seed 0), walkers after 30 "
+                                                                "Metropolis-Hastings steps from the Gaussian start")
         if not args.no_cpu_baseline:
             r_sample = state.r[:32].double().cpu().numpy()
             out["cpu_baseline"] = cpu_baseline(args, a, mol, r_sample, w.backward, p_now)

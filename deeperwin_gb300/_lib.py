@@ -11,7 +11,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "csrc" / "libdwgb.so"
 
-DW_PRECISION = {"fp32": 0, "plain": 0, "mixed": 1, "bf16": 2, "fp64": 3, "fp32_det64": 4}
+DW_PRECISION = {"fp32": 0, "plain": 0, "mixed": 1, "bf16": 2, "fp64": 3, "fp32_det64": 4, "mixed_det64": 5}
 
 
 class DwArch(ctypes.Structure):
@@ -80,6 +80,9 @@ _SIGS = {
                                           ctypes.c_int, _P]),
     "dw_debug_tc_error_flag": (ctypes.c_int, []),
     "dw_debug_set_gemm_bk": (ctypes.c_int, [ctypes.c_int]),
+    "dw_debug_set_guard_form": (ctypes.c_int, [ctypes.c_int]),
+    "dw_guard_tier_stats": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                           ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
     "dw_debug_slogdet_small": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                               _P, _P, _P, _P]),
     "dw_debug_local_energy_scales": (ctypes.c_int, [ctypes.POINTER(DwArch), ctypes.c_int, _P, _P, _P, ctypes.c_int, _P,

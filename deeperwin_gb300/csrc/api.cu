@@ -29,7 +29,8 @@ struct Prepared {
     size_t bytes;
 };
 static inline int tc_parts(int precision) {
-    return precision == DW_PRECISION_MIXED ? 2 : (precision == DW_PRECISION_BF16 ? 1 : 0);
+    return (precision == DW_PRECISION_MIXED || precision == DW_PRECISION_MIXED_DET64) ? 2
+                                                                                      : (precision == DW_PRECISION_BF16 ? 1 : 0);
 }
 static inline int mean_width(const Dims& d, int l) { return round_up(2 * d.hw[l], 64); }
 
@@ -315,7 +316,7 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
             const double esz = (double)sizeof(Act) * ActIO<Act>::kParts;
             const double bytes = rows_alg * (kreal + d.D) * esz + kreal * d.D * esz;
             // the tail re-evaluation's FP32 layers are timed apart from the production form's
-            const char* tag = precision == DW_PRECISION_FP32_DET64 ? "guard_layer_gemm" : "layer_gemm";
+            const char* tag = det64_form(precision) ? "guard_layer_gemm" : "layer_gemm";
             timer_begin(tag, s);
             DW_CHECK(MM<Act>::mm_fl(xin, ldin, wm, xout, kXW, rows, d.D, d.kw[l], e3, d, p.Zb, s));
             timer_end(tag, s, flops, bytes);
@@ -357,7 +358,7 @@ static int run_chunk(const Plan<Act>& p, int Bc, int precision, const float* P, 
         DW_TIMED("backflow_gemm", DW_CHECK(MM<Act>::mm(H, kXW, wb, p.BF, ldbf, rows, 2 * d.KN, d.D, e0, s)));
     }
     DW_TIMED("envelope", launch_envelope(r, R, Z, P, L, pre.sp_alpha, d, Bc, p.BF, ldbf, spin_cols, p.MO, s));
-    if (precision == DW_PRECISION_FP32_DET64 && tang) {
+    if (det64_form(precision) && tang) {
         // FP64 LU, inverse and tangent traces of the FP32 Slater channels; the widened channels use
         // the backflow buffer (consumed by the envelope kernel, at least twice the Slater channels'
         // size) and the inverses the layer buffer XA (the embedding H is in XB)
@@ -398,6 +399,7 @@ static int with_act(int precision, bool need_device, F&& f) {
         case DW_PRECISION_FP32_DET64: return f((float*)nullptr);
         case DW_PRECISION_FP64: return f((double*)nullptr);
         case DW_PRECISION_MIXED:
+        case DW_PRECISION_MIXED_DET64:
             if (need_device && !tc_available()) return DW_ERR_UNSUPPORTED;
             return f((Split*)nullptr);
         case DW_PRECISION_BF16:
@@ -518,12 +520,18 @@ static int local_energy_impl(const DwArch* a, int precision, const float* params
     });
 }
 
-// Local energy of the plain FP32 network with FP64 determinant algebra (DW_PRECISION_FP32_DET64)
-// on a caller region: the mixed form's re-evaluation of flagged walkers (guard.cu).
-size_t det64_plan_bytes(const DwArch* a, int B) { return plan_bytes<float>(a, B, true); }
-int det64_local_energy(const DwArch* a, const float* P, const void* prepared, const float* r, int B, const float* R,
-                       const int32_t* Z, const int32_t* seg, int nseg, float* E, float* lp, float* grad, void* ws,
-                       size_t wsb, cudaStream_t s) {
+// Local energy with FP64 determinant algebra on a caller region (DW_PRECISION_FP32_DET64: plain
+// FP32 network, DW_PRECISION_MIXED_DET64: split-BF16 network): the mixed form's re-evaluation of
+// flagged walkers (guard.cu).
+size_t det64_plan_bytes(const DwArch* a, int precision, int B) {
+    return precision == DW_PRECISION_MIXED_DET64 ? plan_bytes<Split>(a, B, true) : plan_bytes<float>(a, B, true);
+}
+int det64_local_energy(const DwArch* a, int precision, const float* P, const void* prepared, const float* r, int B,
+                       const float* R, const int32_t* Z, const int32_t* seg, int nseg, float* E, float* lp, float* grad,
+                       void* ws, size_t wsb, cudaStream_t s) {
+    if (precision == DW_PRECISION_MIXED_DET64)
+        return forward_all<Split>(a, precision, P, prepared, r, B, R, Z, lp, nullptr, E, grad, true, ws, wsb, s, seg,
+                                  nseg);
     return forward_all<float>(a, DW_PRECISION_FP32_DET64, P, prepared, r, B, R, Z, lp, nullptr, E, grad, true, ws, wsb,
                               s, seg, nseg);
 }
@@ -574,7 +582,7 @@ int dw_prepare_params(const DwArch* a, int precision, const float* params, void*
     reset_launch_count();
     DW_CHECK(check_arch(a));
     if (!params || !prepared) return DW_ERR_ARG;
-    if (precision < DW_PRECISION_FP32 || precision > DW_PRECISION_FP32_DET64) return DW_ERR_ARG;
+    if (precision < DW_PRECISION_FP32 || precision > DW_PRECISION_MIXED_DET64) return DW_ERR_ARG;
     return prepare(a, precision, params, prepared, bytes, (cudaStream_t)stream);
 }
 

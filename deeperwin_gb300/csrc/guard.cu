@@ -8,15 +8,18 @@
 // walker the magnitude of the terms it cancels; walkers whose predicted error (that magnitude
 // times the form's relative entry accuracy) exceeds a threshold are gathered into a fixed-capacity
 // sub-batch (no host synchronisation), re-evaluated with FP64 determinant algebra, and their E_L,
-// log psi^2 and gradient are scattered back. The selection depends only on each walker's own scales, so a walker gets the
-// same result in any batch as long as the flagged walkers fit the capacity; beyond it the walkers
-// with the largest predicted errors are taken.
+// log psi^2 and gradient are scattered back. Walkers so close to a node that the FP32 rounding of
+// the network itself decides their E_L (magnitudes above kGuardFp64Key) are then re-evaluated by the
+// FP64 form (fp64.cu) in a second, smaller sub-batch. The selection depends only on each walker's
+// own scales, so a walker gets the same result in any batch as long as the flagged walkers fit the
+// capacities; beyond them the walkers with the largest predicted errors are taken.
 #include "net.cuh"
 #include <algorithm>
 
 namespace dw {
 
-__device__ unsigned long long g_guard_walkers = 0, g_guard_flagged = 0, g_guard_overflow = 0;
+// [tier][walkers seen, walkers flagged, flagged walkers beyond the capacity]
+__device__ unsigned long long g_guard_cnt[2][3];
 
 // Predicted E_L error of a mixed-form walker: kGuardRel times the largest magnitude the combine
 // kernel cancels (the determinant terms of the Laplacian of log|psi~|, or the terms of E_L). On
@@ -31,7 +34,14 @@ constexpr float kGuardTol = 0.03f;
 // on 4,096 C2H4-shaped walkers near the initial weights the plain FP32 form is off by up to 14 Ha,
 // the same network with FP64 determinants by at most 95 mHa (mean 0.03 mHa), at about 1.5x the
 // plain form's cost per walker. The FP64 form (fp64.cu) would cost about 15x more per walker.
-constexpr bool kGuardFp64 = false;
+// Second tier: walkers whose cancelled magnitude exceeds kGuardFp64Key Ha. At the end of the C2H4
+// optimisation bench (random-init weights after 14 Adam steps) 8-23 of 4,096 walkers exceed it; the
+// FP32 network with FP64 determinants is off by 0.1-4 Ha on those between 1e5 and 1e7 and by up to
+// 57 kHa on the few beyond 1e8 (|E_L| up to 1.4e5 Ha), where only an FP64 network resolves the node.
+constexpr float kGuardFp64Key = 1.0e5f;
+// Network of the first tier's re-evaluation (DW_PRECISION_FP32_DET64 or DW_PRECISION_MIXED_DET64;
+// instrumentation switch dw_debug_set_guard_form).
+static int g_guard_form = DW_PRECISION_FP32_DET64;
 
 // Sort key of a walker (larger = re-evaluate first); NaN scales rank first.
 __device__ __forceinline__ float guard_key(const float* sc) {
@@ -47,7 +57,7 @@ __device__ __forceinline__ float guard_key(const float* sc) {
 // counts[1] = walkers flagged.
 __global__ void __launch_bounds__(1024)
 k_guard_select(const float* __restrict__ esc, int B, float rel, float tol, int cap, int* __restrict__ idx,
-               int* __restrict__ counts) {
+               int* __restrict__ counts, int tier) {
     __shared__ int warp_tot[32];
     __shared__ int base;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -110,9 +120,9 @@ k_guard_select(const float* __restrict__ esc, int B, float rel, float tol, int c
         const int sel = min(base, cap);
         counts[0] = sel;
         counts[1] = flagged;
-        atomicAdd(&g_guard_walkers, (unsigned long long)B);
-        atomicAdd(&g_guard_flagged, (unsigned long long)flagged);
-        if (flagged > sel) atomicAdd(&g_guard_overflow, (unsigned long long)(flagged - sel));
+        atomicAdd(&g_guard_cnt[tier][0], (unsigned long long)B);
+        atomicAdd(&g_guard_cnt[tier][1], (unsigned long long)flagged);
+        if (flagged > sel) atomicAdd(&g_guard_cnt[tier][2], (unsigned long long)(flagged - sel));
     }
 }
 
@@ -143,34 +153,49 @@ __global__ void k_guard_scatter(const float* __restrict__ E_sub, const float* __
 }
 
 int guard_capacity(const DwArch* a, int B) {
-    // up to 1 / 32 of the batch (at least 16); the FP64 form needs the flagged walkers in one chunk
-    // (its kernels skip the unused capacity through the device-side count), the FP32 network with
-    // FP64 determinants runs over the whole capacity (unused slots hold a copy of walker 0)
-    const int want = std::min(B, std::max(16, (B + 31) / 32));
-    return kGuardFp64 ? std::max(1, std::min(want, fp64_max_chunk(a, true))) : want;
+    // first tier: up to 1 / 32 of the batch (at least 16), run over the whole capacity (unused
+    // slots hold a copy of walker 0)
+    (void)a;
+    return std::min(B, std::max(16, (B + 31) / 32));
 }
 
-struct GuardPlan {
+// second tier: up to 1 / 128 of the batch (at least 8) in one FP64 chunk; its kernels skip the
+// unused capacity through the device-side count, so it costs FP64 work only for the walkers
+// flagged (about 0.6 ms per C2H4-shaped walker)
+static int guard64_capacity(const DwArch* a, int B) {
+    return std::max(1, std::min(std::min(B, std::max(8, (B + 127) / 128)), fp64_max_chunk(a, true)));
+}
+
+struct GuardTier {
     int cap;
     int* idx; int* counts; float* r_sub; int32_t* seg_sub; float* E_sub; float* lp_sub; float* g_sub;
-    void* fp64_ws; size_t fp64_bytes;
+};
+
+struct GuardPlan {
+    GuardTier t[2];
+    void* region; size_t region_bytes;              // forward workspace, used by one tier at a time
     size_t bytes;
 };
 
 static GuardPlan carve_guard(const DwArch* a, int B, void* ws) {
     GuardPlan g;
     const int n3 = 3 * a->n_el;
-    g.cap = guard_capacity(a, B);
     Carver c(ws, (size_t)-1);
-    g.idx = c.take<int>((size_t)g.cap);
-    g.counts = c.take<int>(2);
-    g.r_sub = c.take<float>((size_t)g.cap * n3);
-    g.seg_sub = c.take<int32_t>((size_t)g.cap);
-    g.E_sub = c.take<float>((size_t)g.cap);
-    g.lp_sub = c.take<float>((size_t)g.cap);
-    g.g_sub = c.take<float>((size_t)g.cap * n3);
-    g.fp64_bytes = kGuardFp64 ? fp64_plan_bytes(a, g.cap, true) : det64_plan_bytes(a, g.cap);
-    g.fp64_ws = c.take<unsigned char>(g.fp64_bytes);
+    for (int k = 0; k < 2; ++k) {
+        GuardTier& t = g.t[k];
+        t.cap = k == 0 ? guard_capacity(a, B) : guard64_capacity(a, B);
+        t.idx = c.take<int>((size_t)t.cap);
+        t.counts = c.take<int>(2);
+        t.r_sub = c.take<float>((size_t)t.cap * n3);
+        t.seg_sub = c.take<int32_t>((size_t)t.cap);
+        t.E_sub = c.take<float>((size_t)t.cap);
+        t.lp_sub = c.take<float>((size_t)t.cap);
+        t.g_sub = c.take<float>((size_t)t.cap * n3);
+    }
+    g.region_bytes = std::max({det64_plan_bytes(a, DW_PRECISION_FP32_DET64, g.t[0].cap),
+                               det64_plan_bytes(a, DW_PRECISION_MIXED_DET64, g.t[0].cap),
+                               fp64_plan_bytes(a, g.t[1].cap, true)});
+    g.region = c.take<unsigned char>(g.region_bytes);
     g.bytes = c.used + 256;
     return g;
 }
@@ -183,22 +208,30 @@ int tail_guard(const DwArch* a, const float* P, const void* prepared, const floa
     GuardPlan g = carve_guard(a, B, ws);
     if (g.bytes > wsb) return DW_ERR_WORKSPACE;
     const int n3 = 3 * a->n_el;
-    k_guard_select<<<1, 1024, 0, s>>>(esc, B, kGuardRel, kGuardTol, g.cap, g.idx, g.counts);
-    count_launch();
-    const int64_t ne = (int64_t)g.cap * n3;
-    k_guard_gather<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(r, seg, g.idx, g.counts, n3, g.r_sub,
-                                                                 seg ? g.seg_sub : nullptr, g.cap, kGuardFp64 ? 0 : 1);
-    count_launch();
-    if (kGuardFp64)
-        DW_CHECK(fp64_forward_all(a, P, prepared, g.r_sub, g.cap, R, Z, g.lp_sub, nullptr, g.E_sub,
-                                  grad ? g.g_sub : nullptr, true, g.fp64_ws, g.fp64_bytes, s, seg ? g.seg_sub : nullptr,
-                                  nseg, g.counts));
-    else
-        DW_CHECK(det64_local_energy(a, P, prepared, g.r_sub, g.cap, R, Z, seg ? g.seg_sub : nullptr, nseg, g.E_sub,
-                                    g.lp_sub, grad ? g.g_sub : nullptr, g.fp64_ws, g.fp64_bytes, s));
-    k_guard_scatter<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(g.E_sub, g.lp_sub, g.g_sub, g.idx, g.counts, n3, g.cap,
-                                                                  E, lp, grad);
-    count_launch();
+    for (int k = 0; k < 2; ++k) {
+        const GuardTier& t = g.t[k];
+        // tier 0: predicted error above kGuardTol; tier 1: magnitude above kGuardFp64Key
+        k_guard_select<<<1, 1024, 0, s>>>(esc, B, k == 0 ? kGuardRel : 1.0f, k == 0 ? kGuardTol : kGuardFp64Key, t.cap,
+                                          t.idx, t.counts, k);
+        count_launch();
+        const int64_t ne = (int64_t)t.cap * n3;
+        k_guard_gather<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(r, seg, t.idx, t.counts, n3, t.r_sub,
+                                                                     seg ? t.seg_sub : nullptr, t.cap, k == 0 ? 1 : 0);
+        count_launch();
+        if (k == 0) {
+            DW_CHECK(det64_local_energy(a, g_guard_form, P, prepared, t.r_sub, t.cap, R, Z, seg ? t.seg_sub : nullptr,
+                                        nseg, t.E_sub, t.lp_sub, grad ? t.g_sub : nullptr, g.region, g.region_bytes, s));
+        } else {
+            timer_begin("guard_fp64", s);
+            DW_CHECK(fp64_forward_all(a, P, prepared, t.r_sub, t.cap, R, Z, t.lp_sub, nullptr, t.E_sub,
+                                      grad ? t.g_sub : nullptr, true, g.region, g.region_bytes, s,
+                                      seg ? t.seg_sub : nullptr, nseg, t.counts));
+            timer_end("guard_fp64", s, 0.0, 0.0);
+        }
+        k_guard_scatter<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(t.E_sub, t.lp_sub, t.g_sub, t.idx, t.counts, n3,
+                                                                      t.cap, E, lp, grad);
+        count_launch();
+    }
     DW_CHECK_CUDA(cudaGetLastError());
     return DW_OK;
 }
@@ -207,26 +240,38 @@ int tail_guard(const DwArch* a, const float* P, const void* prepared, const floa
 
 extern "C" {
 
-// Cumulative counts of the tail re-evaluation since the last reset: walkers seen, walkers
-// flagged, flagged walkers beyond the capacity (kept at their mixed-form values). Synchronizes
-// the device. No counterpart in the reference.
-int dw_guard_stats(int64_t* walkers, int64_t* flagged, int64_t* overflow, int reset) {
-    unsigned long long v[3] = {0, 0, 0};
+// Cumulative counts of the tail re-evaluation since the last reset (tier 0: the FP64-determinant
+// re-evaluation, tier 1: the FP64-form re-evaluation): walkers seen, walkers flagged, flagged
+// walkers beyond the capacity (kept at the previous tier's values). Synchronizes the device. No
+// counterpart in the reference.
+int dw_guard_tier_stats(int tier, int64_t* walkers, int64_t* flagged, int64_t* overflow, int reset) {
+    if (tier < 0 || tier > 1) return DW_ERR_ARG;
+    unsigned long long v[2][3];
     if (cudaDeviceSynchronize() != cudaSuccess) return DW_ERR_CUDA;
-    if (cudaMemcpyFromSymbol(&v[0], dw::g_guard_walkers, sizeof(v[0])) != cudaSuccess ||
-        cudaMemcpyFromSymbol(&v[1], dw::g_guard_flagged, sizeof(v[1])) != cudaSuccess ||
-        cudaMemcpyFromSymbol(&v[2], dw::g_guard_overflow, sizeof(v[2])) != cudaSuccess)
-        return DW_ERR_CUDA;
-    if (walkers) *walkers = (int64_t)v[0];
-    if (flagged) *flagged = (int64_t)v[1];
-    if (overflow) *overflow = (int64_t)v[2];
+    if (cudaMemcpyFromSymbol(v, dw::g_guard_cnt, sizeof(v)) != cudaSuccess) return DW_ERR_CUDA;
+    if (walkers) *walkers = (int64_t)v[tier][0];
+    if (flagged) *flagged = (int64_t)v[tier][1];
+    if (overflow) *overflow = (int64_t)v[tier][2];
     if (reset) {
-        unsigned long long z = 0;
-        cudaMemcpyToSymbol(dw::g_guard_walkers, &z, sizeof(z));
-        cudaMemcpyToSymbol(dw::g_guard_flagged, &z, sizeof(z));
-        cudaMemcpyToSymbol(dw::g_guard_overflow, &z, sizeof(z));
+        for (int k = 0; k < 3; ++k) v[tier][k] = 0;
+        if (cudaMemcpyToSymbol(dw::g_guard_cnt, v, sizeof(v)) != cudaSuccess) return DW_ERR_CUDA;
     }
     return DW_OK;
+}
+
+// Tier 0 of dw_guard_tier_stats; a reset clears both tiers.
+int dw_guard_stats(int64_t* walkers, int64_t* flagged, int64_t* overflow, int reset) {
+    DW_CHECK(dw_guard_tier_stats(0, walkers, flagged, overflow, reset));
+    return reset ? dw_guard_tier_stats(1, nullptr, nullptr, nullptr, 1) : DW_OK;
+}
+
+// Instrumentation: network of the first re-evaluation tier (DW_PRECISION_FP32_DET64, the default,
+// or DW_PRECISION_MIXED_DET64). Returns the previous form.
+int dw_debug_set_guard_form(int precision) {
+    if (!dw::det64_form(precision)) return -DW_ERR_ARG;
+    const int old = dw::g_guard_form;
+    dw::g_guard_form = precision;
+    return old;
 }
 
 }  // extern "C"

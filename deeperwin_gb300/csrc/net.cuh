@@ -146,11 +146,15 @@ int fp64_forward_all(const DwArch* a, const float* P, const void* prepared, cons
                      const int32_t* Z, float* lp, float* phase, float* E, float* grad, bool tang, void* ws,
                      size_t ws_bytes, cudaStream_t s, const int32_t* seg, int nseg, const int* nvalid);
 
-// api.cu: the plain network with FP64 determinant algebra on a caller region
-size_t det64_plan_bytes(const DwArch* a, int B);
-int det64_local_energy(const DwArch* a, const float* P, const void* prepared, const float* r, int B, const float* R,
-                       const int32_t* Z, const int32_t* seg, int nseg, float* E, float* lp, float* grad, void* ws,
-                       size_t wsb, cudaStream_t s);
+// api.cu: the FP32 (DW_PRECISION_FP32_DET64) or split-BF16 (DW_PRECISION_MIXED_DET64) network with
+// FP64 determinant algebra on a caller region
+inline bool det64_form(int precision) {
+    return precision == DW_PRECISION_FP32_DET64 || precision == DW_PRECISION_MIXED_DET64;
+}
+size_t det64_plan_bytes(const DwArch* a, int precision, int B);
+int det64_local_energy(const DwArch* a, int precision, const float* P, const void* prepared, const float* r, int B,
+                       const float* R, const int32_t* Z, const int32_t* seg, int nseg, float* E, float* lp, float* grad,
+                       void* ws, size_t wsb, cudaStream_t s);
 
 // guard.cu: FP64 re-evaluation of the mixed form's flagged walkers (esc: per-walker error scales
 // written by the combine kernel, 3 floats per walker)

@@ -65,9 +65,12 @@ enum DwPrecision {
                                float_precision: float64 mode, configuration.py:1893 and
                                process_molecule.py:20-29); outputs are rounded to float32. Forward,
                                local energy and MCMC only (no parameter gradient) */
-    DW_PRECISION_FP32_DET64 = 4 /* plain FP32 network (CUDA-core GEMMs) with the determinant algebra in
-                                   FP64: LU, Gauss-Jordan inverse and tangent traces of the FP32 Slater
-                                   channels. Forward, local energy and MCMC (no parameter gradient) */
+    DW_PRECISION_FP32_DET64 = 4, /* plain FP32 network (CUDA-core GEMMs) with the determinant algebra in
+                                    FP64: LU, Gauss-Jordan inverse and tangent traces of the FP32 Slater
+                                    channels. Forward, local energy and MCMC (no parameter gradient) */
+    DW_PRECISION_MIXED_DET64 = 5 /* the mixed form's split-BF16 tensor-core network with the determinant
+                                    algebra of DW_PRECISION_FP32_DET64. Forward, local energy and MCMC
+                                    (no parameter gradient); uses the mixed form's prepared weights */
 };
 
 /* Human-readable text for a status code (static storage). */
@@ -256,11 +259,18 @@ size_t dw_noalloc_scratch_bytes(void);
 
 /* Instrumentation of the mixed form's local energy: walkers whose predicted E_L error (the
  * magnitude of the terms the forward Laplacian cancels, times the split-BF16 entry accuracy) is
- * above the tolerance are re-evaluated in FP64 inside dw_local_energy / dw_local_energy_packed.
- * Returns the cumulative counts since the last reset: walkers seen, walkers flagged, flagged
- * walkers beyond the per-call capacity (those keep their mixed-form values). Synchronizes the
- * device. No reference counterpart. */
+ * above the tolerance are re-evaluated with FP64 determinant algebra inside dw_local_energy /
+ * dw_local_energy_packed (tier 0), and those whose cancelled magnitude exceeds 1e5 Ha by the FP64
+ * form (tier 1). Returns the cumulative counts of a tier since its last reset: walkers seen,
+ * walkers flagged, flagged walkers beyond the per-call capacity (those keep the previous tier's
+ * values). Synchronizes the device. dw_guard_stats reads tier 0 and its reset clears both tiers.
+ * No reference counterpart. */
+int dw_guard_tier_stats(int tier, int64_t* walkers, int64_t* flagged, int64_t* overflow, int reset);
 int dw_guard_stats(int64_t* walkers, int64_t* flagged, int64_t* overflow, int reset);
+
+/* Instrumentation: network of the tier-0 re-evaluation, DW_PRECISION_FP32_DET64 (default) or
+ * DW_PRECISION_MIXED_DET64. Returns the previous form, or -DW_ERR_ARG. No reference counterpart. */
+int dw_debug_set_guard_form(int precision);
 
 /* Number of kernel launches issued by the last call on this host thread (instrumentation). */
 int64_t dw_last_launch_count(void);

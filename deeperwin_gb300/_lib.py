@@ -81,6 +81,7 @@ _SIGS = {
     "dw_debug_tc_error_flag": (ctypes.c_int, []),
     "dw_debug_set_gemm_bk": (ctypes.c_int, [ctypes.c_int]),
     "dw_debug_set_guard_form": (ctypes.c_int, [ctypes.c_int]),
+    "dw_debug_set_det_tangents_kernel": (ctypes.c_int, [ctypes.c_int]),
     "dw_guard_tier_stats": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
                                            ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
     "dw_debug_slogdet_small": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,

@@ -271,28 +271,37 @@ __global__ void k_conv_bwd(const float* __restrict__ dX, int ldx, const float* _
 
 // Pair streams adjoint, thread per unordered pair (i <= j), reverse through
 // w^(l) = tanh(h^(l) W_wm + b) (l = 0..3) and h^(l+1) = res(tanh(h^(l) W_hs + b), h^(l)).
-// Writes the pre-activation adjoints dZp[l] (w maps) and dZp[4 + l] (streams) per pair.
+// Writes the pre-activation adjoints dZp[l] (w maps) and dZp[4 + l] (streams) per pair. A layer's
+// four weight matrices (map and stream, opposite- and same-spin) are staged in shared memory, the
+// copies 16 bytes apart modulo the bank width so that the two spin kinds of a warp read different
+// banks, and read as float4 broadcasts (four FMAs per load); pair rows move as float4.
 __global__ void __launch_bounds__(128)
 k_pair_bwd(const float* __restrict__ r, const float* __restrict__ P, ParamLayout L, Dims d, int B,
            const float* __restrict__ WP, const float* __restrict__ HP, const float* __restrict__ dWP,
            float* __restrict__ dZp, float* __restrict__ HP0, int8_t* __restrict__ sel) {
+    constexpr int WPITCH = 32 * 32 + 4;
+    __shared__ __align__(16) float Wsh[4 * WPITCH];   // map diff, map same, stream diff, stream same
     const int npw = d.n * (d.n + 1) / 2;
-    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (int64_t)B * npw) return;
-    const int b = (int)(gid / npw), p = (int)(gid % npw);
-    int i = 0, rem = p;
-    while (rem >= d.n - i) { rem -= d.n - i; ++i; }
-    const int j = i + rem;
-    const bool same = (i < d.nu) == (j < d.nu);
-    const float* rb = r + (int64_t)b * d.n * 3;
-    float dd = 0.f;
-    if (i != j) {
-        const float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
-        dd = sqrtf(dx * dx + dy * dy + dz * dz);
-    }
-    HP0[gid] = dd;
-    sel[gid] = same ? 1 : 0;
     const int64_t npair = (int64_t)B * npw;
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = gid < npair;
+    int b = 0, i = 0, j = 0;
+    bool same = false;
+    if (live) {
+        b = (int)(gid / npw);
+        int rem = (int)(gid % npw);
+        while (rem >= d.n - i) { rem -= d.n - i; ++i; }
+        j = i + rem;
+        same = (i < d.nu) == (j < d.nu);
+        const float* rb = r + (int64_t)b * d.n * 3;
+        float dd = 0.f;
+        if (i != j) {
+            const float dx = rb[j * 3] - rb[i * 3], dy = rb[j * 3 + 1] - rb[i * 3 + 1], dz = rb[j * 3 + 2] - rb[i * 3 + 2];
+            dd = sqrtf(dx * dx + dy * dy + dz * dz);
+        }
+        HP0[gid] = dd;
+        sel[gid] = same ? 1 : 0;
+    }
     const int64_t plane = (int64_t)B * d.n * d.n;
     const float rs = 0.70710678118654752f;
     float dh[32];
@@ -300,54 +309,93 @@ k_pair_bwd(const float* __restrict__ r, const float* __restrict__ P, ParamLayout
     for (int k = 0; k < 32; ++k) dh[k] = 0.f;
     for (int l = 3; l >= 0; --l) {
         const int in_w = d.eew[l];
+        const int in_prev = l > 0 ? d.eew[l - 1] : 0;
+        __syncthreads();                              // the previous layer's readers are done
+        for (int e = threadIdx.x; e < 4 * 1024; e += blockDim.x) {
+            const int m = e >> 10, kf = e & 1023, k = kf >> 5;
+            float v = 0.f;
+            if (m < 2) {
+                if (k < in_w) v = P[(m ? L.w_same_w[l] : L.w_diff_w[l]) + kf];
+            } else if (k < in_prev) {
+                v = P[(m == 3 ? L.h_same_w[l - 1] : L.h_diff_w[l - 1]) + kf];
+            }
+            Wsh[m * WPITCH + kf] = v;
+        }
+        __syncthreads();
+        if (!live) continue;
         // w map adjoint
-        const float* w = WP + ((int64_t)l * plane + (int64_t)b * d.n * d.n + i * d.n + j) * 32;
-        const float* g1 = dWP + ((int64_t)l * plane + (int64_t)b * d.n * d.n + i * d.n + j) * 32;
-        const float* g2 = dWP + ((int64_t)l * plane + (int64_t)b * d.n * d.n + j * d.n + i) * 32;
-        const float* Wm = P + (same ? L.w_same_w[l] : L.w_diff_w[l]);
-        float* dzw = dZp + ((int64_t)l * npair + gid) * 32;
+        const float* Wm = Wsh + (same ? WPITCH : 0);
+        const int64_t oij = (int64_t)l * plane + (int64_t)b * d.n * d.n + i * d.n + j;
+        const int64_t oji = (int64_t)l * plane + (int64_t)b * d.n * d.n + j * d.n + i;
+        const float4* w4 = reinterpret_cast<const float4*>(WP + oij * 32);
+        const float4* g14 = reinterpret_cast<const float4*>(dWP + oij * 32);
+        const float4* g24 = reinterpret_cast<const float4*>(dWP + oji * 32);
+        float4* dzw4 = reinterpret_cast<float4*>(dZp + ((int64_t)l * npair + gid) * 32);
         float dz[32];
         #pragma unroll
-        for (int f = 0; f < 32; ++f) {
-            const float ww = w[f];
-            const float g = g1[f] + (i != j ? g2[f] : 0.f);
-            dz[f] = g * (1.f - ww * ww);
-            dzw[f] = dz[f];
+        for (int q = 0; q < 8; ++q) {
+            const float4 wv = w4[q], ga = g14[q];
+            const float4 gb = i != j ? g24[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+            dz[4 * q] = (ga.x + gb.x) * (1.f - wv.x * wv.x);
+            dz[4 * q + 1] = (ga.y + gb.y) * (1.f - wv.y * wv.y);
+            dz[4 * q + 2] = (ga.z + gb.z) * (1.f - wv.z * wv.z);
+            dz[4 * q + 3] = (ga.w + gb.w) * (1.f - wv.w * wv.w);
+            dzw4[q] = make_float4(dz[4 * q], dz[4 * q + 1], dz[4 * q + 2], dz[4 * q + 3]);
         }
         #pragma unroll
         for (int k = 0; k < 32; ++k) {
             if (k < in_w) {
-                float s = 0.f;
+                const float4* wr = reinterpret_cast<const float4*>(Wm + k * 32);
+                float acc = 0.f;
                 #pragma unroll
-                for (int f = 0; f < 32; ++f) s = fmaf(dz[f], __ldg(Wm + k * 32 + f), s);
-                dh[k] += s;
+                for (int q = 0; q < 8; ++q) {
+                    const float4 wq = wr[q];
+                    acc = fmaf(dz[4 * q], wq.x, acc);
+                    acc = fmaf(dz[4 * q + 1], wq.y, acc);
+                    acc = fmaf(dz[4 * q + 2], wq.z, acc);
+                    acc = fmaf(dz[4 * q + 3], wq.w, acc);
+                }
+                dh[k] += acc;
             }
         }
-        if (l == 0) break;
+        if (l == 0) continue;
         // stream adjoint: h^(l) = res(y, h^(l-1)), y = tanh(h^(l-1) W_hs + b)
         const bool resid = l - 1 > 0;
-        const float* hl = HP + ((int64_t)(l - 1) * npair + gid) * 32;                 // h^(l)
-        const float* hp = l - 1 > 0 ? HP + ((int64_t)(l - 2) * npair + gid) * 32 : nullptr;   // h^(l-1)
-        const float* Ws = P + (same ? L.h_same_w[l - 1] : L.h_diff_w[l - 1]);
-        float* dzs = dZp + ((int64_t)(4 + l - 1) * npair + gid) * 32;
+        const float* Ws = Wsh + (same ? 3 : 2) * WPITCH;
+        const float4* hl4 = reinterpret_cast<const float4*>(HP + ((int64_t)(l - 1) * npair + gid) * 32);   // h^(l)
+        const float4* hp4 = reinterpret_cast<const float4*>(HP + ((int64_t)(resid ? l - 2 : 0) * npair + gid) * 32);
+        float4* dzs4 = reinterpret_cast<float4*>(dZp + ((int64_t)(4 + l - 1) * npair + gid) * 32);
         float dzh[32];
         #pragma unroll
-        for (int f = 0; f < 32; ++f) {
-            const float y = resid ? 1.41421356237309505f * hl[f] - hp[f] : hl[f];
-            const float dy = resid ? dh[f] * rs : dh[f];
-            dzh[f] = dy * (1.f - y * y);
-            dzs[f] = dzh[f];
+        for (int q = 0; q < 8; ++q) {
+            const float4 hv = hl4[q];
+            const float4 pv = resid ? hp4[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float h4[4] = {hv.x, hv.y, hv.z, hv.w}, p4[4] = {pv.x, pv.y, pv.z, pv.w};
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int f = 4 * q + u;
+                const float y = resid ? 1.41421356237309505f * h4[u] - p4[u] : h4[u];
+                const float dy = resid ? dh[f] * rs : dh[f];
+                dzh[f] = dy * (1.f - y * y);
+            }
+            dzs4[q] = make_float4(dzh[4 * q], dzh[4 * q + 1], dzh[4 * q + 2], dzh[4 * q + 3]);
         }
-        const int in_prev = d.eew[l - 1];
         float dn[32];
         #pragma unroll
         for (int k = 0; k < 32; ++k) {
-            float s = resid ? dh[k] * rs : 0.f;
+            float acc = resid ? dh[k] * rs : 0.f;
             if (k < in_prev) {
+                const float4* wr = reinterpret_cast<const float4*>(Ws + k * 32);
                 #pragma unroll
-                for (int f = 0; f < 32; ++f) s = fmaf(dzh[f], __ldg(Ws + k * 32 + f), s);
+                for (int q = 0; q < 8; ++q) {
+                    const float4 wq = wr[q];
+                    acc = fmaf(dzh[4 * q], wq.x, acc);
+                    acc = fmaf(dzh[4 * q + 1], wq.y, acc);
+                    acc = fmaf(dzh[4 * q + 2], wq.z, acc);
+                    acc = fmaf(dzh[4 * q + 3], wq.w, acc);
+                }
             }
-            dn[k] = s;
+            dn[k] = acc;
         }
         #pragma unroll
         for (int k = 0; k < 32; ++k) dh[k] = dn[k];

@@ -1016,9 +1016,126 @@ k_det_tangents_tile(const float* __restrict__ MO, const float* __restrict__ Ainv
     }
 }
 
+// Instrumentation: run the single-buffer tile kernel for every n (dw_debug_set_det_tangents_kernel).
+static bool g_det_tangents_tile = false;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// The traces of k_det_tangents_tile for n == NP in {4, 8, 16} (a channel's 4 x 4 tiles within one
+// warp): the channel planes stream through three shared-memory buffers by cp.async (the planes of
+// round r + 2 load while round r's products run), the transposed partner tile comes by shuffles
+// instead of a shared-memory round trip, and a channel's partial traces are reduced by shuffles,
+// so a round needs one barrier. The same products and FP32 partial sums, FP64 accumulation over
+// the channels.
+template <int NP>
+__global__ void __launch_bounds__(128)
+k_det_tangents_pipe(const float* __restrict__ MO, const float* __restrict__ Ainv, const double* __restrict__ sign,
+                    int T, double* __restrict__ g, double* __restrict__ lapdet) {
+    constexpr int n = NP, nn = NP * NP;
+    constexpr int NB = NP / 4, TPC = NB * NB, CPR = 128 / TPC, PP = NP * NP + 4, Q = NP * NP / 4;
+    static_assert(32 % TPC == 0, "a channel's tiles lie in one warp");
+    __shared__ __align__(16) float AT[NP * NP];
+    __shared__ __align__(16) float Ds[3][CPR * PP];
+    __shared__ double tr1[3 * 32 + 2], tr2[3 * 32 + 2];
+    const int mat = blockIdx.x, tid = threadIdx.x;
+    if (sign[mat] == 0.0) {
+        for (int t = tid; t < 3 * n; t += 128) g[(int64_t)mat * 3 * n + t] = 0.0;
+        if (tid == 0) lapdet[mat] = 0.0;
+        return;
+    }
+    const int nrounds = (T - 1 + CPR - 1) / CPR;
+    // round r stages channels 1 + r CPR .. (contiguous in MO) into buffer r % 3; an empty group
+    // keeps the group count uniform past the last round
+    auto stage = [&](int r) {
+        if (r < nrounds) {
+            const int t0 = 1 + r * CPR, nc = min(CPR, T - t0);
+            const float* src = MO + ((int64_t)mat * T + t0) * nn;
+            float* dst = Ds[r % 3];
+            for (int q = tid; q < nc * Q; q += 128) {
+                const int cc = q / Q, r4 = q - cc * Q;
+                cp_async16(dst + cc * PP + 4 * r4, src + (int64_t)cc * nn + 4 * r4);
+            }
+        }
+        cp_async_commit();
+    };
+    stage(0);
+    stage(1);
+    for (int e = tid; e < nn; e += 128) {
+        const int k = e / NP, a = e % NP;
+        AT[e] = __ldg(Ainv + (int64_t)mat * nn + a * n + k);
+    }
+    const int c = tid / TPC, tile = tid % TPC, ab = tile / NB, jb = tile % NB;
+    const int partner = (tid & 31 & ~(TPC - 1)) | (jb * NB + ab);      // lane of the transposed tile
+    for (int r = 0; r < nrounds; ++r) {
+        const int t0 = 1 + r * CPR, nc = min(CPR, T - t0);
+        cp_async_wait1();                        // this thread's copies of round r have landed
+        __syncthreads();                         // everyone's; round r - 1's buffer is free again
+        stage(r + 2);
+        const bool on = c < nc;
+        float acc[4][4];
+        #pragma unroll
+        for (int x = 0; x < 4; ++x)
+            #pragma unroll
+            for (int y = 0; y < 4; ++y) acc[x][y] = 0.f;
+        if (on) {
+            const float* dp = Ds[r % 3] + c * PP + 4 * jb;
+            const float* ap = AT + 4 * ab;
+            #pragma unroll
+            for (int k = 0; k < n; ++k) {
+                const float4 av = *reinterpret_cast<const float4*>(ap + k * NP);
+                const float4 dv = *reinterpret_cast<const float4*>(dp + k * NP);
+                const float a4[4] = {av.x, av.y, av.z, av.w}, d4[4] = {dv.x, dv.y, dv.z, dv.w};
+                #pragma unroll
+                for (int x = 0; x < 4; ++x)
+                    #pragma unroll
+                    for (int y = 0; y < 4; ++y) acc[x][y] = fmaf(a4[x], d4[y], acc[x][y]);
+            }
+        }
+        // tr(C^2) part of this tile: sum_xy C[4 ab + x][4 jb + y] C[4 jb + y][4 ab + x], the second
+        // factor being the partner's acc[y][x]
+        float p2 = 0.f;
+        #pragma unroll
+        for (int x = 0; x < 4; ++x)
+            #pragma unroll
+            for (int y = 0; y < 4; ++y) p2 = fmaf(acc[x][y], __shfl_sync(0xffffffffu, acc[y][x], partner), p2);
+        float p1 = ab == jb ? acc[0][0] + acc[1][1] + acc[2][2] + acc[3][3] : 0.f;
+        #pragma unroll
+        for (int o = TPC / 2; o > 0; o >>= 1) {
+            p1 += __shfl_xor_sync(0xffffffffu, p1, o);
+            p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+        }
+        if (on && tile == 0) {
+            tr1[t0 + c] = (double)p1;
+            tr2[t0 + c] = (double)p2;
+        }
+    }
+    __syncthreads();
+    for (int t = 1 + tid; t < T - 1; t += 128) g[(int64_t)mat * 3 * n + (t - 1)] = tr1[t];
+    if (tid < 32) {
+        double sacc = 0.0;
+        for (int t = 1 + tid; t < T - 1; t += 32) sacc += tr2[t];
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+        if (tid == 0) lapdet[mat] = tr1[T - 1] - sacc;
+    }
+}
+
 void launch_det_tangents(const float* MO, const float* Ainv, const double* sign, const Dims& d, int B,
                          double* g, double* lapdet, cudaStream_t s) {
     int nmat = B * d.K;
+    if ((d.n == 4 || d.n == 8 || d.n == 16) && d.T == 3 * d.n + 2 && (((uintptr_t)MO) & 15) == 0 && !g_det_tangents_tile) {
+        auto go = [&](auto kern) { kern<<<nmat, 128, 0, s>>>(MO, Ainv, sign, d.T, g, lapdet); };
+        if (d.n == 4) go(k_det_tangents_pipe<4>);
+        else if (d.n == 8) go(k_det_tangents_pipe<8>);
+        else go(k_det_tangents_pipe<16>);
+        count_launch();
+        return;
+    }
     if (d.n <= 32 && d.T == 3 * d.n + 2) {
         auto go = [&](auto kern) { kern<<<nmat, 128, 0, s>>>(MO, Ainv, sign, d.n, d.T, g, lapdet); };
         if (d.n <= 4) go(k_det_tangents_tile<4>);
@@ -1223,5 +1340,14 @@ int dw_debug_slogdet_small(const float* MO, int n, int T, int nmat, int scalar, 
     if (scalar == 0) dw::launch_slogdet_small<double>(MO, n, T, nmat, logdet, sign, Ainv, want_inv != 0, s);
     else dw::launch_slogdet_small<dw::FF>(MO, n, T, nmat, logdet, sign, Ainv, want_inv != 0, s);
     return cudaGetLastError() == cudaSuccess ? DW_OK : DW_ERR_CUDA;
+}
+
+// Instrumentation: determinant-tangent kernel for n in {4, 8, 16} (0: the pipelined kernel, the
+// default; 1: the single-buffer tile kernel). Returns the previous choice.
+int dw_debug_set_det_tangents_kernel(int which) {
+    if (which != 0 && which != 1) return -DW_ERR_ARG;
+    const int old = dw::g_det_tangents_tile ? 1 : 0;
+    dw::g_det_tangents_tile = which == 1;
+    return old;
 }
 }  // extern "C"

@@ -25,10 +25,14 @@ __device__ unsigned long long g_guard_cnt[2][3];
 // kernel cancels (the determinant terms of the Laplacian of log|psi~|, or the terms of E_L). On
 // C2H4-shaped walkers (16 electrons, 32 determinants) the measured |E_mixed - E_FP64| / that
 // magnitude has median 1.7e-6 and 99th percentile 1.5e-5 (2e-5 to 5e-5 after optimisation steps).
-// Walkers predicted above kGuardTol (magnitude above 2,000 Ha) are re-evaluated, those of the
-// largest magnitudes first when more than the capacity (1 / 32 of the batch) are flagged.
+// Walkers predicted above kGuardTol (magnitude above 1,000 Ha) are re-evaluated, those of the
+// largest magnitudes first when more than the capacity (1 / 32 of the batch) are flagged. The
+// capacity is re-evaluated every call whatever the count, so a lower threshold costs nothing while
+// the flagged walkers fit: on eleven C2H4 states (initial weights, the end of the optimisation
+// bench) lowering it from 2,000 to 1,000 Ha moved the worst batch-mean error from -0.58 to
+// -0.38 mHa; below 1,000 Ha nothing changed further.
 constexpr float kGuardRel = 1.5e-5f;
-constexpr float kGuardTol = 0.03f;
+constexpr float kGuardTol = 0.015f;
 // Re-evaluation form: the plain FP32 network with FP64 determinant algebra (LU, inverse, tangent
 // traces). The catastrophic errors of ill-conditioned walkers come from the determinant algebra:
 // on 4,096 C2H4-shaped walkers near the initial weights the plain FP32 form is off by up to 14 Ha,

@@ -61,7 +61,7 @@ def _equilibrated(mol, K, B, steps, seed=0):
     return a, prm, st
 
 
-THRESHOLD = 2000.0      # re-evaluation above this cancelled magnitude (kGuardTol / kGuardRel)
+THRESHOLD = 1000.0      # re-evaluation above this cancelled magnitude (kGuardTol / kGuardRel)
 FP64_KEY = 1.0e5        # FP64-form re-evaluation above this cancelled magnitude (kGuardFp64Key)
 
 

@@ -262,6 +262,10 @@ def run_ours(args, rank, world, dev):
     ms, E_mixed, clocks, kt, n_launch = timed(params, args.steps, args.warmup, sample_clocks=True, instrument=True)
     gs = guard_stats(True)
     value = world * B / (ms / 1e3)
+    # the chain's own state at the end of the timed steps: its walkers and the weights they were
+    # equilibrated for (the end-to-end leg below restarts every step from one host copy of them)
+    r_chain = state.r.clone()
+    params_chain = api.Params(a, params.flat.clone(), w.precision)
 
     # end to end through the public API with host buffers: H2D of the walkers, D2H of E_L
     r_host = state.r.detach().cpu().pin_memory()
@@ -287,7 +291,8 @@ def run_ours(args, rank, world, dev):
     e2e = {"value": world * B / (ms_e2e / 1e3), "unit": "walker-evals/s",
            "h2d_bytes_per_step": int(r_host.numel() * 4), "d2h_bytes_per_step": int(B * 4)}
 
-    # walkers of the mixed chain at its current weights (the plain leg below moves the shared chain)
+    # walkers of the end-to-end leg at the weights the run ends with (the plain leg below moves
+    # the shared chain)
     r_mixed = state.r.clone()
     plain = None
     if not args.no_plain and w.precision != "fp32":
@@ -297,9 +302,9 @@ def run_ours(args, rank, world, dev):
         ms_p, E_plain, _, _, _ = timed(pparams, kp, 1)
         # same walkers and weights through both forms: accuracy of the mixed form against plain
         # FP32 on the full batch
-        pcmp = params.with_precision("fp32") if w.backward else pparams
-        E_m = api.local_energy(params, spin, r_mixed, state.R, state.Z).double()
-        E_p = api.local_energy(pcmp, spin, r_mixed, state.R, state.Z).double()
+        pcmp = params_chain.with_precision("fp32")
+        E_m = api.local_energy(params_chain, spin, r_chain, state.R, state.Z).double()
+        E_p = api.local_energy(pcmp, spin, r_chain, state.R, state.Z).double()
         d = (E_m - E_p)
         ad = d.abs().cpu().numpy() * 1e3
         plain = {"value": world * B / (ms_p / 1e3), "ms_per_step": ms_p,
@@ -358,7 +363,7 @@ def run_ours(args, rank, world, dev):
             # above the tolerance and which were re-evaluated inside the mixed form: with FP64
             # determinant algebra, and (cancelled magnitude above 1e5 Ha) by the FP64 form
             out["tail_reevaluation"] = gs
-    return out, (state, params, a, mol, w, r_mixed, breakdown)
+    return out, (state, params, a, mol, w, r_mixed, breakdown, r_chain, params_chain)
 
 
 def ours_config(w, mol, a, B, world):
@@ -512,14 +517,22 @@ def main():
     if rank == 0:
         from deeperwin_gb300 import params as P
         from deeperwin_gb300 import api
-        state, params, a, mol, w, r_mixed, breakdown = ctx
+        state, params, a, mol, w, r_mixed, breakdown, r_chain, params_chain = ctx
         # the checks evaluate the weights the GPU holds now (updated ones after optimisation steps)
         p_now = P.unpack(a, params.flat.detach().cpu().numpy())
         if w.precision != "fp32" and not args.no_plain:
             n64 = args.fp64_walkers or (1024 if a.n_el > 30 else state.r.shape[0])
-            out["accuracy_vs_fp64"] = accuracy_vs_fp64(a, mol, r_mixed, state, params, min(n64, state.r.shape[0]), p_now)
-            out["accuracy_vs_fp64"]["state"] = ("the mixed chain's walkers and weights at the end of the run "
-                                                "(after the warm-up, timed and end-to-end optimisation steps)")
+            n64 = min(n64, state.r.shape[0])
+            p_chain = P.unpack(a, params_chain.flat.detach().cpu().numpy())
+            out["accuracy_vs_fp64"] = accuracy_vs_fp64(a, mol, r_chain, state, params_chain, n64, p_chain)
+            out["accuracy_vs_fp64"]["state"] = ("the mixed chain's walkers and weights at the end of the timed "
+                                                "optimisation steps")
+            # stress case: the end-to-end leg restarts every step from one host copy of the walkers
+            # while the weights keep changing, so its final walkers sit closer to the new nodes
+            out["accuracy_vs_fp64_restarted_walkers"] = accuracy_vs_fp64(a, mol, r_mixed, state, params, n64, p_now)
+            out["accuracy_vs_fp64_restarted_walkers"]["state"] = (
+                "the end-to-end leg's walkers (restarted every step from the walkers of the timed chain, 10 "
+                "Metropolis-Hastings steps under weights that moved by up to 6 more Adam steps) at the final weights")
             # the same comparison at the random-init weights, on a chain equilibrated by 30 steps
             p0 = P.init_params(a, seed=0)
             params0 = api.Params.from_dict(a, p0, w.precision)

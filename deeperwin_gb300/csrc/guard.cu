@@ -27,8 +27,8 @@ __device__ unsigned long long g_guard_cnt[2][3];
 // magnitude has median 1.7e-6 and 99th percentile 1.5e-5 (2e-5 to 5e-5 after optimisation steps).
 // Walkers predicted above kGuardTol (magnitude above 1,000 Ha) are re-evaluated, those of the
 // largest magnitudes first when more than the capacity (1 / 32 of the batch) are flagged. The
-// capacity is re-evaluated every call whatever the count, so a lower threshold costs nothing while
-// the flagged walkers fit: on eleven C2H4 states (initial weights, the end of the optimisation
+// whole capacity is re-evaluated every call whatever the count, so a lower threshold costs nothing
+// while the flagged walkers fit: on eleven C2H4 states (initial weights, the end of the optimisation
 // bench) lowering it from 2,000 to 1,000 Ha moved the worst batch-mean error from -0.58 to
 // -0.38 mHa; below 1,000 Ha nothing changed further.
 constexpr float kGuardRel = 1.5e-5f;
@@ -39,7 +39,7 @@ constexpr float kGuardTol = 0.015f;
 // the same network with FP64 determinants by at most 95 mHa (mean 0.03 mHa), at about 1.5x the
 // plain form's cost per walker. The FP64 form (fp64.cu) would cost about 15x more per walker.
 // Second tier: walkers whose cancelled magnitude exceeds kGuardFp64Key Ha. At the end of the C2H4
-// optimisation bench (random-init weights after 14 Adam steps) 8-23 of 4,096 walkers exceed it; the
+// optimisation bench (random-init weights after 14 Adam steps) 4-37 of 4,096 walkers exceed it; the
 // FP32 network with FP64 determinants is off by 0.1-4 Ha on those between 1e5 and 1e7 and by up to
 // 57 kHa on the few beyond 1e8 (|E_L| up to 1.4e5 Ha), where only an FP64 network resolves the node.
 constexpr float kGuardFp64Key = 1.0e5f;

@@ -1418,9 +1418,12 @@ void launch_conv(const float* r, const float* WPl, const float* HM, const float*
 // stay in registers across all rows of the block; per (electron, ion) the difference vector,
 // distance and inverse distance are formed once in shared memory (a negative distance marks a
 // padding ion of a packed geometry). Same mathematics as k_envelope.
+// NI bounds the ions held in registers; with NI = 8 four blocks fit an SM, which doubles the loads
+// in flight of this memory-bound kernel.
 constexpr int kEnvWG = 4;
 constexpr int kEnvMaxIons = 16;
-__global__ void __launch_bounds__(256)
+template <int NI>
+__global__ void __launch_bounds__(256, NI <= 8 ? 4 : 2)
 k_envelope_rows(const float* __restrict__ r, const float* __restrict__ Rall, const int32_t* __restrict__ Zall,
                 const float* __restrict__ P, ParamLayout L, const float* __restrict__ spA, Dims d, int B,
                 const float* __restrict__ BF, int ldbf, int spin_cols, float* __restrict__ MO) {
@@ -1448,9 +1451,9 @@ k_envelope_rows(const float* __restrict__ r, const float* __restrict__ Rall, con
     if (col >= d.KN) return;
     const float* spa = spA + (spin ? (size_t)N * d.KN : 0);   // softplus(alpha), prepared
     const float* wts = P + (spin ? L.weights_dn : L.weights_up);
-    float av[kEnvMaxIons], wv[kEnvMaxIons];
+    float av[NI], wv[NI];
     #pragma unroll
-    for (int I = 0; I < kEnvMaxIons; ++I) {
+    for (int I = 0; I < NI; ++I) {
         av[I] = I < N ? __ldg(spa + (size_t)I * d.KN + col) : 0.f;
         wv[I] = I < N ? __ldg(wts + (size_t)I * d.KN + col) : 0.f;
     }
@@ -1472,7 +1475,7 @@ k_envelope_rows(const float* __restrict__ r, const float* __restrict__ Rall, con
                 const float* gv = se + (size_t)min(r4 + u, rows - 1) * N * 5;
                 float env = 0.f;
                 #pragma unroll
-                for (int I = 0; I < kEnvMaxIons; ++I) {
+                for (int I = 0; I < NI; ++I) {
                     if (I >= N) break;
                     const float dd = gv[I * 5 + 3];
                     if (dd < 0.f) continue;                  // padding ion
@@ -1494,7 +1497,7 @@ k_envelope_rows(const float* __restrict__ r, const float* __restrict__ Rall, con
         const float* gv = se + (size_t)rr * N * 5;
         float env = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, lapv = 0.f;
         #pragma unroll
-        for (int I = 0; I < kEnvMaxIons; ++I) {
+        for (int I = 0; I < NI; ++I) {
             if (I >= N) break;
             const float dd = gv[I * 5 + 3];
             if (dd < 0.f) continue;                          // padding ion
@@ -1536,7 +1539,8 @@ void launch_envelope(const float* r, const float* R, const int32_t* Z, const flo
         const int ns_max = std::max(d.nu, d.nd);
         const size_t sm = (size_t)kEnvWG * ns_max * d.N * 5 * sizeof(float);
         dim3 grid((unsigned)((B + kEnvWG - 1) / kEnvWG), (unsigned)((d.KN + threads - 1) / threads), d.nd > 0 ? 2 : 1);
-        k_envelope_rows<<<grid, threads, sm, s>>>(r, R, Z, P, L, sp_alpha, d, B, BF, ldbf, spin_cols, MO);
+        if (d.N <= 8) k_envelope_rows<8><<<grid, threads, sm, s>>>(r, R, Z, P, L, sp_alpha, d, B, BF, ldbf, spin_cols, MO);
+        else k_envelope_rows<16><<<grid, threads, sm, s>>>(r, R, Z, P, L, sp_alpha, d, B, BF, ldbf, spin_cols, MO);
         count_launch();
         return;
     }

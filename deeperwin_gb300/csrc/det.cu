@@ -898,7 +898,8 @@ k_det_tangents_warp(const float* __restrict__ MO, const float* __restrict__ Ainv
 // transposed tile for its part of tr(C_t^2). A channel's traces are FP32 sums of products of
 // FP32 entries (as C_t itself is FP32), formed from the tile partials by one lane per channel;
 // the traces of all channels are accumulated in FP64 into
-// lap = tr(A^-1 Lap A) - sum_t tr(C_t^2). Matrices are zero-padded to NP = round_up(n, 4) <= 32.
+// lap = tr(A^-1 Lap A) - sum_t tr(C_t^2). Matrices are zero-padded to NP = round_up(n, 4) for n <= 32
+// and to 40 for n = 33..40 (a channel's 100 tiles then leave 28 of the 128 threads idle).
 template <int NP>
 __global__ void __launch_bounds__(128)
 k_det_tangents_tile(const float* __restrict__ MO, const float* __restrict__ Ainv, const double* __restrict__ sign,
@@ -910,7 +911,7 @@ k_det_tangents_tile(const float* __restrict__ MO, const float* __restrict__ Ainv
     __shared__ __align__(16) float AT[NP * NP];  // AT[k][a] = Ainv[a][k]
     __shared__ __align__(16) float Ds[CPR * PP];
     __shared__ float part[2][128];
-    __shared__ double tr1[3 * 32 + 2], tr2[3 * 32 + 2];
+    __shared__ double tr1[3 * NP + 2], tr2[3 * NP + 2];
     const int mat = blockIdx.x, tid = threadIdx.x;
     if (sign[mat] == 0.0) {
         for (int t = tid; t < 3 * n; t += 128) g[(int64_t)mat * 3 * n + t] = 0.0;
@@ -1136,7 +1137,7 @@ void launch_det_tangents(const float* MO, const float* Ainv, const double* sign,
         count_launch();
         return;
     }
-    if (d.n <= 32 && d.T == 3 * d.n + 2) {
+    if ((d.n <= 32 || (d.n <= 40 && !g_det_tangents_tile)) && d.T == 3 * d.n + 2) {
         auto go = [&](auto kern) { kern<<<nmat, 128, 0, s>>>(MO, Ainv, sign, d.n, d.T, g, lapdet); };
         if (d.n <= 4) go(k_det_tangents_tile<4>);
         else if (d.n <= 8) go(k_det_tangents_tile<8>);
@@ -1145,7 +1146,8 @@ void launch_det_tangents(const float* MO, const float* Ainv, const double* sign,
         else if (d.n <= 20) go(k_det_tangents_tile<20>);
         else if (d.n <= 24) go(k_det_tangents_tile<24>);
         else if (d.n <= 28) go(k_det_tangents_tile<28>);
-        else go(k_det_tangents_tile<32>);
+        else if (d.n <= 32) go(k_det_tangents_tile<32>);
+        else go(k_det_tangents_tile<40>);
         count_launch();
         return;
     }
@@ -1342,8 +1344,9 @@ int dw_debug_slogdet_small(const float* MO, int n, int T, int nmat, int scalar, 
     return cudaGetLastError() == cudaSuccess ? DW_OK : DW_ERR_CUDA;
 }
 
-// Instrumentation: determinant-tangent kernel for n in {4, 8, 16} (0: the pipelined kernel, the
-// default; 1: the single-buffer tile kernel). Returns the previous choice.
+// Instrumentation: determinant-tangent kernels (0: the default choice; 1: the single-buffer tile
+// kernel for n in {4, 8, 16} instead of the pipelined one, and the general kernel instead of the
+// tile kernel for n = 33..40). Returns the previous choice.
 int dw_debug_set_det_tangents_kernel(int which) {
     if (which != 0 && which != 1) return -DW_ERR_ARG;
     const int old = dw::g_det_tangents_tile ? 1 : 0;

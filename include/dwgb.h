@@ -268,9 +268,10 @@ size_t dw_noalloc_scratch_bytes(void);
 int dw_guard_tier_stats(int tier, int64_t* walkers, int64_t* flagged, int64_t* overflow, int reset);
 int dw_guard_stats(int64_t* walkers, int64_t* flagged, int64_t* overflow, int reset);
 
-/* Instrumentation: determinant-tangent kernel for n_el in {4, 8, 16}: 0 = the pipelined kernel
- * (default), 1 = the single-buffer tile kernel used for the other sizes. Returns the previous
- * choice, or -DW_ERR_ARG. No reference counterpart. */
+/* Instrumentation: determinant-tangent kernels. 0 = the default choice; 1 = the single-buffer
+ * tile kernel instead of the pipelined one for n_el in {4, 8, 16} and the general kernel instead
+ * of the tile kernel for n_el in 33..40. Returns the previous choice, or -DW_ERR_ARG. No
+ * reference counterpart. */
 int dw_debug_set_det_tangents_kernel(int which);
 
 /* Instrumentation: network of the tier-0 re-evaluation, DW_PRECISION_FP32_DET64 (default) or

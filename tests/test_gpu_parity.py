@@ -447,16 +447,18 @@ def test_split_gemm_stage_depths_agree_on_local_energy(cuda, le_cases):
     assert np.all(np.abs(out[32] - out[64]) <= 1e-6 * S + 1e-5), (out[32], out[64])
 
 
-@pytest.mark.parametrize("mol_name,K,B", [("lih", 8, 64), ("c2h4", 32, 96), ("h4", 4, 40)])
+@pytest.mark.parametrize("mol_name,K,B", [("lih", 8, 64), ("c2h4", 32, 96), ("h4", 4, 40), ("s40", 4, 8)])
 def test_det_tangent_kernels_agree(cuda, mol_name, K, B):
-    """The pipelined determinant-tangent kernel (n in {4, 8, 16}) and the single-buffer tile kernel
-    form the same FP32 products and sum a channel's partial traces in another order: plain and
-    mixed local energies (without the tail re-evaluation, whose selection could flip) agree to
-    2e-6 of the magnitude the kinetic term cancels."""
+    """The pipelined determinant-tangent kernel (n in {4, 8, 16}) against the single-buffer tile
+    kernel, and the tile kernel (n = 33..40, padded to 40) against the general kernel: the same FP32
+    products with the traces summed in another order, so plain and mixed local energies (without the
+    tail re-evaluation, whose selection could flip) agree to 2e-6 of the magnitude the kinetic term
+    cancels; at n = 40 the general kernel sums each channel's 1,600 products of tr(C_t^2) in FP64 and
+    the tile kernel in FP32 partials (measured up to 4.1e-6 of that magnitude apart), bound 1e-5."""
     import ctypes
     from deeperwin_gb300 import _lib
     L = _lib.lib()
-    mol = {"lih": A.lih(), "c2h4": A.c2h4_shaped(), "h4": A.h_chain(4)}[mol_name]
+    mol = {"lih": A.lih(), "c2h4": A.c2h4_shaped(), "h4": A.h_chain(4), "s40": A.scale_molecule(7)}[mol_name]
     a = A.arch_for(mol, K)
     p = P.init_params(a, 6, bias_std=0.1, envelope_jitter=0.2)
     rt = torch.as_tensor(A.init_walkers(mol, B, seed=4).astype(np.float32), device="cuda")
@@ -480,7 +482,8 @@ def test_det_tangent_kernels_agree(cuda, mol_name, K, B):
             finally:
                 L.dw_debug_set_det_tangents_kernel(prev)
             out[which] = (E.double().cpu().numpy(), sc.double().cpu().numpy()[:, :2].max(axis=1), lp.cpu().numpy())
-        assert np.all(np.abs(out[0][0] - out[1][0]) <= 2e-6 * out[1][1] + 1e-6), (prec, np.abs(out[0][0] - out[1][0]) / out[1][1])
+        tol = 1e-5 if a.n_el > 32 else 2e-6
+        assert np.all(np.abs(out[0][0] - out[1][0]) <= tol * out[1][1] + 1e-6), (prec, np.abs(out[0][0] - out[1][0]) / out[1][1])
         np.testing.assert_array_equal(out[0][2], out[1][2])      # log psi^2 does not involve the tangents
 
 

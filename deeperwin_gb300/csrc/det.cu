@@ -143,6 +143,162 @@ __global__ void k_slogdet(const float* __restrict__ MO, int n, int T, int nmat, 
     }
 }
 
+// Value-mode log|det| for 32 < n <= 64: warp per matrix, the matrix in shared memory (row pitch
+// n + 1), LU with partial pivoting (first row of maximal |a|, as LAPACK getrf). Each step scales
+// the L column and then spreads the (n - k - 1)^2 elements of the trailing update over all 32
+// lanes in row-major order, so the lanes stay busy as the trailing block shrinks (the row-at-a-
+// time form of k_slogdet leaves most lanes idle once fewer than 32 columns remain). Rows are
+// exchanged from the pivot column on (the L factors are not needed for the determinant); the
+// pivot magnitudes accumulate as a normalised mantissa and a binary exponent, one log per matrix.
+__device__ __forceinline__ long long wide_key(double v) { return __double_as_longlong(v) & 0x7fffffffffffffffll; }
+__device__ __forceinline__ long long wide_key(float v) { return (long long)(__float_as_int(v) & 0x7fffffff); }
+__device__ __forceinline__ double wide_fnma(double l, double u, double a) { return fma(-l, u, a); }
+__device__ __forceinline__ float wide_fnma(float l, float u, float a) { return fmaf(-l, u, a); }
+
+template <class S>
+__global__ void __launch_bounds__(256)
+k_slogdet_wide(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
+               double* __restrict__ sign) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    const int mat = blockIdx.x * wpb + wid;
+    if (mat >= nmat) return;                              // the whole warp
+    const int ld = n + 1;
+    S* M = reinterpret_cast<S*>(smem_raw) + (size_t)wid * n * ld;
+    const float* A = MO + (int64_t)mat * T * n * n;       // channel 0 of this (walker, det)
+    for (int e = lane; e < n * n; e += 32) {
+        const int r = e / n, c = e - r * n;
+        M[r * ld + c] = (S)__ldg(A + e);
+    }
+    __syncwarp();
+    double mant = 1.0, sg = 1.0;
+    int expo = 0;
+    bool singular = false;
+    for (int k = 0; k < n; ++k) {
+        long long best = -1;
+        int p = n;
+        for (int r = k + lane; r < n; r += 32) {
+            const long long v = wide_key(M[r * ld + k]);
+            if (v > best) { best = v; p = r; }
+        }
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int op = __shfl_xor_sync(0xffffffffu, p, o);
+            if (ob > best || (ob == best && op < p)) { best = ob; p = op; }
+        }
+        if (best <= 0) { singular = true; break; }        // the same in every lane
+        if (p != k) {
+            for (int j = k + lane; j < n; j += 32) {
+                const S t = M[k * ld + j]; M[k * ld + j] = M[p * ld + j]; M[p * ld + j] = t;
+            }
+            sg = -sg;
+            __syncwarp();
+        }
+        const S piv = M[k * ld + k];
+        if (piv < (S)0) sg = -sg;
+        mant = mant_mul_norm(mant, fabs((double)piv), expo);
+        const S rp = recip_nr(piv);
+        for (int r = k + 1 + lane; r < n; r += 32) M[r * ld + k] *= rp;
+        __syncwarp();
+        const int m = n - k - 1;
+        if (m > 0) {
+            // element e = lane + 32 s of the m x m trailing block: row e / m, column e % m,
+            // advanced by 32 = dr m + dc with a carry instead of a division per element
+            int r = lane / m, c = lane - r * m;
+            const int dr = 32 / m, dc = 32 - dr * m;
+            for (int e = lane; e < m * m; e += 32) {
+                S* row = M + (k + 1 + r) * ld;
+                row[k + 1 + c] = wide_fnma(row[k], M[k * ld + k + 1 + c], row[k + 1 + c]);
+                r += dr;
+                c += dc;
+                if (c >= m) { c -= m; ++r; }
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        logdet[mat] = singular ? -INFINITY : log(mant) + (double)expo * 0.69314718055994530942;
+        sign[mat] = singular ? 0.0 : sg;
+    }
+}
+
+// log|det| and the inverse for 32 < n <= 64: Gauss-Jordan elimination on [A | I] with partial
+// pivoting, warp per matrix in shared memory (row pitch 2n + 1). At step k the columns left of k
+// of the A half are unit vectors and are neither stored nor touched: the pivot row is scaled on
+// the columns right of k and every other row is updated there, the (n - 1)(2n - k - 1) elements
+// spread over all 32 lanes. The right half ends as A^-1 (row exchanges act on both halves).
+template <class S>
+__global__ void __launch_bounds__(256)
+k_slogdet_wide_inv(const float* __restrict__ MO, int n, int T, int nmat, double* __restrict__ logdet,
+                   double* __restrict__ sign, float* __restrict__ Ainv) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    const int mat = blockIdx.x * wpb + wid;
+    if (mat >= nmat) return;                              // the whole warp
+    const int nc = 2 * n, ld = nc + 1;
+    S* M = reinterpret_cast<S*>(smem_raw) + (size_t)wid * n * ld;
+    const float* A = MO + (int64_t)mat * T * n * n;
+    for (int e = lane; e < n * nc; e += 32) {
+        const int r = e / nc, c = e - r * nc;
+        M[r * ld + c] = c < n ? (S)__ldg(A + r * n + c) : (S)((c - n) == r ? 1 : 0);
+    }
+    __syncwarp();
+    double mant = 1.0, sg = 1.0;
+    int expo = 0;
+    bool singular = false;
+    for (int k = 0; k < n; ++k) {
+        long long best = -1;
+        int p = n;
+        for (int r = k + lane; r < n; r += 32) {
+            const long long v = wide_key(M[r * ld + k]);
+            if (v > best) { best = v; p = r; }
+        }
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int op = __shfl_xor_sync(0xffffffffu, p, o);
+            if (ob > best || (ob == best && op < p)) { best = ob; p = op; }
+        }
+        if (best <= 0) { singular = true; break; }        // the same in every lane
+        if (p != k) {
+            for (int j = k + lane; j < nc; j += 32) {
+                const S t = M[k * ld + j]; M[k * ld + j] = M[p * ld + j]; M[p * ld + j] = t;
+            }
+            sg = -sg;
+            __syncwarp();
+        }
+        const S piv = M[k * ld + k];
+        if (piv < (S)0) sg = -sg;
+        mant = mant_mul_norm(mant, fabs((double)piv), expo);
+        const S rp = recip_nr(piv);
+        for (int j = k + 1 + lane; j < nc; j += 32) M[k * ld + j] *= rp;
+        __syncwarp();
+        const int w = nc - k - 1;                         // columns right of k
+        // element e = lane + 32 s: row q = e / w of the n - 1 other rows, column e % w
+        int q = lane / w, c = lane - q * w;
+        const int dq = 32 / w, dc = 32 - dq * w;
+        for (int e = lane; e < (n - 1) * w; e += 32) {
+            const int r = q < k ? q : q + 1;
+            S* row = M + r * ld;
+            row[k + 1 + c] = wide_fnma(row[k], M[k * ld + k + 1 + c], row[k + 1 + c]);
+            q += dq;
+            c += dc;
+            if (c >= w) { c -= w; ++q; }
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        logdet[mat] = singular ? -INFINITY : log(mant) + (double)expo * 0.69314718055994530942;
+        sign[mat] = singular ? 0.0 : sg;
+    }
+    float* out = Ainv + (int64_t)mat * n * n;
+    for (int e = lane; e < n * n; e += 32) {
+        const int r = e / n, c = e - r * n;
+        out[e] = singular ? 0.f : (float)M[r * ld + n + c];
+    }
+}
+
 // Register-resident variant for n <= NMAX <= 32: a team of n lanes per matrix (32 / n
 // matrices per warp), lane c owning column c of A (and of the identity block when INV).
 // Partial pivoting: the owner of the pivot column finds the first row of maximal |a| at or
@@ -754,6 +910,27 @@ void launch_slogdet_impl(const float* MO, const Dims& d, int B, double* logdet, 
         else if (n <= 16) { if (want_inv) go(k_slogdet_reg<S, 16, true>); else go(k_slogdet_reg<S, 16, false>); }
         else if (n <= 24) { if (want_inv) go(k_slogdet_reg<S, 24, true>); else go(k_slogdet_reg<S, 24, false>); }
         else { if (want_inv) go(k_slogdet_reg<S, 32, true>); else go(k_slogdet_reg<S, 32, false>); }
+        count_launch();
+        return;
+    }
+    if (!want_inv && n <= 64) {
+        const size_t per = (size_t)n * (n + 1) * sizeof(S);
+        int wpb = (int)(96 * 1024 / per);
+        wpb = wpb < 1 ? 1 : (wpb > 8 ? 8 : wpb);
+        const size_t sm = per * wpb;
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k_slogdet_wide<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_slogdet_wide<S><<<(nmat + wpb - 1) / wpb, wpb * 32, sm, s>>>(MO, n, d.T, nmat, logdet, sign);
+        count_launch();
+        return;
+    }
+    if (want_inv && n <= 64) {
+        const size_t per = (size_t)n * (2 * n + 1) * sizeof(S);
+        int wpb = (int)(96 * 1024 / per);
+        wpb = wpb < 1 ? 1 : (wpb > 8 ? 8 : wpb);
+        const size_t sm = per * wpb;
+        if (sm > 48 * 1024)
+            cudaFuncSetAttribute(k_slogdet_wide_inv<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_slogdet_wide_inv<S><<<(nmat + wpb - 1) / wpb, wpb * 32, sm, s>>>(MO, n, d.T, nmat, logdet, sign, Ainv);
         count_launch();
         return;
     }

@@ -354,7 +354,7 @@ def test_local_energy_many_channels(cuda, name):
 
 def _count_case(n_el, K, seed):
     """A molecule with n_el electrons: an H chain up to 16 atoms, heavier atoms beyond."""
-    heavy = {18: [8, 8, 1, 1], 21: [8, 7, 6], 26: [8, 8, 8, 1, 1]}
+    heavy = {18: [8, 8, 1, 1], 21: [8, 7, 6], 26: [8, 8, 8, 1, 1], 34: [8, 8, 8, 8, 1, 1], 40: [8, 8, 8, 8, 6, 1, 1]}
     if n_el <= 16:
         mol = A.h_chain(n_el, 1.6)
     else:
@@ -387,7 +387,7 @@ def _slater_condition(p, a, r, mol):
 # split-BF16 GEMM entries: hi + lo represents each operand to about 2^-17, and sums of 256
 # products cancel). Random-init Slater matrices of the heavier atoms reach kappa ~ 1e6.
 @pytest.mark.parametrize("n_el,K", [(3, 2), (5, 3), (7, 2), (9, 4), (11, 2), (12, 3), (13, 2), (14, 4), (15, 2),
-                                    (18, 2), (21, 1), (26, 1)])
+                                    (18, 2), (21, 1), (26, 1), (34, 2), (40, 2)])
 def test_log_psi_across_electron_counts(cuda, n_el, K):
     mol, a, p, r = _count_case(n_el, K, n_el)
     lp_ref = O.log_psi_sqr(O.tparams(p), a, r, mol.R, mol.Z)[1].numpy()
